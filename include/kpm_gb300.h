@@ -1,0 +1,216 @@
+/*
+ * kpm_gb300.h -- C ABI of the GB300 kernel polynomial method (KPM) engine.
+ *
+ * A drop-in compute backend for pybinding's KPM path. Every entry point takes
+ * plain pointers and sizes; all arrays are HOST memory unless a parameter says
+ * otherwise. Each call returns KPM_OK (0) or an error code; the message of the
+ * last error on the calling thread is returned by kpm_last_error().
+ *
+ * The engine owns its device memory and one CUDA stream; calls on the same
+ * engine must be serialised by the caller (the reference serialises them with
+ * the GIL / one KPM object per thread). All device waits are bounded.
+ *
+ * Scalar types follow pybinding's Hamiltonian variants (float32, float64,
+ * complex64, complex128; hamiltonian/Hamiltonian.hpp:48-66). Complex arrays
+ * are interleaved (re, im) pairs of the real type. Hamiltonian indices are
+ * int32, as in the reference (detail/config.hpp:16).
+ */
+#ifndef KPM_GB300_H
+#define KPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define KPM_OK 0
+#define KPM_ERR_RUNTIME 1     /* std::runtime_error / logic_error -> Python RuntimeError */
+#define KPM_ERR_VALUE 2       /* std::invalid_argument -> Python ValueError */
+#define KPM_ERR_CUDA 3        /* a CUDA call failed */
+#define KPM_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+
+/* scalar types */
+#define KPM_F32 0
+#define KPM_F64 1
+#define KPM_C64 2
+#define KPM_C128 3
+
+/* damping kernels, kpm/Kernel.cpp:6-50 */
+#define KPM_KERNEL_JACKSON 0
+#define KPM_KERNEL_LORENTZ 1
+#define KPM_KERNEL_DIRICHLET 2
+
+/* recursion precision */
+#define KPM_PREC_AUTO 0   /* f32/c64 H: FP32 vectors + FP64 moment sums; f64/c128 H: FP64 */
+#define KPM_PREC_FP64 1   /* FP64 (f64 or c128) vectors, values and sums */
+#define KPM_PREC_FP32 2   /* FP32 (f32 or c64) vectors and values, FP64 moment sums */
+
+/* matrix formats accepted for API compatibility (kpm/Config.hpp:7) */
+#define KPM_FORMAT_CSR 0
+#define KPM_FORMAT_ELL 1
+
+/* KPM configuration: kpm::Config (kpm/Config.hpp:23-33) plus GPU knobs. */
+typedef struct kpm_config {
+    double min_energy;        /* equal min/max -> bounds found by Lanczos */
+    double max_energy;
+    int32_t kernel;           /* KPM_KERNEL_* */
+    double kernel_param;      /* lambda of the Lorentz kernel */
+    int32_t matrix_format;    /* KPM_FORMAT_*; the device always uses padded ELL */
+    int32_t optimal_size;     /* AlgorithmConfig::optimal_size */
+    int32_t interleaved;      /* AlgorithmConfig::interleaved */
+    double lanczos_precision; /* percent, default 0.002 */
+    int32_t precision;        /* KPM_PREC_* */
+    int32_t batch_width;      /* vectors per recursion block; 0 = autotuned */
+} kpm_config;
+
+/* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */
+typedef struct kpm_stats {
+    int64_t num_moments;
+    int32_t uses_full_system;
+    int64_t nnz;              /* matrix non-zeros over all steps */
+    int64_t opt_nnz;
+    int64_t vec;
+    int64_t opt_vec;
+    double multiplier;        /* vectors processed */
+    int64_t matrix_memory;    /* bytes of the device matrix */
+    int64_t vector_memory;    /* bytes of one KPM vector */
+    double hamiltonian_time;  /* seconds: reorder + upload */
+    double moments_time;      /* seconds: device time of the recursion */
+    double bounds_time;       /* seconds: Lanczos */
+    int32_t lanczos_loops;
+    double eps;               /* opt_nnz * multiplier / moments_time */
+} kpm_stats;
+
+typedef struct kpm_engine kpm_engine;
+
+/* Message of the last failed call on this thread (empty string if none). */
+const char* kpm_last_error(void);
+
+/* Fill *cfg with the reference defaults (kpm/Config.hpp:23-33). */
+void kpm_config_default(kpm_config* cfg);
+
+/*
+ * Create an engine for one Hamiltonian, or for a ragged batch of independent
+ * Hamiltonians stored as one block-diagonal CSR (num_systems blocks whose first
+ * rows are system_offsets[0..num_systems], system_offsets[num_systems] == rows).
+ * Replaces cpb::KPM::KPM / kpm::Core::Core (cppcore/src/KPM.cpp:7-8,
+ * cppcore/src/kpm/Core.cpp:17-23): copies the CSR, checks it (sorted, in
+ * range, finite: hamiltonian/Hamiltonian.hpp:133-140), and raises
+ * "KPM: Invalid energy range specified (min > max)." for min > max.
+ */
+int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const int32_t* indices,
+               const void* values, int32_t num_systems, const int64_t* system_offsets,
+               const kpm_config* cfg, kpm_engine** out);
+
+/* Release the engine and its device memory. */
+int kpm_destroy(kpm_engine* engine);
+
+/* Replace the Hamiltonian (same shape rules as kpm_create). cpb::KPM::set_model
+ * (cppcore/src/KPM.cpp:10-13) / Core::set_hamiltonian (Core.cpp:25-29). */
+int kpm_set_hamiltonian(kpm_engine* engine, int32_t scalar_type, int64_t rows, const int32_t* indptr,
+                        const int32_t* indices, const void* values, int32_t num_systems,
+                        const int64_t* system_offsets);
+
+/* Spectral bounds of one system, by FP64 Lanczos on the GPU unless set in the
+ * config. kpm::Bounds (kpm/Bounds.hpp:39-72, compute/lanczos.hpp:101-154). */
+int kpm_energy_bounds(kpm_engine* engine, int32_t system, double* min_energy, double* max_energy,
+                      int32_t* loops);
+
+/* KPM scaling factors a, b of one system: Bounds::scaling_factors (kpm/Bounds.hpp:57). */
+int kpm_scaling_factors(kpm_engine* engine, int32_t system, double* a, double* b);
+
+/*
+ * Diagonal moments mu_n = <r|T_n(H~)|r> for caller-supplied starters: the hot
+ * path (kpm/default/Compute.cpp:24-88 with kpm/calc_moments.hpp:35-89 and the
+ * collectors of kpm/default/collectors.cpp:6-36), run on the GPU for every
+ * system at once.
+ *   starters: for each system s, num_vectors vectors of length rows_s in the
+ *             ORIGINAL site order, stored [s][vector][site] (the engine's
+ *             scalar type, complex interleaved); the engine reorders them.
+ *   num_moments: rounded up so that (M - 2) % 4 == 0 (kpm/Kernel.hpp:9-13);
+ *             the rounded count is written to *num_moments_out.
+ *   out: per system [s][vector][M] moments, undamped, as complex double
+ *        (2 doubles each) when `average` == 0; [s][M] averaged over the
+ *        vectors (BatchAccumulator, kpm/Moments.cpp:30-48) when `average` != 0.
+ *        out must hold num_systems * (average ? 1 : num_vectors) * M complex.
+ *   starters_on_device: nonzero if `starters` is a device pointer (same layout).
+ */
+int kpm_moments_diag(kpm_engine* engine, int64_t num_moments, int64_t num_vectors, const void* starters,
+                     int32_t starters_on_device, int32_t average, double* out, int64_t* num_moments_out);
+
+/* Stochastic DOS of every system: kpm::Core::dos (cppcore/src/kpm/Core.cpp:74-90)
+ * with the reference's random starters (std::mt19937 default seed per system,
+ * kpm/Starter.cpp:48-84). out: [num_systems][num_energy]. */
+int kpm_calc_dos(kpm_engine* engine, const double* energy, int64_t num_energy, double broadening,
+                 int64_t num_random, double* out);
+
+/* LDOS at Hamiltonian indices (system 0): kpm::Core::ldos (Core.cpp:58-72).
+ * out: column-major [num_indices][num_energy]. */
+int kpm_calc_ldos(kpm_engine* engine, const int64_t* indices, int64_t num_indices, const double* energy,
+                  int64_t num_energy, double broadening, double* out);
+
+/* Green's function elements (row, cols[j]) (system 0): kpm::Core::greens_vector
+ * (Core.cpp:96-117). Indices are checked like cpb::KPM::calc_greens_vector
+ * (KPM.cpp:110-121). out: [num_cols][num_energy] complex. */
+int kpm_calc_greens(kpm_engine* engine, int64_t row, const int64_t* cols, int64_t num_cols,
+                    const double* energy, int64_t num_energy, double broadening, double* out);
+
+/* Moments <beta| op T_n(H) |alpha> (system 0): cpb::KPM::moments (KPM.cpp:19-53) +
+ * kpm::Core::moments (Core.cpp:35-56). alpha/beta are complex double vectors of
+ * the Hamiltonian size (beta may be NULL: beta = alpha); op is an optional
+ * complex double CSR (op_rows == 0 when absent). Damped with the rounded
+ * moment count; out: num_moments complex. Raises the reference's
+ * "Size mismatch ..." and "The model Hamiltonian is real, but the given
+ * argument '...' is complex" errors. */
+int kpm_moments(kpm_engine* engine, int64_t num_moments, const double* alpha, int64_t alpha_size,
+                const double* beta, int64_t beta_size, int64_t op_rows, const int32_t* op_indptr,
+                const int32_t* op_indices, const double* op_values, double* out);
+
+/* Kubo-Bastin conductivity (system 0): kpm::Core::conductivity (Core.cpp:119-150).
+ * left/right: float32 site coordinates of the two directions (KPM.cpp:131-149).
+ * gemm_mode: 0 = FP64 moments matrix, 1 = split-bf16 tensor-core GEMM.
+ * out: num_mu complex (the caller takes the real part). */
+int kpm_calc_conductivity(kpm_engine* engine, const float* left_coords, const float* right_coords,
+                          const double* chemical_potential, int64_t num_mu, double broadening,
+                          double temperature, int64_t num_random, int64_t num_points, int32_t gemm_mode,
+                          double* out);
+
+/* Stats of the last calculation (kpm/Stats.cpp:31-65; KPMStats, cppmodule/src/kpm.cpp:50-66). */
+int kpm_get_stats(kpm_engine* engine, kpm_stats* out);
+
+/* Report string: cpb::KPM::report (KPM.cpp:15-17, Stats.cpp:9-28). */
+int kpm_report(kpm_engine* engine, int32_t shortform, char* buf, int64_t buf_size);
+
+/*
+ * The optimized Hamiltonian for target indices (system 0), as the test hook
+ * _cpp.OptimizedHamiltonian (cppmodule/src/kpm.cpp:106-125) and
+ * kpm::OptimizedHamiltonian::optimize_for (OptimizedHamiltonian.cpp:42-152):
+ * scaled by 2/a, BFS-reordered from src[0] (when reorder != 0), in the
+ * engine's native scalar type. Output capacities: out_indptr rows+1,
+ * out_indices/out_values nnz+rows, out_map rows, out_slices rows+1,
+ * out_src n_src, out_dest n_dest. Sizes come back through *out_nnz and
+ * *out_num_slices; *offsets receives the SliceMap src/dest offsets.
+ */
+int kpm_optimized_hamiltonian(kpm_engine* engine, const int32_t* src, int64_t n_src, const int32_t* dest,
+                              int64_t n_dest, int32_t reorder, int32_t* out_indptr, int32_t* out_indices,
+                              void* out_values, int64_t* out_nnz, int32_t* out_map, int32_t* out_slices,
+                              int64_t* out_num_slices, int32_t* out_src, int32_t* out_dest, int64_t* offsets);
+
+/* The engine's CUDA stream (a cudaStream_t) for interop: callers may record
+ * events on it or order their own work after the engine's. No reference
+ * counterpart (the reference has no device). Initialises the device. */
+int kpm_get_stream(kpm_engine* engine, void** stream);
+
+/* Damping coefficients g_n of a kernel (kpm/Kernel.cpp:6-50). */
+int kpm_damping_coefficients(int32_t kernel, double kernel_param, int64_t num_moments, double* out);
+
+/* Moments needed for a scaled broadening, rounded (kpm/Kernel.cpp:16-20,34-37,45-48). */
+int64_t kpm_required_num_moments(int32_t kernel, double kernel_param, double scaled_broadening);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KPM_GB300_H */

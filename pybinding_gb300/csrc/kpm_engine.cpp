@@ -1,0 +1,1391 @@
+// Host side of the GB300 KPM engine: the C ABI of include/kpm_gb300.h.
+//
+// Responsibilities (the reference's kpm::Core + OptimizedHamiltonian + Bounds +
+// Starter + DefaultCompute, re-designed around one device and one stream):
+//   * keep the Hamiltonian (one system or a ragged batch of block-diagonal
+//     systems) and the per-system spectral bounds / scale factors;
+//   * build the scaled, BFS-reordered matrix H~ = 2 (H - b) / a of every system
+//     (the reference's create_reordered, OptimizedHamiltonian.cpp:75-152) and
+//     upload it as padded row-major ELL in the recursion precision;
+//   * draw the reference's random starters with std::mt19937 (Starter.cpp:48-84);
+//   * drive the recursion kernels (one launch per Chebyshev step covering every
+//     system and vector batch), collect moments, damp and reconstruct on the GPU;
+//   * run Lanczos in FP64 on the GPU with the tridiagonal eigenproblem solved on
+//     the host by Sturm-sequence bisection.
+#include "kpm_gb300.h"
+#include "kpm_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using kpm::Tile;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct KpmError : std::runtime_error {
+    int code;
+    KpmError(int c, std::string const& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, std::string const& msg) { throw KpmError(code, msg); }
+
+#define KPM_CUDA(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            fail(KPM_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " + #expr); \
+    } while (0)
+
+template<class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return KPM_OK;
+    } catch (KpmError const& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (std::invalid_argument const& e) {
+        g_last_error = e.what();
+        return KPM_ERR_VALUE;
+    } catch (std::bad_alloc const&) {
+        g_last_error = "out of host memory";
+        return KPM_ERR_RUNTIME;
+    } catch (std::exception const& e) {
+        g_last_error = e.what();
+        return KPM_ERR_RUNTIME;
+    }
+}
+
+// ------------------------------------------------------------------ device memory
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(DBuf const&) = delete;
+    DBuf& operator=(DBuf const&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t n) {
+        if (n <= bytes && p) return;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            fail(KPM_ERR_CUDA, "device allocation of " + std::to_string(n) + " bytes failed: " + cudaGetErrorString(e));
+        }
+        bytes = n;
+    }
+    template<class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ------------------------------------------------------------------ scalar helpers
+using cf = std::complex<float>;
+using cd = std::complex<double>;
+
+int scalar_bytes(int st) { return st == KPM_F32 ? 4 : (st == KPM_C128 ? 16 : 8); }
+bool scalar_complex(int st) { return st == KPM_C64 || st == KPM_C128; }
+
+template<class T> struct RealOf { using type = T; };
+template<class T> struct RealOf<std::complex<T>> { using type = T; };
+template<class T> using real_of = typename RealOf<T>::type;
+template<class T> constexpr bool is_cplx_v = !std::is_same<T, real_of<T>>::value;
+
+template<class T> cd to_cd(T v) { return cd(static_cast<double>(v), 0.0); }
+template<> cd to_cd<cf>(cf v) { return cd(v.real(), v.imag()); }
+template<> cd to_cd<cd>(cd v) { return v; }
+
+template<class T> T from_cd(cd v);
+template<> float from_cd<float>(cd v) { return static_cast<float>(v.real()); }
+template<> double from_cd<double>(cd v) { return v.real(); }
+template<> cf from_cd<cf>(cd v) { return cf(static_cast<float>(v.real()), static_cast<float>(v.imag())); }
+template<> cd from_cd<cd>(cd v) { return v; }
+
+// convert value of scalar type Tin to compute type Tc (real->complex allowed)
+template<class Tc, class Tin> Tc convert(Tin v) {
+    if constexpr (is_cplx_v<Tc>) {
+        if constexpr (is_cplx_v<Tin>)
+            return Tc(static_cast<real_of<Tc>>(v.real()), static_cast<real_of<Tc>>(v.imag()));
+        else
+            return Tc(static_cast<real_of<Tc>>(v), real_of<Tc>(0));
+    } else {
+        if constexpr (is_cplx_v<Tin>) return static_cast<Tc>(v.real());
+        else return static_cast<Tc>(v);
+    }
+}
+
+template<class F>
+void with_scalar(int st, F&& f) {
+    switch (st) {
+        case KPM_F32: f(float{}); break;
+        case KPM_F64: f(double{}); break;
+        case KPM_C64: f(cf{}); break;
+        case KPM_C128: f(cd{}); break;
+        default: fail(KPM_ERR_VALUE, "unknown scalar type");
+    }
+}
+template<class F>
+void with_vtype(int vt, F&& f) {
+    switch (vt) {
+        case kpm::V_F32: f(float{}); break;
+        case kpm::V_F64: f(double{}); break;
+        case kpm::V_C64: f(cf{}); break;
+        default: f(cd{}); break;
+    }
+}
+
+// ------------------------------------------------------------------ scale and kernels
+// kpm::Scale<double>(min, max) (kpm/Bounds.hpp:15-30): float constants as in the reference
+struct ScaleAB { double a = 0, b = 0; };
+ScaleAB make_scale(double emin, double emax) {
+    constexpr float tol = 0.01f;
+    ScaleAB s;
+    s.a = 0.5f * (emax - emin) * (1 + tol);
+    s.b = 0.5f * (emax + emin);
+    if (std::abs(s.b / s.a) < 0.01f * tol) s.b = 0;
+    return s;
+}
+
+constexpr float PI_F = 3.14159265358979323846f;  // the reference's pi constant is a float
+
+int64_t round_moments(int64_t n) {
+    if (n < 2) return 2;
+    return n + ((4 - (n - 2) % 4) % 4);
+}
+
+std::vector<double> damping(int kernel, double lambda, int64_t M) {
+    std::vector<double> g(static_cast<size_t>(M));
+    double const N = static_cast<double>(M);
+    double const pi = static_cast<double>(PI_F);
+    for (int64_t i = 0; i < M; ++i) {
+        double const n = static_cast<double>(i);
+        if (kernel == KPM_KERNEL_JACKSON) {
+            double const Np = N + 1;
+            g[i] = ((Np - n) * std::cos(pi * n / Np) + std::sin(pi * n / Np) / std::tan(pi / Np)) / Np;
+        } else if (kernel == KPM_KERNEL_LORENTZ) {
+            g[i] = std::sinh(lambda * (1 - n / N)) / std::sinh(lambda);
+        } else {
+            g[i] = 1.0;
+        }
+    }
+    return g;
+}
+
+int64_t required_moments(int kernel, double lambda, double scaled_broadening) {
+    double const num = kernel == KPM_KERNEL_LORENTZ ? lambda : static_cast<double>(PI_F);
+    return round_moments(static_cast<int64_t>(num / scaled_broadening) + 1);
+}
+
+// ------------------------------------------------------------------ tridiagonal extremes
+// Extreme eigenvalues of the symmetric tridiagonal (alpha, beta[0..k-2]) by
+// Sturm-sequence bisection: count(x) = #eigenvalues < x.
+int sturm_count(std::vector<double> const& a, std::vector<double> const& b, double x) {
+    int cnt = 0;
+    double q = a[0] - x;
+    if (q < 0) ++cnt;
+    for (size_t i = 1; i < a.size(); ++i) {
+        double const bb = b[i - 1] * b[i - 1];
+        if (q == 0) q = std::numeric_limits<double>::epsilon() * (std::abs(b[i - 1]) + 1e-300);
+        q = a[i] - x - bb / q;
+        if (q < 0) ++cnt;
+    }
+    return cnt;
+}
+
+void tridiagonal_extremes(std::vector<double> const& a, std::vector<double> const& b, double& mn, double& mx) {
+    size_t const k = a.size();
+    double lo = std::numeric_limits<double>::max(), hi = std::numeric_limits<double>::lowest();
+    for (size_t i = 0; i < k; ++i) {
+        double r = 0;
+        if (i > 0) r += std::abs(b[i - 1]);
+        if (i + 1 < k) r += std::abs(b[i]);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    double const span = std::max(hi - lo, 1e-300);
+    lo -= 1e-12 * span;
+    hi += 1e-12 * span;
+    auto bisect = [&](int target) {  // smallest x with count(x) > target
+        double l = lo, h = hi;
+        for (int it = 0; it < 200 && h - l > 1e-15 * std::max(std::abs(l), std::abs(h)) + 1e-300; ++it) {
+            double const m = 0.5 * (l + h);
+            if (sturm_count(a, b, m) > target) h = m; else l = m;
+        }
+        return 0.5 * (l + h);
+    };
+    mn = bisect(0);
+    mx = bisect(static_cast<int>(k) - 1);
+}
+
+std::string with_suffix(double v) {
+    char buf[64];
+    char const* suf[] = {"", "K", "M", "G", "T", "P"};
+    int i = 0;
+    while (std::abs(v) >= 1000.0 && i < 5) { v /= 1000.0; ++i; }
+    std::snprintf(buf, sizeof buf, i == 0 ? "%.0f%s" : "%.3g%s", v, suf[i]);
+    return buf;
+}
+
+std::string pretty_time(double s) {
+    char buf[64];
+    if (s < 1e-3) std::snprintf(buf, sizeof buf, "%.1f us", s * 1e6);
+    else if (s < 1) std::snprintf(buf, sizeof buf, "%.2f ms", s * 1e3);
+    else std::snprintf(buf, sizeof buf, "%.3f s", s);
+    return buf;
+}
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+// ====================================================================== engine
+struct kpm_engine {
+    // input
+    int stype = KPM_F32;
+    kpm_config cfg{};
+    int vtype = kpm::V_F32;
+    int64_t rows = 0;
+    int nsys = 1;
+    std::vector<int64_t> sys_off;           // nsys + 1
+    std::vector<int32_t> indptr, indices;   // global CSR, global column indices
+    std::vector<unsigned char> values;      // stype
+
+    // per system bounds
+    struct Sys {
+        bool have_bounds = false;
+        double emin = 0, emax = 0;
+        int loops = 0;
+    };
+    std::vector<Sys> sys;
+
+    // current optimization (reordered, scaled device matrix)
+    bool opt_valid = false;
+    std::vector<int32_t> opt_src, opt_dest;  // target indices (system 0) or {0} for all systems
+    std::vector<int32_t> map;                // original global row -> reordered global row
+    std::vector<int32_t> slices;             // SliceMap borders (system 0)
+    int64_t src_offset = 0, dest_offset = 0;
+    std::vector<int32_t> idx_src, idx_dest;  // reordered target indices
+    int W = 0;
+    int64_t opt_nnz = 0;                     // reordered CSR non-zeros (all systems)
+    DBuf d_col, d_val, d_map, d_sysoff;
+
+    // Lanczos device state
+    bool lz_uploaded = false;
+    DBuf d_lip, d_lix, d_lval, d_lv0, d_lv1, d_ltiles, d_lab;
+    int lz_tiles = 0;
+
+    // recursion buffers
+    DBuf d_x0, d_x1, d_acc, d_tiles, d_mu, d_mu_avg, d_stage, d_pos, d_gamma, d_energy, d_out;
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // stats of the last calculation
+    kpm_stats st{};
+    double calc_time = 0;
+    bool last_bounds_lanczos = false;
+
+    ~kpm_engine() {
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int64_t sys_rows(int s) const { return sys_off[s + 1] - sys_off[s]; }
+
+    // The device is touched on first use, so that argument checks and host-only
+    // entry points work (and fail cleanly) without a GPU.
+    void ensure_device() {
+        if (stream) return;
+        int dev_count = 0;
+        cudaError_t e = cudaGetDeviceCount(&dev_count);
+        if (e != cudaSuccess || dev_count < 1) {
+            cudaGetLastError();
+            fail(KPM_ERR_CUDA, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+        }
+        KPM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        KPM_CUDA(cudaEventCreate(&ev0));
+        KPM_CUDA(cudaEventCreate(&ev1));
+    }
+
+    void set_h(int st_, int64_t n, int32_t const* ip, int32_t const* ix, void const* v, int ns, int64_t const* offs) {
+        if (n <= 0) fail(KPM_ERR_VALUE, "the Hamiltonian must have at least one row");
+        if (!ip || !ix || !v) fail(KPM_ERR_VALUE, "null Hamiltonian arrays");
+        if (st_ < KPM_F32 || st_ > KPM_C128) fail(KPM_ERR_VALUE, "unknown scalar type");
+        if (ns < 1) fail(KPM_ERR_VALUE, "num_systems must be >= 1");
+        if (n > std::numeric_limits<int32_t>::max()) fail(KPM_ERR_VALUE, "too many rows for int32 indices");
+        std::vector<int64_t> off(ns + 1);
+        if (ns == 1 || !offs) {
+            if (ns != 1) fail(KPM_ERR_VALUE, "system_offsets required for num_systems > 1");
+            off = {0, n};
+        } else {
+            off.assign(offs, offs + ns + 1);
+            if (off[0] != 0 || off[ns] != n) fail(KPM_ERR_VALUE, "system_offsets must start at 0 and end at rows");
+            for (int s = 0; s < ns; ++s)
+                if (off[s + 1] <= off[s]) fail(KPM_ERR_VALUE, "system_offsets must be strictly increasing");
+        }
+        int64_t const nnz = ip[n];
+        if (ip[0] != 0 || nnz < 0) fail(KPM_ERR_VALUE, "invalid CSR indptr");
+        for (int64_t r = 0; r < n; ++r)
+            if (ip[r + 1] < ip[r]) fail(KPM_ERR_VALUE, "invalid CSR indptr (decreasing)");
+        // columns in range, sorted, within the row's own system (block diagonal)
+        int s = 0;
+        for (int64_t r = 0; r < n; ++r) {
+            while (r >= off[s + 1]) ++s;
+            for (int64_t k = ip[r]; k < ip[r + 1]; ++k) {
+                int64_t const c = ix[k];
+                if (c < off[s] || c >= off[s + 1])
+                    fail(KPM_ERR_VALUE, "CSR column index out of range (or outside its system block)");
+                if (k > ip[r] && ix[k - 1] >= c) fail(KPM_ERR_VALUE, "CSR column indices must be sorted and unique");
+            }
+        }
+        // Hamiltonian.hpp:133-140
+        size_t const sb = static_cast<size_t>(scalar_bytes(st_));
+        bool finite = true;
+        with_scalar(st_, [&](auto z) {
+            using T = decltype(z);
+            auto const* p = static_cast<T const*>(v);
+            for (int64_t k = 0; k < nnz && finite; ++k) {
+                cd const c = to_cd(p[k]);
+                if (!std::isfinite(c.real()) || !std::isfinite(c.imag())) finite = false;
+            }
+        });
+        if (!finite)
+            fail(KPM_ERR_RUNTIME, "The Hamiltonian contains invalid values: NaN or INF.\n"
+                                  "Check the lattice and/or modifier functions.");
+        stype = st_;
+        rows = n;
+        nsys = ns;
+        sys_off = off;
+        indptr.assign(ip, ip + n + 1);
+        indices.assign(ix, ix + nnz);
+        values.assign(static_cast<unsigned char const*>(v), static_cast<unsigned char const*>(v) + nnz * sb);
+        sys.assign(ns, Sys{});
+        if (cfg.min_energy != cfg.max_energy)
+            for (auto& x : sys) { x.have_bounds = true; x.emin = cfg.min_energy; x.emax = cfg.max_energy; }
+        opt_valid = false;
+        lz_uploaded = false;
+        // recursion precision (KPM_PREC_*)
+        bool const dbl = cfg.precision == KPM_PREC_FP64 ||
+                         (cfg.precision == KPM_PREC_AUTO && (st_ == KPM_F64 || st_ == KPM_C128));
+        bool const cpx = scalar_complex(st_);
+        vtype = cpx ? (dbl ? kpm::V_C128 : kpm::V_C64) : (dbl ? kpm::V_F64 : kpm::V_F32);
+    }
+
+    // ---------------------------------------------------------------- Lanczos (FP64, GPU)
+    void upload_lanczos() {
+        if (lz_uploaded) return;
+        ensure_device();
+        bool const cpx = scalar_complex(stype);
+        size_t const es = cpx ? 16 : 8;
+        int64_t const nnz = indptr[rows];
+        std::vector<unsigned char> vals(static_cast<size_t>(nnz) * es);
+        with_scalar(stype, [&](auto z) {
+            using T = decltype(z);
+            auto const* p = reinterpret_cast<T const*>(values.data());
+            if (cpx) {
+                auto* o = reinterpret_cast<cd*>(vals.data());
+                for (int64_t k = 0; k < nnz; ++k) o[k] = to_cd(p[k]);
+            } else {
+                auto* o = reinterpret_cast<double*>(vals.data());
+                for (int64_t k = 0; k < nnz; ++k) o[k] = to_cd(p[k]).real();
+            }
+        });
+        d_lip.ensure(sizeof(int32_t) * (rows + 1));
+        d_lix.ensure(sizeof(int32_t) * std::max<int64_t>(nnz, 1));
+        d_lval.ensure(std::max<size_t>(vals.size(), 16));
+        KPM_CUDA(cudaMemcpyAsync(d_lip.p, indptr.data(), sizeof(int32_t) * (rows + 1), cudaMemcpyHostToDevice, stream));
+        if (nnz > 0) {
+            KPM_CUDA(cudaMemcpyAsync(d_lix.p, indices.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, stream));
+            KPM_CUDA(cudaMemcpyAsync(d_lval.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, stream));
+        }
+        std::vector<Tile> tiles;
+        for (int s = 0; s < nsys; ++s)
+            for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += 2048)
+                tiles.push_back({static_cast<int32_t>(r), static_cast<int32_t>(std::min(sys_off[s + 1], r + 2048)), s, 0});
+        lz_tiles = static_cast<int>(tiles.size());
+        d_ltiles.ensure(sizeof(Tile) * tiles.size());
+        KPM_CUDA(cudaMemcpyAsync(d_ltiles.p, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream));
+        d_lv0.ensure(es * rows);
+        d_lv1.ensure(es * rows);
+        d_lab.ensure(sizeof(double) * 3 * nsys);
+        KPM_CUDA(cudaStreamSynchronize(stream));
+        lz_uploaded = true;
+    }
+
+    // Bounds for every system that lacks them: compute/lanczos.hpp:101-154 in FP64.
+    void compute_bounds() {
+        std::vector<int> todo;
+        for (int s = 0; s < nsys; ++s)
+            if (!sys[s].have_bounds) todo.push_back(s);
+        if (todo.empty()) return;
+        double const t0 = now_s();
+        upload_lanczos();
+        bool const cpx = scalar_complex(stype);
+        size_t const es = cpx ? 16 : 8;
+        // start vectors: U[0,1) from a fresh default mt19937 per system in H's real type, normalized
+        std::vector<unsigned char> v1(es * rows);
+        for (int s = 0; s < nsys; ++s) {
+            std::mt19937 gen;
+            int64_t const n = sys_rows(s);
+            std::vector<double> u(static_cast<size_t>(n));
+            if (stype == KPM_F32 || stype == KPM_C64) {
+                std::uniform_real_distribution<float> dist;
+                for (auto& x : u) x = dist(gen);
+            } else {
+                std::uniform_real_distribution<double> dist;
+                for (auto& x : u) x = dist(gen);
+            }
+            double nrm = 0;
+            for (auto x : u) nrm += x * x;
+            nrm = std::sqrt(nrm);
+            for (int64_t i = 0; i < n; ++i) {
+                double const val = nrm > 0 ? u[i] / nrm : 0.0;
+                if (cpx) reinterpret_cast<cd*>(v1.data())[sys_off[s] + i] = cd(val, 0);
+                else reinterpret_cast<double*>(v1.data())[sys_off[s] + i] = val;
+            }
+        }
+        KPM_CUDA(cudaMemcpyAsync(d_lv1.p, v1.data(), v1.size(), cudaMemcpyHostToDevice, stream));
+        KPM_CUDA(cudaMemsetAsync(d_lv0.p, 0, es * rows, stream));
+        std::vector<std::vector<double>> alpha(nsys), beta(nsys);
+        std::vector<double> prev_min(nsys, std::numeric_limits<double>::max());
+        std::vector<double> prev_max(nsys, std::numeric_limits<double>::lowest());
+        std::vector<char> done(nsys, 1);
+        for (int s : todo) done[s] = 0;
+        double const precision = static_cast<double>(static_cast<float>(cfg.lanczos_precision)) / 100;
+        std::vector<double> hb(3 * nsys, 0.0);  // [bprev | alpha | nrm]
+        void* v0 = d_lv0.p;
+        void* v1d = d_lv1.p;
+        for (int it = 0; it < 1000; ++it) {
+            for (int s = 0; s < nsys; ++s) hb[s] = beta[s].empty() ? 0.0 : beta[s].back();
+            std::fill(hb.begin() + nsys, hb.end(), 0.0);
+            double* dab = d_lab.as<double>();
+            KPM_CUDA(cudaMemcpyAsync(dab, hb.data(), sizeof(double) * 3 * nsys, cudaMemcpyHostToDevice, stream));
+            KPM_CUDA(kpm::launch_lanczos_a(cpx, d_lip.as<int32_t>(), d_lix.as<int32_t>(), d_lval.p, v1d, v0,
+                                           d_ltiles.as<Tile>(), lz_tiles, dab, dab + nsys, stream));
+            KPM_CUDA(kpm::launch_lanczos_b(cpx, v1d, v0, d_ltiles.as<Tile>(), lz_tiles, dab + nsys, dab + 2 * nsys, stream));
+            KPM_CUDA(kpm::launch_lanczos_c(cpx, v0, d_ltiles.as<Tile>(), lz_tiles, dab + 2 * nsys, stream));
+            KPM_CUDA(cudaMemcpyAsync(hb.data(), dab, sizeof(double) * 3 * nsys, cudaMemcpyDeviceToHost, stream));
+            KPM_CUDA(cudaStreamSynchronize(stream));
+            std::swap(v0, v1d);
+            bool all = true;
+            for (int s = 0; s < nsys; ++s) {
+                if (done[s]) continue;
+                alpha[s].push_back(hb[nsys + s]);
+                beta[s].push_back(std::sqrt(hb[2 * nsys + s]));
+                double mn, mx;
+                tridiagonal_extremes(alpha[s], beta[s], mn, mx);
+                bool const cmin = std::abs((prev_min[s] - mn) / mn) < precision;
+                bool const cmax = std::abs((prev_max[s] - mx) / mx) < precision;
+                if (cmin && cmax) {
+                    done[s] = 1;
+                    sys[s].have_bounds = true;
+                    sys[s].emin = mn;
+                    sys[s].emax = mx;
+                    sys[s].loops = it;
+                } else {
+                    all = false;
+                }
+                prev_min[s] = mn;
+                prev_max[s] = mx;
+            }
+            if (all) {
+                st.bounds_time = now_s() - t0;
+                st.lanczos_loops = sys[todo.front()].loops;
+                last_bounds_lanczos = true;
+                return;
+            }
+        }
+        fail(KPM_ERR_RUNTIME, "Lanczos algorithm did not converge for the min/max eigenvalues.");
+    }
+
+    ScaleAB scale(int s) {
+        compute_bounds();
+        return make_scale(sys[s].emin, sys[s].emax);
+    }
+
+    // ---------------------------------------------------------------- optimization
+    // BFS reorder + scale of one system into the compute type Tc, appended to the
+    // global reordered CSR (OptimizedHamiltonian.cpp:75-152 / 55-72 semantics).
+    template<class Tc, class Tin>
+    void reorder_system(int s, std::vector<int32_t> const& src_local, ScaleAB sc, bool reorder,
+                        std::vector<int32_t>& oip, std::vector<int32_t>& oix, std::vector<Tc>& oval,
+                        std::vector<int32_t>* borders_out) {
+        using R = real_of<Tc>;
+        int64_t const off = sys_off[s], n = sys_rows(s);
+        auto const* hv = reinterpret_cast<Tin const*>(values.data());
+        R const a = static_cast<R>(sc.a), b = static_cast<R>(sc.b);
+        R const inv_a = R{2 / a};
+        std::vector<int32_t> order;
+        order.reserve(n);
+        std::vector<int32_t> local(n, -1);
+        std::vector<int32_t> borders{1};
+        if (reorder) {
+            order.push_back(src_local[0]);
+            local[src_local[0]] = 0;
+        } else {
+            for (int64_t i = 0; i < n; ++i) { order.push_back(static_cast<int32_t>(i)); local[i] = static_cast<int32_t>(i); }
+        }
+        std::vector<std::pair<int32_t, Tc>> row_buf;
+        for (int64_t nr = 0; nr < n; ++nr) {
+            int32_t const orow = order[nr];
+            row_buf.clear();
+            bool diag = false;
+            for (int32_t k = indptr[off + orow]; k < indptr[off + orow + 1]; ++k) {
+                int32_t const ocol = static_cast<int32_t>(indices[k] - off);
+                if (local[ocol] < 0) {
+                    local[ocol] = static_cast<int32_t>(order.size());
+                    order.push_back(ocol);
+                }
+                Tc v;
+                if (reorder) {  // value * (2/a) - b * (2/a) on the diagonal
+                    v = convert<Tc>(hv[k]) * inv_a;
+                    if (ocol == orow) { v -= b * inv_a; diag = true; }
+                } else {        // (value - b) * (2/a)
+                    v = convert<Tc>(hv[k]);
+                    if (ocol == orow) { if (b != R(0)) v -= b; diag = true; }
+                    v = v * (R{2} / a);
+                }
+                row_buf.push_back({local[ocol], v});
+            }
+            if (b != R(0) && !diag) {
+                Tc v = reorder ? Tc(-b * inv_a) : (Tc(R(0)) - Tc(b)) * (R{2} / a);
+                row_buf.push_back({static_cast<int32_t>(nr), v});
+            }
+            std::sort(row_buf.begin(), row_buf.end(),
+                      [](std::pair<int32_t, Tc> const& x, std::pair<int32_t, Tc> const& y) { return x.first < y.first; });
+            for (auto const& p : row_buf) {
+                oix.push_back(static_cast<int32_t>(p.first + off));
+                oval.push_back(p.second);
+            }
+            oip.push_back(static_cast<int32_t>(oix.size()));
+            if (reorder && nr == borders.back() - 1) borders.push_back(static_cast<int32_t>(order.size()));
+        }
+        for (int64_t i = 0; i < n; ++i) map[off + i] = static_cast<int32_t>(local[i] + off);
+        if (borders_out) {
+            if (reorder) {
+                borders.pop_back();
+                *borders_out = borders;
+            } else {
+                *borders_out = {static_cast<int32_t>(n)};
+            }
+        }
+    }
+
+    bool reorders() const { return cfg.optimal_size || cfg.interleaved; }
+
+    // Optimize every system for source row 0 (DOS, moments, conductivity) or system 0
+    // for (src, dest) targets; upload the padded ELL in the recursion type.
+    void optimize(std::vector<int32_t> const& src, std::vector<int32_t> const& dest) {
+        if (opt_valid && src == opt_src && dest == opt_dest) return;
+        ensure_device();
+        double const t0 = now_s();
+        compute_bounds();
+        map.assign(rows, 0);
+        std::vector<int32_t> oip{0}, oix;
+        W = 0;
+        with_vtype(vtype, [&](auto zc) {
+            using Tc = decltype(zc);
+            std::vector<Tc> oval;
+            with_scalar(stype, [&](auto zi) {
+                using Tin = decltype(zi);
+                for (int s = 0; s < nsys; ++s) {
+                    std::vector<int32_t> sl = (s == 0) ? src : std::vector<int32_t>{0};
+                    reorder_system<Tc, Tin>(s, sl, scale(s), reorders(), oip, oix, oval, s == 0 ? &slices : nullptr);
+                }
+            });
+            for (int64_t r = 0; r < rows; ++r) W = std::max(W, oip[r + 1] - oip[r]);
+            W = std::max(W, 1);
+            std::vector<int32_t> col(static_cast<size_t>(rows) * W);
+            std::vector<Tc> val(static_cast<size_t>(rows) * W, Tc(0));
+            for (int64_t r = 0; r < rows; ++r) {
+                int j = 0;
+                for (int32_t k = oip[r]; k < oip[r + 1]; ++k, ++j) {
+                    col[r * W + j] = oix[k];
+                    val[r * W + j] = oval[k];
+                }
+                for (; j < W; ++j) col[r * W + j] = static_cast<int32_t>(r);
+            }
+            d_col.ensure(col.size() * sizeof(int32_t));
+            d_val.ensure(val.size() * sizeof(Tc));
+            KPM_CUDA(cudaMemcpyAsync(d_col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+            KPM_CUDA(cudaMemcpyAsync(d_val.p, val.data(), val.size() * sizeof(Tc), cudaMemcpyHostToDevice, stream));
+            KPM_CUDA(cudaStreamSynchronize(stream));
+        });
+        opt_nnz = oip.back();
+        d_map.ensure(sizeof(int32_t) * rows);
+        KPM_CUDA(cudaMemcpy(d_map.p, map.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice));
+        d_sysoff.ensure(sizeof(int64_t) * (nsys + 1));
+        KPM_CUDA(cudaMemcpy(d_sysoff.p, sys_off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice));
+        idx_src.clear();
+        idx_dest.clear();
+        for (auto i : src) idx_src.push_back(map[i]);
+        for (auto i : dest) idx_dest.push_back(map[i]);
+        // SliceMap offsets (OptimizedHamiltonian.cpp:5-18)
+        auto find_offset = [&](std::vector<int32_t> const& idx) {
+            int32_t const mx = *std::max_element(idx.begin(), idx.end());
+            auto it = std::find_if(slices.begin(), slices.end(), [&](int32_t v) { return v > mx; });
+            return static_cast<int64_t>(it - slices.begin());
+        };
+        src_offset = find_offset(idx_src);
+        dest_offset = find_offset(idx_dest);
+        opt_src = src;
+        opt_dest = dest;
+        opt_valid = true;
+        st.hamiltonian_time = now_s() - t0;
+    }
+
+    int64_t slice_index(int64_t n, int64_t M) const {  // SliceMap::index
+        int64_t const last = static_cast<int64_t>(slices.size()) - 1;
+        int64_t const mid = (M - 1 + dest_offset - src_offset) / 2;
+        int64_t const mx = std::min(last, mid + src_offset);
+        if (n < mid) return std::min(mx, n + src_offset);
+        return std::min(mx, M - 1 - n + dest_offset);
+    }
+    int32_t optimal_size(int64_t n, int64_t M) const { return slices[slice_index(n, M)]; }
+
+    // ---------------------------------------------------------------- batching
+    struct Shape { int E, LPR, K, nbatch, rows_per_tile; };
+
+    Shape pick_shape(int64_t nvec) const {
+        int const vb = kpm::vtype_bytes(vtype);
+        int const E16 = 16 / vb;
+        int kmax = cfg.batch_width > 0 ? cfg.batch_width : 256 / vb;  // 256-byte rows by default
+        Shape sh{1, 1, 1, 1, 0};
+        if (nvec >= E16 * 2 && kmax >= E16 * 2) {
+            int K = E16 * 2;
+            while (K * 2 <= kmax && K * 2 <= nvec && K * 2 <= E16 * 32) K *= 2;
+            sh.E = E16;
+            sh.LPR = K / E16;
+            sh.K = K;
+        }
+        if (cfg.batch_width == 1) sh = Shape{1, 1, 1, 1, 0};
+        sh.nbatch = static_cast<int>((nvec + sh.K - 1) / sh.K);
+        sh.rows_per_tile = (256 / sh.LPR) * 16;
+        return sh;
+    }
+
+    int build_tiles(Shape const& sh, bool sys0_only) {
+        std::vector<Tile> tiles;
+        int const ns = sys0_only ? 1 : nsys;
+        for (int s = 0; s < ns; ++s)
+            for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += sh.rows_per_tile)
+                for (int b = 0; b < sh.nbatch; ++b)
+                    tiles.push_back({static_cast<int32_t>(r),
+                                     static_cast<int32_t>(std::min(sys_off[s + 1], r + sh.rows_per_tile)), s, b});
+        d_tiles.ensure(sizeof(Tile) * tiles.size());
+        KPM_CUDA(cudaMemcpyAsync(d_tiles.p, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream));
+        return static_cast<int>(tiles.size());
+    }
+
+    // ---------------------------------------------------------------- diagonal recursion
+    // Starters: kind 0 = host/device array [s][v][i] original order, kind 1 = unit vectors at
+    // reordered positions `units` (system 0). Per-vector moments land in d_mu as
+    // [s][v][M] complex double. `opt_rows` applies the optimal-size row limit (system 0).
+    void run_diag(int64_t M, int64_t nvec, void const* starters, bool on_device, std::vector<int32_t> const* units,
+                  bool opt_rows) {
+        if (M < 2 || (M - 2) % 4 != 0) fail(KPM_ERR_VALUE, "num_moments must satisfy (M - 2) % 4 == 0");
+        if (nvec < 1) fail(KPM_ERR_VALUE, "num_vectors must be >= 1");
+        Shape const sh = pick_shape(nvec);
+        int const vb = kpm::vtype_bytes(vtype);
+        int const NV = kpm::vtype_nv(vtype);
+        bool const sys0 = units != nullptr;
+        int const ns = sys0 ? 1 : nsys;
+        int64_t const bstride = rows * sh.K;
+        size_t const vbytes = static_cast<size_t>(bstride) * sh.nbatch * vb;
+        d_x0.ensure(vbytes);
+        d_x1.ensure(vbytes);
+        int64_t const half = M / 2;
+        size_t const step_acc = static_cast<size_t>(ns) * sh.nbatch * sh.K * NV;
+        d_acc.ensure(sizeof(double) * step_acc * half);
+        d_mu.ensure(sizeof(double) * 2 * ns * nvec * M);
+        int const ntiles = build_tiles(sh, sys0);
+
+        KPM_CUDA(cudaMemsetAsync(d_x0.p, 0, vbytes, stream));
+        if (units) {
+            d_pos.ensure(sizeof(int32_t) * units->size());
+            KPM_CUDA(cudaMemcpyAsync(d_pos.p, units->data(), sizeof(int32_t) * units->size(), cudaMemcpyHostToDevice, stream));
+            KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, sh.K, rows, stream));
+        } else {
+            size_t const in_bytes = static_cast<size_t>(nvec) * rows * vb;
+            void const* src = starters;
+            if (!on_device) {
+                d_stage.ensure(in_bytes);
+                KPM_CUDA(cudaMemcpyAsync(d_stage.p, starters, in_bytes, cudaMemcpyHostToDevice, stream));
+                src = d_stage.p;
+            }
+            KPM_CUDA(kpm::launch_scatter_starters(vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(), nsys,
+                                                  nvec, sh.K, sh.nbatch, rows, stream));
+        }
+        KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
+        KPM_CUDA(cudaEventRecord(ev0, stream));
+        kpm::DiagStep a{};
+        a.vtype = vtype;
+        a.E = sh.E;
+        a.LPR = sh.LPR;
+        a.col = d_col.as<int32_t>();
+        a.val = d_val.p;
+        a.W = W;
+        a.batch_stride = bstride;
+        a.tiles = d_tiles.as<Tile>();
+        a.num_tiles = ntiles;
+        a.nbatch = sh.nbatch;
+        a.row_limit = static_cast<int32_t>(rows);
+        // r1 = H~ r0 / 2 with mu0, mu1 sums
+        a.x = d_x0.p;
+        a.y = d_x1.p;
+        a.acc = d_acc.as<double>();
+        a.init = true;
+        KPM_CUDA(kpm::launch_diag_step(a, stream));
+        a.init = false;
+        void* r0 = d_x0.p;
+        void* r1 = d_x1.p;
+        for (int64_t n = 2; n <= half; ++n) {
+            a.x = r1;
+            a.y = r0;
+            a.acc = d_acc.as<double>() + step_acc * (n - 1);
+            if (opt_rows) {
+                int32_t const lim = optimal_size(n, M);
+                a.row_limit = lim;
+                // tiles are ordered [tile][batch]: launch those that start below the limit
+                int64_t const t = (lim + sh.rows_per_tile - 1) / sh.rows_per_tile;
+                a.num_tiles = static_cast<int>(std::min<int64_t>(ntiles, t * sh.nbatch));
+            }
+            KPM_CUDA(kpm::launch_diag_step(a, stream));
+            std::swap(r0, r1);
+        }
+        KPM_CUDA(cudaEventRecord(ev1, stream));
+        KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
+                                          d_mu.as<double>(), stream));
+        KPM_CUDA(cudaStreamSynchronize(stream));
+        float ms = 0;
+        KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        st.moments_time = ms * 1e-3;
+        last_shape = sh;
+    }
+    Shape last_shape{};
+
+    void reset_stats(int64_t M, bool diagonal, bool opt, double multiplier, int64_t active_rows_nnz_rows) {
+        (void)active_rows_nnz_rows;
+        st.num_moments = M;
+        st.multiplier = multiplier;
+        int64_t const ell_nnz = rows * W;
+        st.uses_full_system = static_cast<int32_t>(static_cast<int64_t>(slices.size()) < M / 2);
+        int64_t nnz = M * ell_nnz, vec = M * rows;
+        int64_t onnz = nnz, ovec = vec;
+        if (opt) {
+            onnz = 0;
+            ovec = 0;
+            for (int64_t n = 0; n < M; ++n) {
+                int64_t const sz = optimal_size(n, M);
+                onnz += sz * W;
+                ovec += sz;
+            }
+        }
+        if (diagonal) { nnz /= 2; onnz /= 2; vec /= 2; ovec /= 2; }
+        st.nnz = nnz;
+        st.opt_nnz = onnz;
+        st.vec = vec;
+        st.opt_vec = ovec;
+        st.matrix_memory = static_cast<int64_t>(rows) * W * (kpm::vtype_bytes(vtype) + 4);
+        st.vector_memory = static_cast<int64_t>(rows) * kpm::vtype_bytes(vtype);
+    }
+    void finish_stats() { st.eps = st.moments_time > 0 ? st.multiplier * st.opt_nnz / st.moments_time : 0.0; }
+
+    // ---------------------------------------------------------------- reconstruction
+    void spectral(double const* d_moments_cd, int64_t M, int cols, double const* energy, int64_t ne, ScaleAB sc,
+                  double* out_host) {
+        d_energy.ensure(sizeof(double) * std::max<int64_t>(ne, 1));
+        d_out.ensure(sizeof(double) * 2 * std::max<int64_t>(ne * cols, 1));
+        KPM_CUDA(cudaMemcpyAsync(d_energy.p, energy, sizeof(double) * ne, cudaMemcpyHostToDevice, stream));
+        KPM_CUDA(kpm::launch_spectral_density(d_moments_cd, M, cols, d_energy.as<double>(), static_cast<int>(ne),
+                                              sc.a, sc.b, d_out.as<double>(), stream));
+        KPM_CUDA(cudaMemcpyAsync(out_host, d_out.p, sizeof(double) * ne * cols, cudaMemcpyDeviceToHost, stream));
+        KPM_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    // damp per-column complex moments in place on the device copy (host round trip is tiny)
+    void damp_device(double* d_moments_cd, int64_t M, int64_t cols, int64_t stride_M) {
+        std::vector<double> h(static_cast<size_t>(2 * cols * stride_M));
+        KPM_CUDA(cudaMemcpyAsync(h.data(), d_moments_cd, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream));
+        KPM_CUDA(cudaStreamSynchronize(stream));
+        auto g = damping(cfg.kernel, cfg.kernel_param, M);
+        std::vector<double> o(static_cast<size_t>(2 * cols * M));
+        for (int64_t c = 0; c < cols; ++c)
+            for (int64_t n = 0; n < M; ++n) {
+                o[2 * (c * M + n)] = h[2 * (c * stride_M + n)] * g[n];
+                o[2 * (c * M + n) + 1] = h[2 * (c * stride_M + n) + 1] * g[n];
+            }
+        KPM_CUDA(cudaMemcpyAsync(d_moments_cd, o.data(), sizeof(double) * o.size(), cudaMemcpyHostToDevice, stream));
+    }
+};
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* kpm_last_error(void) { return g_last_error.c_str(); }
+
+void kpm_config_default(kpm_config* c) {
+    if (!c) return;
+    c->min_energy = 0;
+    c->max_energy = 0;
+    c->kernel = KPM_KERNEL_JACKSON;
+    c->kernel_param = 4.0;
+    c->matrix_format = KPM_FORMAT_ELL;
+    c->optimal_size = 1;
+    c->interleaved = 1;
+    c->lanczos_precision = 0.002;
+    c->precision = KPM_PREC_AUTO;
+    c->batch_width = 0;
+}
+
+int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const int32_t* indices, const void* values,
+               int32_t num_systems, const int64_t* system_offsets, const kpm_config* cfg, kpm_engine** out) {
+    return guarded([&] {
+        if (!out) fail(KPM_ERR_VALUE, "null output handle");
+        *out = nullptr;
+        auto e = std::make_unique<kpm_engine>();
+        if (cfg) e->cfg = *cfg; else kpm_config_default(&e->cfg);
+        // Config holds the energy range as float (kpm/Config.hpp:24-25)
+        e->cfg.min_energy = static_cast<float>(e->cfg.min_energy);
+        e->cfg.max_energy = static_cast<float>(e->cfg.max_energy);
+        if (e->cfg.min_energy > e->cfg.max_energy)
+            fail(KPM_ERR_VALUE, "KPM: Invalid energy range specified (min > max).");
+        if (e->cfg.kernel == KPM_KERNEL_LORENTZ && e->cfg.kernel_param <= 0)
+            fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
+        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
+            fail(KPM_ERR_VALUE, "unknown precision mode");
+        e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
+        *out = e.release();
+    });
+}
+
+int kpm_destroy(kpm_engine* engine) {
+    return guarded([&] {
+        if (engine) {
+            if (engine->stream) cudaStreamSynchronize(engine->stream);
+            delete engine;
+        }
+    });
+}
+
+int kpm_set_hamiltonian(kpm_engine* e, int32_t scalar_type, int64_t rows, const int32_t* indptr,
+                        const int32_t* indices, const void* values, int32_t num_systems,
+                        const int64_t* system_offsets) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
+    });
+}
+
+int kpm_energy_bounds(kpm_engine* e, int32_t system, double* mn, double* mx, int32_t* loops) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (system < 0 || system >= e->nsys) fail(KPM_ERR_VALUE, "system index out of range");
+        e->compute_bounds();
+        if (mn) *mn = e->sys[system].emin;
+        if (mx) *mx = e->sys[system].emax;
+        if (loops) *loops = e->sys[system].loops;
+    });
+}
+
+int kpm_scaling_factors(kpm_engine* e, int32_t system, double* a, double* b) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (system < 0 || system >= e->nsys) fail(KPM_ERR_VALUE, "system index out of range");
+        auto const s = e->scale(system);
+        if (a) *a = s.a;
+        if (b) *b = s.b;
+    });
+}
+
+int kpm_moments_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, const void* starters,
+                     int32_t starters_on_device, int32_t average, double* out, int64_t* num_moments_out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (!starters || !out) fail(KPM_ERR_VALUE, "null starters or output");
+        int64_t const M = round_moments(num_moments);
+        double const t0 = now_s();
+        e->optimize({0}, {0});
+        e->run_diag(M, num_vectors, starters, starters_on_device != 0, nullptr, false);
+        e->reset_stats(M, true, false, static_cast<double>(num_vectors) * e->nsys, 0);
+        int64_t const cols = average ? e->nsys : e->nsys * num_vectors;
+        if (average) {
+            e->d_mu_avg.ensure(sizeof(double) * 2 * e->nsys * M);
+            KPM_CUDA(kpm::launch_average(e->d_mu.as<double>(), e->nsys, num_vectors, M, e->d_mu_avg.as<double>(), e->stream));
+            KPM_CUDA(cudaMemcpyAsync(out, e->d_mu_avg.p, sizeof(double) * 2 * cols * M, cudaMemcpyDeviceToHost, e->stream));
+        } else {
+            KPM_CUDA(cudaMemcpyAsync(out, e->d_mu.p, sizeof(double) * 2 * cols * M, cudaMemcpyDeviceToHost, e->stream));
+        }
+        KPM_CUDA(cudaStreamSynchronize(e->stream));
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+        if (num_moments_out) *num_moments_out = M;
+    });
+}
+
+int kpm_calc_dos(kpm_engine* e, const double* energy, int64_t ne, double broadening, int64_t num_random, double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (num_random < 1) fail(KPM_ERR_VALUE, "num_random must be >= 1");
+        if (ne > 0 && (!energy || !out)) fail(KPM_ERR_VALUE, "null energy or output");
+        double const t0 = now_s();
+        e->compute_bounds();
+        std::vector<int64_t> Ms(e->nsys);
+        int64_t Mmax = 2;
+        for (int s = 0; s < e->nsys; ++s) {
+            Ms[s] = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / e->scale(s).a);
+            Mmax = std::max(Mmax, Ms[s]);
+        }
+        e->optimize({0}, {0});
+        // the reference's random starters: one default-seeded mt19937 per system (Starter.cpp:48-84)
+        int const vb = kpm::vtype_bytes(e->vtype);
+        std::vector<unsigned char> st(static_cast<size_t>(num_random) * e->rows * vb);
+        with_vtype(e->vtype, [&](auto zc) {
+            using Tc = decltype(zc);
+            auto* o = reinterpret_cast<Tc*>(st.data());
+            for (int s = 0; s < e->nsys; ++s) {
+                int64_t const n = e->sys_rows(s);
+                Tc* base = o + e->sys_off[s] * num_random;
+                with_scalar(e->stype, [&](auto zi) {
+                    using Tin = decltype(zi);
+                    using R = real_of<Tin>;
+                    std::mt19937 gen;
+                    std::uniform_real_distribution<R> dist;
+                    for (int64_t v = 0; v < num_random; ++v)
+                        for (int64_t i = 0; i < n; ++i) {
+                            Tin val;
+                            if constexpr (is_cplx_v<Tin>) {
+                                std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
+                                std::complex<R> const k(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
+                                val = std::exp(k * dist(gen));
+                            } else {
+                                val = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
+                            }
+                            base[v * n + i] = convert<Tc>(val);
+                        }
+                });
+            }
+        });
+        e->run_diag(Mmax, num_random, st.data(), false, nullptr, false);
+        e->reset_stats(Mmax, true, false, static_cast<double>(num_random) * e->nsys, 0);
+        e->d_mu_avg.ensure(sizeof(double) * 2 * e->nsys * Mmax);
+        KPM_CUDA(kpm::launch_average(e->d_mu.as<double>(), e->nsys, num_random, Mmax, e->d_mu_avg.as<double>(), e->stream));
+        for (int s = 0; s < e->nsys; ++s) {
+            double* m = e->d_mu_avg.as<double>() + 2 * s * Mmax;
+            e->damp_device(m, Ms[s], 1, Mmax);
+            e->spectral(m, Ms[s], 1, energy, ne, e->scale(s), out + s * ne);
+        }
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_calc_ldos(kpm_engine* e, const int64_t* idx, int64_t nidx, const double* energy, int64_t ne,
+                  double broadening, double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "LDOS needs a single-system engine");
+        if (nidx < 1 || !idx) fail(KPM_ERR_VALUE, "no LDOS indices");
+        double const t0 = now_s();
+        std::vector<int32_t> ii;
+        for (int64_t i = 0; i < nidx; ++i) {
+            if (idx[i] < 0 || idx[i] >= e->rows) fail(KPM_ERR_RUNTIME, "LDOS index out of range");
+            ii.push_back(static_cast<int32_t>(idx[i]));
+        }
+        auto const sc = e->scale(0);
+        int64_t const M = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / sc.a);
+        e->optimize(ii, ii);
+        std::vector<int32_t> pos = e->idx_src;
+        bool const opt = e->cfg.optimal_size != 0 && e->reorders();
+        e->run_diag(M, nidx, nullptr, false, &pos, opt);
+        e->reset_stats(M, true, opt, static_cast<double>(nidx), 0);
+        e->damp_device(e->d_mu.as<double>(), M, nidx, M);
+        e->spectral(e->d_mu.as<double>(), M, static_cast<int>(nidx), energy, ne, sc, out);
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_calc_greens(kpm_engine* e, int64_t row, const int64_t* cols, int64_t ncols, const double* energy, int64_t ne,
+                    double broadening, double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "Green's function needs a single-system engine");
+        if (ncols < 1 || !cols) fail(KPM_ERR_VALUE, "no Green's function columns");
+        int64_t const size = e->rows;
+        bool bad = row < 0 || row > size;
+        for (int64_t j = 0; j < ncols; ++j) bad = bad || cols[j] < 0 || cols[j] > size;
+        if (bad) fail(KPM_ERR_RUNTIME, "KPM::calc_greens(i,j): invalid value for i or j.");
+        double const t0 = now_s();
+        auto const sc = e->scale(0);
+        int64_t const M = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / sc.a);
+        std::vector<int32_t> src{static_cast<int32_t>(row)}, dest;
+        for (int64_t j = 0; j < ncols; ++j) dest.push_back(static_cast<int32_t>(cols[j]));
+        e->optimize(src, dest);
+        bool const opt = e->cfg.optimal_size != 0 && e->reorders();
+        bool const diagonal = src == dest;
+        e->d_energy.ensure(sizeof(double) * std::max<int64_t>(ne, 1));
+        KPM_CUDA(cudaMemcpyAsync(e->d_energy.p, energy, sizeof(double) * ne, cudaMemcpyHostToDevice, e->stream));
+        if (diagonal) {
+            std::vector<int32_t> pos = e->idx_src;
+            e->run_diag(M, 1, nullptr, false, &pos, opt);
+            e->reset_stats(M, true, opt, 1.0, 0);
+            e->damp_device(e->d_mu.as<double>(), M, 1, M);
+            e->d_out.ensure(sizeof(double) * 2 * std::max<int64_t>(ne, 1));
+            KPM_CUDA(kpm::launch_greens(e->d_mu.as<double>(), M, 1, e->d_energy.as<double>(), static_cast<int>(ne), sc.a,
+                                        sc.b, e->d_out.as<double>(), e->stream));
+            KPM_CUDA(cudaMemcpyAsync(out, e->d_out.p, sizeof(double) * 2 * ne, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+        } else {
+            // MultiUnit off-diagonal recursion (calc_moments.hpp:102-114, collectors.cpp:60-76):
+            // r0 = unit at src, collect r_n[dest_j] after every step
+            int const vt = e->vtype;
+            int const vb = kpm::vtype_bytes(vt);
+            int64_t const nd = ncols;
+            e->d_x0.ensure(static_cast<size_t>(e->rows) * vb);
+            e->d_x1.ensure(static_cast<size_t>(e->rows) * vb);
+            e->d_mu.ensure(sizeof(double) * 2 * nd * M);
+            e->d_pos.ensure(sizeof(int32_t) * (nd + 1));
+            KPM_CUDA(cudaMemcpyAsync(e->d_pos.p, e->idx_src.data(), sizeof(int32_t), cudaMemcpyHostToDevice, e->stream));
+            int32_t* d_dest = e->d_pos.as<int32_t>() + 1;
+            KPM_CUDA(cudaMemcpyAsync(d_dest, e->idx_dest.data(), sizeof(int32_t) * nd, cudaMemcpyHostToDevice, e->stream));
+            KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, static_cast<size_t>(e->rows) * vb, e->stream));
+            KPM_CUDA(kpm::launch_set_units(vt, e->d_x0.p, e->d_pos.as<int32_t>(), 1, 1, e->rows, e->stream));
+            kpm_engine::Shape sh{1, 1, 1, 1, 4096};
+            int const ntiles = e->build_tiles(sh, true);
+            std::vector<double> mu(static_cast<size_t>(2 * nd * M));
+            // gather buffers: step n -> d_acc[n * nd]
+            e->d_acc.ensure(sizeof(double) * 2 * nd * M);
+            KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
+            KPM_CUDA(kpm::launch_gather_rows(vt, e->d_x0.p, d_dest, static_cast<int>(nd), e->d_acc.as<double>(), e->stream));
+            kpm::OffStep a{};
+            a.vtype = vt;
+            a.E = 1;
+            a.LPR = 1;
+            a.col = e->d_col.as<int32_t>();
+            a.val = e->d_val.p;
+            a.W = e->W;
+            a.batch_stride = e->rows;
+            a.tiles = e->d_tiles.as<Tile>();
+            a.num_tiles = ntiles;
+            a.row_limit = static_cast<int32_t>(e->rows);
+            a.gamma = nullptr;
+            a.acc = nullptr;
+            a.x = e->d_x0.p;
+            a.y = e->d_x1.p;
+            a.init = true;
+            KPM_CUDA(kpm::launch_off_step(a, e->stream));
+            KPM_CUDA(kpm::launch_gather_rows(vt, e->d_x1.p, d_dest, static_cast<int>(nd), e->d_acc.as<double>() + 2 * nd,
+                                             e->stream));
+            a.init = false;
+            void* r0 = e->d_x0.p;
+            void* r1 = e->d_x1.p;
+            for (int64_t n = 2; n < M; ++n) {
+                a.x = r1;
+                a.y = r0;
+                if (opt) {
+                    int32_t const lim = e->optimal_size(n, M);
+                    a.row_limit = lim;
+                    a.num_tiles = static_cast<int>(std::min<int64_t>(ntiles, (lim + 4095) / 4096));
+                }
+                KPM_CUDA(kpm::launch_off_step(a, e->stream));
+                std::swap(r0, r1);
+                KPM_CUDA(kpm::launch_gather_rows(vt, r1, d_dest, static_cast<int>(nd), e->d_acc.as<double>() + 2 * nd * n,
+                                                 e->stream));
+            }
+            KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
+            KPM_CUDA(cudaMemcpyAsync(mu.data(), e->d_acc.p, sizeof(double) * mu.size(), cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+            float ms = 0;
+            KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+            e->st.moments_time = ms * 1e-3;
+            auto g = damping(e->cfg.kernel, e->cfg.kernel_param, M);
+            std::vector<double> cm(static_cast<size_t>(2 * nd * M));  // [j][n]
+            for (int64_t j = 0; j < nd; ++j)
+                for (int64_t n = 0; n < M; ++n) {
+                    double const h = n == 0 ? 0.5 : 1.0;
+                    cm[2 * (j * M + n)] = mu[2 * (n * nd + j)] * h * g[n];
+                    cm[2 * (j * M + n) + 1] = mu[2 * (n * nd + j) + 1] * h * g[n];
+                }
+            KPM_CUDA(cudaMemcpyAsync(e->d_mu.p, cm.data(), sizeof(double) * cm.size(), cudaMemcpyHostToDevice, e->stream));
+            e->d_out.ensure(sizeof(double) * 2 * std::max<int64_t>(ne * nd, 1));
+            KPM_CUDA(kpm::launch_greens(e->d_mu.as<double>(), M, static_cast<int>(nd), e->d_energy.as<double>(),
+                                        static_cast<int>(ne), sc.a, sc.b, e->d_out.as<double>(), e->stream));
+            KPM_CUDA(cudaMemcpyAsync(out, e->d_out.p, sizeof(double) * 2 * ne * nd, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+            e->reset_stats(M, false, opt, 1.0, 0);
+        }
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_moments(kpm_engine* e, int64_t num_moments, const double* alpha, int64_t alpha_size, const double* beta,
+                int64_t beta_size, int64_t op_rows, const int32_t* op_indptr, const int32_t* op_indices,
+                const double* op_values, double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "moments() needs a single-system engine");
+        int64_t const n = e->rows;
+        // KPM.cpp:20-33 (checked in the reference's unordered_map order: operator, beta, alpha)
+        if (op_rows != 0 && op_rows != n) fail(KPM_ERR_RUNTIME, "Size mismatch between the model Hamiltonian and the given argument 'operator'");
+        if (beta_size != 0 && beta_size != n) fail(KPM_ERR_RUNTIME, "Size mismatch between the model Hamiltonian and the given argument 'beta'");
+        if (alpha_size != n) fail(KPM_ERR_RUNTIME, "Size mismatch between the model Hamiltonian and the given argument 'alpha'");
+        if (!scalar_complex(e->stype)) {  // KPM.cpp:35-48
+            auto has_imag = [](double const* v, int64_t m) {
+                for (int64_t i = 0; i < m; ++i) if (v[2 * i + 1] != 0) return true;
+                return false;
+            };
+            if (op_rows && has_imag(op_values, op_indptr[op_rows])) fail(KPM_ERR_RUNTIME, "The model Hamiltonian is real, but the given argument 'operator' is complex");
+            if (beta_size && has_imag(beta, beta_size)) fail(KPM_ERR_RUNTIME, "The model Hamiltonian is real, but the given argument 'beta' is complex");
+            if (has_imag(alpha, alpha_size)) fail(KPM_ERR_RUNTIME, "The model Hamiltonian is real, but the given argument 'alpha' is complex");
+        }
+        double const t0 = now_s();
+        int64_t const M = round_moments(num_moments);
+        e->optimize({0}, {0});
+        int const vt = e->vtype;
+        int const vb = kpm::vtype_bytes(vt);
+        // alpha in the engine's vector type, original order
+        std::vector<unsigned char> st(static_cast<size_t>(n) * vb);
+        with_vtype(vt, [&](auto zc) {
+            using Tc = decltype(zc);
+            auto* o = reinterpret_cast<Tc*>(st.data());
+            for (int64_t i = 0; i < n; ++i) o[i] = from_cd<Tc>(cd(alpha[2 * i], alpha[2 * i + 1]));
+        });
+        std::vector<double> mu(static_cast<size_t>(2 * M));
+        if (beta_size == 0 && op_rows == 0) {
+            e->run_diag(M, 1, st.data(), false, nullptr, false);
+            KPM_CUDA(cudaMemcpyAsync(mu.data(), e->d_mu.p, sizeof(double) * 2 * M, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+            e->reset_stats(M, true, false, 1.0, 0);
+        } else {
+            // GenericCollector (collectors.cpp:38-58): mu_n = <beta| op r_n> = <gamma | r_n>, gamma = op^H beta
+            std::vector<cd> bv(n), gv(n, cd(0, 0)), av(n);
+            for (int64_t i = 0; i < n; ++i) {
+                av[i] = cd(alpha[2 * i], alpha[2 * i + 1]);
+                bv[i] = beta_size ? cd(beta[2 * i], beta[2 * i + 1]) : av[i];
+            }
+            if (op_rows) {
+                for (int64_t r = 0; r < n; ++r)
+                    for (int32_t k = op_indptr[r]; k < op_indptr[r + 1]; ++k) {
+                        int32_t const c = op_indices[k];
+                        if (c < 0 || c >= n) fail(KPM_ERR_VALUE, "operator column index out of range");
+                        gv[c] += std::conj(cd(op_values[2 * k], op_values[2 * k + 1])) * bv[r];
+                    }
+            } else {
+                gv = bv;
+            }
+            // mu0 = 0.5 <gamma|alpha> on the host (one dot), the rest fused in the step kernel
+            cd mu0(0, 0);
+            for (int64_t i = 0; i < n; ++i) mu0 += std::conj(gv[i]) * av[i];
+            mu0 *= 0.5;
+            std::vector<unsigned char> gam(static_cast<size_t>(n) * vb);
+            with_vtype(vt, [&](auto zc) {
+                using Tc = decltype(zc);
+                auto* o = reinterpret_cast<Tc*>(gam.data());
+                for (int64_t i = 0; i < n; ++i) o[e->map[i]] = from_cd<Tc>(gv[i]);
+            });
+            e->d_gamma.ensure(gam.size());
+            KPM_CUDA(cudaMemcpyAsync(e->d_gamma.p, gam.data(), gam.size(), cudaMemcpyHostToDevice, e->stream));
+            e->d_x0.ensure(st.size());
+            e->d_x1.ensure(st.size());
+            e->d_stage.ensure(st.size());
+            KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, st.data(), st.size(), cudaMemcpyHostToDevice, e->stream));
+            KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, st.size(), e->stream));
+            KPM_CUDA(kpm::launch_scatter_starters(vt, e->d_stage.p, e->d_x0.p, e->d_map.as<int32_t>(),
+                                                  e->d_sysoff.as<int64_t>(), 1, 1, 1, 1, n, e->stream));
+            kpm_engine::Shape sh{1, 1, 1, 1, 4096};
+            int const ntiles = e->build_tiles(sh, true);
+            e->d_acc.ensure(sizeof(double) * 2 * M);
+            KPM_CUDA(cudaMemsetAsync(e->d_acc.p, 0, sizeof(double) * 2 * M, e->stream));
+            kpm::OffStep a{};
+            a.vtype = vt;
+            a.E = 1;
+            a.LPR = 1;
+            a.col = e->d_col.as<int32_t>();
+            a.val = e->d_val.p;
+            a.W = e->W;
+            a.batch_stride = n;
+            a.tiles = e->d_tiles.as<Tile>();
+            a.num_tiles = ntiles;
+            a.row_limit = static_cast<int32_t>(n);
+            a.gamma = e->d_gamma.p;
+            KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
+            a.x = e->d_x0.p;
+            a.y = e->d_x1.p;
+            a.init = true;
+            a.acc = e->d_acc.as<double>() + 2;
+            KPM_CUDA(kpm::launch_off_step(a, e->stream));
+            a.init = false;
+            void* r0 = e->d_x0.p;
+            void* r1 = e->d_x1.p;
+            for (int64_t k = 2; k < M; ++k) {
+                a.x = r1;
+                a.y = r0;
+                a.acc = e->d_acc.as<double>() + 2 * k;
+                KPM_CUDA(kpm::launch_off_step(a, e->stream));
+                std::swap(r0, r1);
+            }
+            KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
+            KPM_CUDA(cudaMemcpyAsync(mu.data(), e->d_acc.p, sizeof(double) * 2 * M, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+            float ms = 0;
+            KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+            e->st.moments_time = ms * 1e-3;
+            mu[0] = mu0.real();
+            mu[1] = mu0.imag();
+            e->reset_stats(M, false, false, 1.0, 0);
+        }
+        auto g = damping(e->cfg.kernel, e->cfg.kernel_param, M);
+        for (int64_t i = 0; i < num_moments; ++i) {
+            out[2 * i] = mu[2 * i] * g[i];
+            out[2 * i + 1] = mu[2 * i + 1] * g[i];
+        }
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, const double* chem, int64_t nmu,
+                          double broadening, double temperature, int64_t num_random, int64_t num_points,
+                          int32_t gemm_mode, double* out) {
+    return guarded([&] {
+        (void)e; (void)left; (void)right; (void)chem; (void)nmu; (void)broadening; (void)temperature;
+        (void)num_random; (void)num_points; (void)gemm_mode; (void)out;
+        fail(KPM_ERR_RUNTIME, "conductivity is not available in this build");
+    });
+}
+
+int kpm_get_stats(kpm_engine* e, kpm_stats* out) {
+    return guarded([&] {
+        if (!e || !out) fail(KPM_ERR_VALUE, "null argument");
+        *out = e->st;
+    });
+}
+
+int kpm_report(kpm_engine* e, int32_t shortform, char* buf, int64_t size) {
+    return guarded([&] {
+        if (!e || !buf || size < 1) fail(KPM_ERR_VALUE, "null argument");
+        auto const& s = e->st;
+        char line[512];
+        std::string r;
+        auto const& b = e->sys.empty() ? kpm_engine::Sys{} : e->sys[0];
+        // Bounds::report (Bounds.cpp:33-39) + Stats::report (Stats.cpp:9-28, 67-69)
+        if (shortform) {
+            std::snprintf(line, sizeof line, "%.2f, %.2f, %d [%s] ", b.emin, b.emax, b.loops, pretty_time(s.bounds_time).c_str());
+            r += line;
+            double const removed = s.nnz ? 100.0 * static_cast<double>(s.nnz - s.opt_nnz) / static_cast<double>(s.nnz) : 0.0;
+            std::snprintf(line, sizeof line, "%.0f%%%s [%s] ", removed, s.uses_full_system ? "" : "*", pretty_time(s.hamiltonian_time).c_str());
+            r += line;
+            std::snprintf(line, sizeof line, "%s @ %seps [%s] ", with_suffix(static_cast<double>(s.num_moments)).c_str(),
+                          with_suffix(s.eps).c_str(), pretty_time(s.moments_time).c_str());
+            r += line;
+            r += "|";
+        } else {
+            std::snprintf(line, sizeof line, "Spectrum bounds found (%.2f, %.2f eV) using Lanczos procedure with %d loops", b.emin, b.emax, b.loops);
+            char l2[640];
+            std::snprintf(l2, sizeof l2, "- %-80s | %s\n", line, pretty_time(s.bounds_time).c_str());
+            r += l2;
+            double const removed = s.nnz ? 100.0 * static_cast<double>(s.nnz - s.opt_nnz) / static_cast<double>(s.nnz) : 0.0;
+            std::snprintf(line, sizeof line, "The reordering optimization was able to remove %.0f%%%s of the workload", removed, s.uses_full_system ? "" : "*");
+            std::snprintf(l2, sizeof l2, "- %-80s | %s\n", line, pretty_time(s.hamiltonian_time).c_str());
+            r += l2;
+            std::snprintf(line, sizeof line, "KPM calculated %s moments at %s non-zero elements per second",
+                          with_suffix(static_cast<double>(s.num_moments)).c_str(), with_suffix(s.eps).c_str());
+            std::snprintf(l2, sizeof l2, "- %-80s | %s\n", line, pretty_time(s.moments_time).c_str());
+            r += l2;
+            r += "Total time:";
+        }
+        r += " " + pretty_time(e->calc_time);
+        std::strncpy(buf, r.c_str(), static_cast<size_t>(size - 1));
+        buf[size - 1] = 0;
+    });
+}
+
+int kpm_optimized_hamiltonian(kpm_engine* e, const int32_t* src, int64_t n_src, const int32_t* dest, int64_t n_dest,
+                              int32_t reorder, int32_t* oip, int32_t* oix, void* ov, int64_t* onnz, int32_t* omap,
+                              int32_t* oslices, int64_t* onslices, int32_t* osrc, int32_t* odest, int64_t* offsets) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "needs a single-system engine");
+        if (n_src < 1 || n_dest < 1) fail(KPM_ERR_VALUE, "empty index lists");
+        for (int64_t i = 0; i < n_src; ++i) if (src[i] < 0 || src[i] >= e->rows) fail(KPM_ERR_VALUE, "src index out of range");
+        for (int64_t i = 0; i < n_dest; ++i) if (dest[i] < 0 || dest[i] >= e->rows) fail(KPM_ERR_VALUE, "dest index out of range");
+        auto const sc = e->scale(0);
+        std::vector<int32_t> s(src, src + n_src), d(dest, dest + n_dest);
+        std::vector<int32_t> ip{0}, ix, borders;
+        std::vector<int32_t> saved_map = e->map;
+        e->map.assign(e->rows, 0);
+        // in H's own scalar type: the reference's arithmetic, bit for bit
+        with_scalar(e->stype, [&](auto z) {
+            using T = decltype(z);
+            std::vector<T> vals;
+            e->reorder_system<T, T>(0, s, sc, reorder != 0, ip, ix, vals, &borders);
+            std::memcpy(ov, vals.data(), vals.size() * sizeof(T));
+        });
+        std::copy(ip.begin(), ip.end(), oip);
+        std::copy(ix.begin(), ix.end(), oix);
+        *onnz = static_cast<int64_t>(ix.size());
+        std::copy(e->map.begin(), e->map.end(), omap);
+        std::copy(borders.begin(), borders.end(), oslices);
+        *onslices = static_cast<int64_t>(borders.size());
+        std::vector<int32_t> os, od;
+        for (auto i : s) os.push_back(e->map[i]);
+        for (auto i : d) od.push_back(e->map[i]);
+        std::copy(os.begin(), os.end(), osrc);
+        std::copy(od.begin(), od.end(), odest);
+        auto find_offset = [&](std::vector<int32_t> const& idx) {
+            int32_t const mx = *std::max_element(idx.begin(), idx.end());
+            auto it = std::find_if(borders.begin(), borders.end(), [&](int32_t v) { return v > mx; });
+            return static_cast<int64_t>(it - borders.begin());
+        };
+        offsets[0] = find_offset(os);
+        offsets[1] = find_offset(od);
+        e->map = saved_map;
+    });
+}
+
+int kpm_get_stream(kpm_engine* e, void** stream) {
+    return guarded([&] {
+        if (!e || !stream) fail(KPM_ERR_VALUE, "null argument");
+        e->ensure_device();
+        *stream = static_cast<void*>(e->stream);
+    });
+}
+
+int kpm_damping_coefficients(int32_t kernel, double param, int64_t M, double* out) {
+    return guarded([&] {
+        if (M < 0 || (M > 0 && !out)) fail(KPM_ERR_VALUE, "bad arguments");
+        if (kernel == KPM_KERNEL_LORENTZ && param <= 0) fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
+        auto g = damping(kernel, param, M);
+        std::copy(g.begin(), g.end(), out);
+    });
+}
+
+int64_t kpm_required_num_moments(int32_t kernel, double param, double scaled_broadening) {
+    return required_moments(kernel, param, scaled_broadening);
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// Internal interface between the host engine (kpm_engine.cpp) and the CUDA
+// kernels (kpm_kernels.cu). Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace kpm {
+
+// vector / matrix element types on the device
+enum VType : int { V_F32 = 0, V_F64 = 1, V_C64 = 2, V_C128 = 3 };
+
+inline int vtype_bytes(int vt) { return vt == V_F32 ? 4 : (vt == V_C128 ? 16 : 8); }
+inline bool vtype_complex(int vt) { return vt == V_C64 || vt == V_C128; }
+inline bool vtype_double(int vt) { return vt == V_F64 || vt == V_C128; }
+// moment sums per vector: real: (|x|^2, <y|x>), complex: (|x|^2, Re<y|x>, Im<y|x>)
+inline int vtype_nv(int vt) { return vtype_complex(vt) ? 3 : 2; }
+
+// A tile: rows [row_begin, row_end) of one system for one batch of vectors.
+struct Tile {
+    int32_t row_begin, row_end, system, batch;
+};
+
+// One step of the diagonal recursion, y <- H~ x - y (or y <- H~ x / 2 when init),
+// with the moment sums m2 += |x_r|^2, m3 += conj(y_r) x_r per vector accumulated
+// into acc[((system * nbatch + batch) * K + v) * NV + q].
+struct DiagStep {
+    int vtype;
+    int E, LPR;               // K = E * LPR vectors per batch
+    const int32_t* col;       // [rows_total][W]
+    const void* val;          // [rows_total][W], vtype
+    int W;
+    const void* x;            // [nbatch][rows_total][K]
+    void* y;
+    int64_t batch_stride;     // rows_total * K elements
+    const Tile* tiles;
+    int num_tiles;
+    int32_t row_limit;        // rows >= row_limit are skipped (optimal size)
+    int nbatch;
+    double* acc;
+    bool init;
+};
+
+// Off-diagonal step: y <- H~ x - y (or H~ x / 2 when init), optional fused dot
+// acc[batch*K+v] += <gamma_r | y_r> (complex sums, 2 doubles) when gamma != nullptr,
+// optional store of y into `store` (dense matrix of vectors, row n).
+struct OffStep {
+    int vtype;
+    int E, LPR;
+    const int32_t* col;
+    const void* val;
+    int W;
+    const void* x;
+    void* y;
+    int64_t batch_stride;
+    const Tile* tiles;
+    int num_tiles;
+    int32_t row_limit;
+    bool init;
+    const void* gamma;        // [rows_total] (single vector), nullable
+    double* acc;
+};
+
+cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s);
+cudaError_t launch_off_step(OffStep const& a, cudaStream_t s);
+bool diag_shape_supported(int vtype, int E, int LPR);
+
+// moments from the accumulated sums: out[(s*nbatch*K + v) * M + n] complex double,
+// or averaged over `nvec` vectors per system into out[s * M + n] when average.
+cudaError_t launch_collect_diag(int vtype, double const* acc, int num_systems, int nbatch, int K,
+                                int64_t half_M, int64_t M, int64_t nvec, bool average, double* out,
+                                cudaStream_t s);
+
+cudaError_t launch_average(double const* per_vec, int num_systems, int64_t nvec, int64_t M, double* out,
+                           cudaStream_t s);
+
+// unit starters: dst[(b * rows_total + pos[v]) * K + j] = 1 for v = b*K + j < nvec
+cudaError_t launch_set_units(int vtype, void* dst, int32_t const* pos, int64_t nvec, int K, int64_t rows_total,
+                             cudaStream_t s);
+
+// scatter host-order starters into the reordered, batched device layout:
+// dst[(b * rows_total + map[g]) * K + j] = src[(s, v, i)], v = b*K + j
+cudaError_t launch_scatter_starters(int vtype, void const* src, void* dst, int32_t const* map,
+                                    int64_t const* sys_offsets, int num_systems, int64_t nvec,
+                                    int K, int nbatch, int64_t rows_total, cudaStream_t s);
+
+// gather y[dest[i]] (batch 0, vector 0) into out[n * ndest + i] as complex double
+cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, int ndest, double* out,
+                               cudaStream_t s);
+
+// Lanczos (FP64 or complex FP64, all systems in lockstep, CSR per system in global rows)
+// A: t = H v1; v0 = t - bprev[s] v0; alpha[s] += Re(conj(t) v1)
+// B: v0 -= alpha[s] v1; nrm[s] += |v0|^2
+// C: v0 *= 1/sqrt(nrm[s])
+cudaError_t launch_lanczos_a(bool cplx, int32_t const* ip, int32_t const* ix, void const* v,
+                             void const* v1, void* v0, Tile const* tiles, int num_tiles,
+                             double const* bprev, double* alpha, cudaStream_t s);
+cudaError_t launch_lanczos_b(bool cplx, void const* v1, void* v0, Tile const* tiles, int num_tiles,
+                             double const* alpha, double* nrm, cudaStream_t s);
+cudaError_t launch_lanczos_c(bool cplx, void* v0, Tile const* tiles, int num_tiles, double const* nrm,
+                             cudaStream_t s);
+
+// reconstruction in FP64: out[c * ne + e] = k/sqrt(1-E^2) sum_n Re(mu[c*M+n]) cos(n acos E)
+cudaError_t launch_spectral_density(double const* mu, int64_t M, int cols, double const* energy, int ne,
+                                    double a, double b, double* out, cudaStream_t s);
+// Green's: out[c * ne + e] = -2i/(a sqrt(1-E^2)) sum_n mu[c*M+n] exp(-i n acos E) (complex)
+cudaError_t launch_greens(double const* mu, int64_t M, int cols, double const* energy, int ne, double a,
+                          double b, double* out, cudaStream_t s);
+
+}  // namespace kpm

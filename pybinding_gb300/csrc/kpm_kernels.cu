@@ -1,0 +1,690 @@
+// CUDA kernels of the GB300 KPM engine (sm_103a).
+//
+// The hot path is one step of the Chebyshev recursion over a block of K
+// vectors, y <- H~ x - y, as an ELL SpMM with the two moment dot products of the
+// diagonal KPM (m2 = |x|^2, m3 = <y|x>) fused into the same pass
+// (cppcore/include/compute/kernel_polynomial.hpp:219-323 is the CPU form).
+//
+// Layout: the matrix is padded ELL, row-major per row ([row][W] indices and
+// values, padding = (row, 0)), so one row's entries are one contiguous load
+// shared by the lanes that work on that row. A vector block is row-major,
+// [row][K] with the K vectors interleaved per row, so gathering x[col] reads
+// K contiguous elements: each lane loads 16 bytes (E elements) and LPR lanes
+// cover a row. Vector blocks of all batches live side by side
+// ([batch][row][K]) and one launch covers every batch and every system of a
+// ragged batch through a tile list (rows of one system x one batch).
+//
+// Moment sums: each thread accumulates its rows in the vector precision
+// (FP32 for FP32 vectors), the block reduces them (shuffles + shared memory,
+// still FP32), and one FP64 atomic add per (block, vector, sum) lands in a
+// per-step FP64 accumulator. Per-element FP64 work is avoided on purpose:
+// GB300's FP64 rate is ~1/300 of its FP32 rate.
+#include "kpm_internal.h"
+
+#include <cstdint>
+#include <cstring>
+
+namespace kpm {
+namespace {
+
+constexpr int BLOCK = 256;
+constexpr int WARPS = BLOCK / 32;
+
+template<class V> struct Tr;
+template<> struct Tr<float> { using R = float; static constexpr bool C = false; };
+template<> struct Tr<double> { using R = double; static constexpr bool C = false; };
+template<> struct Tr<float2> { using R = float; static constexpr bool C = true; };
+template<> struct Tr<double2> { using R = double; static constexpr bool C = true; };
+
+__device__ __forceinline__ void vzero(float& a) { a = 0.f; }
+__device__ __forceinline__ void vzero(double& a) { a = 0.0; }
+__device__ __forceinline__ void vzero(float2& a) { a = make_float2(0.f, 0.f); }
+__device__ __forceinline__ void vzero(double2& a) { a = make_double2(0.0, 0.0); }
+
+// acc += a * x
+__device__ __forceinline__ void vfma(float& acc, float a, float x) { acc = fmaf(a, x, acc); }
+__device__ __forceinline__ void vfma(double& acc, double a, double x) { acc = fma(a, x, acc); }
+__device__ __forceinline__ void vfma(float2& acc, float2 a, float2 x) {
+    acc.x = fmaf(a.x, x.x, acc.x);
+    acc.x = fmaf(-a.y, x.y, acc.x);
+    acc.y = fmaf(a.x, x.y, acc.y);
+    acc.y = fmaf(a.y, x.x, acc.y);
+}
+__device__ __forceinline__ void vfma(double2& acc, double2 a, double2 x) {
+    acc.x = fma(a.x, x.x, acc.x);
+    acc.x = fma(-a.y, x.y, acc.x);
+    acc.y = fma(a.x, x.y, acc.y);
+    acc.y = fma(a.y, x.x, acc.y);
+}
+__device__ __forceinline__ float vsub(float a, float b) { return a - b; }
+__device__ __forceinline__ double vsub(double a, double b) { return a - b; }
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 vsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float vhalf(float a) { return 0.5f * a; }
+__device__ __forceinline__ double vhalf(double a) { return 0.5 * a; }
+__device__ __forceinline__ float2 vhalf(float2 a) { return make_float2(0.5f * a.x, 0.5f * a.y); }
+__device__ __forceinline__ double2 vhalf(double2 a) { return make_double2(0.5 * a.x, 0.5 * a.y); }
+// |x|^2
+__device__ __forceinline__ float vsq(float a) { return a * a; }
+__device__ __forceinline__ double vsq(double a) { return a * a; }
+__device__ __forceinline__ float vsq(float2 a) { return fmaf(a.x, a.x, a.y * a.y); }
+__device__ __forceinline__ double vsq(double2 a) { return fma(a.x, a.x, a.y * a.y); }
+// conj(y) * x
+__device__ __forceinline__ float vdre(float y, float x) { return y * x; }
+__device__ __forceinline__ double vdre(double y, double x) { return y * x; }
+__device__ __forceinline__ float vdre(float2 y, float2 x) { return fmaf(y.x, x.x, y.y * x.y); }
+__device__ __forceinline__ double vdre(double2 y, double2 x) { return fma(y.x, x.x, y.y * x.y); }
+__device__ __forceinline__ float vdim(float, float) { return 0.f; }
+__device__ __forceinline__ double vdim(double, double) { return 0.0; }
+__device__ __forceinline__ float vdim(float2 y, float2 x) { return fmaf(y.x, x.y, -y.y * x.x); }
+__device__ __forceinline__ double vdim(double2 y, double2 x) { return fma(y.x, x.y, -y.y * x.x); }
+
+// E elements of V in one aligned register pack (4, 8 or 16 bytes)
+template<class V, int E>
+struct alignas(sizeof(V) * E) Pack {
+    V v[E];
+};
+template<int B> struct Raw;
+template<> struct Raw<4> { using T = float; };
+template<> struct Raw<8> { using T = float2; };
+template<> struct Raw<16> { using T = float4; };
+
+template<class P>
+__device__ __forceinline__ P ld_ro(P const* p) {  // read-only path (L1 cached): x gathers
+    using T = typename Raw<sizeof(P)>::T;
+    T t = __ldg(reinterpret_cast<T const*>(p));
+    P r;
+    memcpy(&r, &t, sizeof(P));
+    return r;
+}
+template<class P>
+__device__ __forceinline__ P ld_stream(P const* p) {  // streamed once: y_old
+    using T = typename Raw<sizeof(P)>::T;
+    T t = __ldcs(reinterpret_cast<T const*>(p));
+    P r;
+    memcpy(&r, &t, sizeof(P));
+    return r;
+}
+template<class P>
+__device__ __forceinline__ void st_stream(P* p, P const& v) {
+    using T = typename Raw<sizeof(P)>::T;
+    T t;
+    memcpy(&t, &v, sizeof(P));
+    __stcs(reinterpret_cast<T*>(p), t);
+}
+
+// ------------------------------------------------------------------ diagonal step
+template<class V, int E, int LPR, bool INIT>
+__global__ void __launch_bounds__(BLOCK)
+diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
+                 V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+                 Tile const* __restrict__ tiles, int32_t row_limit, int nbatch, double* __restrict__ acc) {
+    using R = typename Tr<V>::R;
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;  // rows per pass of the block
+    constexpr int NV = CPLX ? 3 : 2;
+    using P = Pack<V, E>;
+
+    Tile const t = tiles[blockIdx.x];
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    V const* __restrict__ x = x_all + t.batch * batch_stride;
+    V* __restrict__ y = y_all + t.batch * batch_stride;
+    int const row_end = min(t.row_end, row_limit);
+
+    R m2[E], m3r[E], m3i[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+
+    for (int r = t.row_begin + slot; r < row_end; r += RPP) {
+        V sum[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) vzero(sum[e]);
+        int32_t const* cp = col + static_cast<int64_t>(r) * W;
+        V const* vp = val + static_cast<int64_t>(r) * W;
+        for (int j = 0; j < W; ++j) {
+            int32_t const c = __ldg(cp + j);
+            V const a = vp[j];
+            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
+#pragma unroll
+            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+        }
+        P const xr = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane);
+        P* yp = reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane;
+        P yn;
+        if (INIT) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) yn.v[e] = vhalf(sum[e]);
+        } else {
+            P const yo = ld_stream(yp);
+#pragma unroll
+            for (int e = 0; e < E; ++e) yn.v[e] = vsub(sum[e], yo.v[e]);
+        }
+        st_stream(yp, yn);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            m2[e] += vsq(xr.v[e]);
+            m3r[e] += vdre(yn.v[e], xr.v[e]);
+            if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
+        }
+    }
+
+    // reduce over the rows of the block: lanes with equal (threadIdx % LPR) hold the same vectors
+#pragma unroll
+    for (int off = LPR; off < 32; off <<= 1) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            m2[e] += __shfl_xor_sync(0xffffffffu, m2[e], off);
+            m3r[e] += __shfl_xor_sync(0xffffffffu, m3r[e], off);
+            if (CPLX) m3i[e] += __shfl_xor_sync(0xffffffffu, m3i[e], off);
+        }
+    }
+    __shared__ R red[WARPS][K][NV];
+    int const warp = threadIdx.x / 32;
+    int const wl = threadIdx.x % 32;
+    if (wl < LPR) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            red[warp][wl * E + e][0] = m2[e];
+            red[warp][wl * E + e][1] = m3r[e];
+            if (CPLX) red[warp][wl * E + e][NV - 1] = m3i[e];
+        }
+    }
+    __syncthreads();
+    double* a = acc + static_cast<int64_t>(t.system * nbatch + t.batch) * K * NV;
+    for (int i = threadIdx.x; i < K * NV; i += BLOCK) {
+        R s = R(0);
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) s += red[w][i / NV][i % NV];
+        atomicAdd(a + i, static_cast<double>(s));
+    }
+}
+
+// ------------------------------------------------------------------ off-diagonal step
+template<class V, int E, int LPR, bool INIT>
+__global__ void __launch_bounds__(BLOCK)
+off_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
+                V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+                Tile const* __restrict__ tiles, int32_t row_limit, V const* __restrict__ gamma,
+                double* __restrict__ acc) {
+    using R = typename Tr<V>::R;
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;
+    using P = Pack<V, E>;
+    Tile const t = tiles[blockIdx.x];
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    V const* __restrict__ x = x_all + t.batch * batch_stride;
+    V* __restrict__ y = y_all + t.batch * batch_stride;
+    int const row_end = min(t.row_end, row_limit);
+    R dre[E], dim[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) { dre[e] = R(0); dim[e] = R(0); }
+    for (int r = t.row_begin + slot; r < row_end; r += RPP) {
+        V sum[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) vzero(sum[e]);
+        int32_t const* cp = col + static_cast<int64_t>(r) * W;
+        V const* vp = val + static_cast<int64_t>(r) * W;
+        for (int j = 0; j < W; ++j) {
+            int32_t const c = __ldg(cp + j);
+            V const a = vp[j];
+            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
+#pragma unroll
+            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+        }
+        P* yp = reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane;
+        P yn;
+        if (INIT) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) yn.v[e] = vhalf(sum[e]);
+        } else {
+            P const yo = *yp;
+#pragma unroll
+            for (int e = 0; e < E; ++e) yn.v[e] = vsub(sum[e], yo.v[e]);
+        }
+        *yp = yn;
+        if (gamma != nullptr) {
+            V const g = gamma[r];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                dre[e] += vdre(g, yn.v[e]);
+                dim[e] += vdim(g, yn.v[e]);
+            }
+        }
+    }
+    if (gamma == nullptr) return;
+#pragma unroll
+    for (int off = LPR; off < 32; off <<= 1)
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            dre[e] += __shfl_xor_sync(0xffffffffu, dre[e], off);
+            dim[e] += __shfl_xor_sync(0xffffffffu, dim[e], off);
+        }
+    __shared__ R red[WARPS][K][2];
+    int const warp = threadIdx.x / 32;
+    int const wl = threadIdx.x % 32;
+    if (wl < LPR)
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            red[warp][wl * E + e][0] = dre[e];
+            red[warp][wl * E + e][1] = dim[e];
+        }
+    __syncthreads();
+    double* a = acc + static_cast<int64_t>(t.batch) * K * 2;
+    for (int i = threadIdx.x; i < K * 2; i += BLOCK) {
+        R s = R(0);
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) s += red[w][i / 2][i % 2];
+        atomicAdd(a + i, static_cast<double>(s));
+    }
+}
+
+template<class V, int E, int LPR>
+cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    auto const* val = static_cast<V const*>(a.val);
+    auto const* x = static_cast<V const*>(a.x);
+    auto* y = static_cast<V*>(a.y);
+    if (a.init)
+        diag_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride,
+                                                                        a.tiles, a.row_limit, a.nbatch, a.acc);
+    else
+        diag_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride,
+                                                                         a.tiles, a.row_limit, a.nbatch, a.acc);
+    return cudaGetLastError();
+}
+
+template<class V, int E, int LPR>
+cudaError_t off_launch(OffStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    auto const* val = static_cast<V const*>(a.val);
+    auto const* x = static_cast<V const*>(a.x);
+    auto* y = static_cast<V*>(a.y);
+    auto const* g = static_cast<V const*>(a.gamma);
+    if (a.init)
+        off_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride,
+                                                                       a.tiles, a.row_limit, g, a.acc);
+    else
+        off_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride,
+                                                                        a.tiles, a.row_limit, g, a.acc);
+    return cudaGetLastError();
+}
+
+// supported (E, LPR) shapes per element type: E fills 16 bytes, or E = 1 for one vector
+#define KPM_SHAPES_F32(X) X(float, 1, 1) X(float, 4, 2) X(float, 4, 4) X(float, 4, 8) X(float, 4, 16) X(float, 4, 32)
+#define KPM_SHAPES_F64(X) X(double, 1, 1) X(double, 2, 2) X(double, 2, 4) X(double, 2, 8) X(double, 2, 16) X(double, 2, 32)
+#define KPM_SHAPES_C64(X) X(float2, 1, 1) X(float2, 2, 2) X(float2, 2, 4) X(float2, 2, 8) X(float2, 2, 16) X(float2, 2, 32)
+#define KPM_SHAPES_C128(X) X(double2, 1, 1) X(double2, 1, 2) X(double2, 1, 4) X(double2, 1, 8) X(double2, 1, 16) X(double2, 1, 32)
+
+template<class V> constexpr int vcode();
+template<> constexpr int vcode<float>() { return V_F32; }
+template<> constexpr int vcode<double>() { return V_F64; }
+template<> constexpr int vcode<float2>() { return V_C64; }
+template<> constexpr int vcode<double2>() { return V_C128; }
+
+// ------------------------------------------------------------------ collect
+__global__ void collect_diag_kernel(double const* __restrict__ acc, int NV, int num_systems, int nbatch, int K,
+                                    int64_t half_M, int64_t M, int64_t nvec, double* __restrict__ out) {
+    int64_t const per_sys = nvec * half_M;
+    int64_t const total = per_sys * num_systems;
+    int64_t const step_stride = static_cast<int64_t>(num_systems) * nbatch * K * NV;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t const s = i / per_sys;
+        int64_t const rem = i % per_sys;
+        int64_t const v = rem / half_M;
+        int64_t const n = rem % half_M;
+        int64_t const b = v / K, j = v % K;
+        int64_t const base = ((s * nbatch + b) * K + j) * NV;
+        double const m0 = acc[base];
+        double const m1r = acc[base + 1];
+        double const m1i = NV == 3 ? acc[base + 2] : 0.0;
+        double* o = out + ((s * nvec + v) * M) * 2;
+        if (n == 0) {
+            o[0] = 0.5 * m0; o[1] = 0.0;
+            o[2] = m1r; o[3] = m1i;
+        } else {
+            double const* a = acc + n * step_stride + base;
+            double const m2 = a[0], m3r = a[1], m3i = NV == 3 ? a[2] : 0.0;
+            o[4 * n] = 2.0 * m2 - m0;  // 2 (m2 - mu0), mu0 = m0 / 2
+            o[4 * n + 1] = 0.0;
+            o[4 * n + 2] = 2.0 * m3r - m1r;
+            o[4 * n + 3] = 2.0 * m3i - m1i;
+        }
+    }
+}
+
+__global__ void average_kernel(double const* __restrict__ per_vec, int num_systems, int64_t nvec, int64_t M,
+                               double* __restrict__ out) {
+    int64_t const total = static_cast<int64_t>(num_systems) * M;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t const s = i / M, n = i % M;
+        double re = 0.0, im = 0.0;
+        for (int64_t v = 0; v < nvec; ++v) {
+            double const* p = per_vec + ((s * nvec + v) * M + n) * 2;
+            re += p[0];
+            im += p[1];
+        }
+        double const inv = nvec != 1 ? 1.0 / static_cast<double>(nvec) : 1.0;
+        out[2 * i] = re * inv;
+        out[2 * i + 1] = im * inv;
+    }
+}
+
+// ------------------------------------------------------------------ starters scatter
+template<class V>
+__global__ void scatter_kernel(V const* __restrict__ src, V* __restrict__ dst, int32_t const* __restrict__ map,
+                               int64_t const* __restrict__ sys_off, int num_systems, int64_t nvec, int K,
+                               int64_t rows_total) {
+    int64_t const v = blockIdx.y;
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < rows_total;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int lo = 0, hi = num_systems;  // find s with sys_off[s] <= g < sys_off[s+1]
+        while (hi - lo > 1) {
+            int const mid = (lo + hi) / 2;
+            if (sys_off[mid] <= g) lo = mid; else hi = mid;
+        }
+        int64_t const off = sys_off[lo];
+        int64_t const rows_s = sys_off[lo + 1] - off;
+        V const value = src[off * nvec + v * rows_s + (g - off)];
+        int64_t const b = v / K, j = v % K;
+        dst[(b * rows_total + map[g]) * K + j] = value;
+    }
+}
+
+template<class V>
+__global__ void set_units_kernel(V* __restrict__ dst, int32_t const* __restrict__ pos, int64_t nvec, int K,
+                                 int64_t rows_total) {
+    int64_t const v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (v >= nvec) return;
+    V one;
+    vzero(one);
+    if constexpr (Tr<V>::C) one.x = 1; else one = 1;
+    dst[((v / K) * rows_total + pos[v]) * K + v % K] = one;
+}
+
+template<class V>
+__global__ void gather_rows_kernel(V const* __restrict__ y, int32_t const* __restrict__ dest, int ndest,
+                                   double* __restrict__ out) {
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ndest) return;
+    V const v = y[dest[i]];
+    if constexpr (Tr<V>::C) {
+        out[2 * i] = static_cast<double>(v.x);
+        out[2 * i + 1] = static_cast<double>(v.y);
+    } else {
+        out[2 * i] = static_cast<double>(v);
+        out[2 * i + 1] = 0.0;
+    }
+}
+
+// ------------------------------------------------------------------ Lanczos (FP64)
+template<class V>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (threadIdx.x % 32 == 0) sh[threadIdx.x / 32] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < WARPS; ++w) s += sh[w];
+    return s;
+}
+
+template<class V>
+__global__ void __launch_bounds__(BLOCK)
+lanczos_a_kernel(int32_t const* __restrict__ ip, int32_t const* __restrict__ ix, V const* __restrict__ hv,
+                 V const* __restrict__ v1, V* __restrict__ v0, Tile const* __restrict__ tiles,
+                 double const* __restrict__ bprev, double* __restrict__ alpha) {
+    __shared__ double sh[WARPS];
+    Tile const t = tiles[blockIdx.x];
+    double const bp = bprev[t.system];
+    double a = 0.0;
+    for (int r = t.row_begin + threadIdx.x; r < t.row_end; r += BLOCK) {
+        V sum;
+        vzero(sum);
+        for (int k = ip[r]; k < ip[r + 1]; ++k) vfma(sum, hv[k], v1[ix[k]]);
+        V const old = v0[r];
+        if constexpr (Tr<V>::C) v0[r] = make_double2(sum.x - bp * old.x, sum.y - bp * old.y);
+        else v0[r] = sum - bp * old;
+        a += vdre(sum, v1[r]);
+    }
+    double const s = block_sum<V>(a, sh);
+    if (threadIdx.x == 0) atomicAdd(alpha + t.system, s);
+}
+
+template<class V>
+__global__ void __launch_bounds__(BLOCK)
+lanczos_b_kernel(V const* __restrict__ v1, V* __restrict__ v0, Tile const* __restrict__ tiles,
+                 double const* __restrict__ alpha, double* __restrict__ nrm) {
+    __shared__ double sh[WARPS];
+    Tile const t = tiles[blockIdx.x];
+    double const a = alpha[t.system];
+    double n2 = 0.0;
+    for (int r = t.row_begin + threadIdx.x; r < t.row_end; r += BLOCK) {
+        V l = v0[r];
+        V const x = v1[r];
+        if constexpr (Tr<V>::C) { l.x -= a * x.x; l.y -= a * x.y; }
+        else l -= a * x;
+        v0[r] = l;
+        n2 += vsq(l);
+    }
+    double const s = block_sum<V>(n2, sh);
+    if (threadIdx.x == 0) atomicAdd(nrm + t.system, s);
+}
+
+template<class V>
+__global__ void __launch_bounds__(BLOCK)
+lanczos_c_kernel(V* __restrict__ v0, Tile const* __restrict__ tiles, double const* __restrict__ nrm) {
+    Tile const t = tiles[blockIdx.x];
+    double const inv = 1.0 / sqrt(nrm[t.system]);
+    for (int r = t.row_begin + threadIdx.x; r < t.row_end; r += BLOCK) {
+        V l = v0[r];
+        if constexpr (Tr<V>::C) { l.x *= inv; l.y *= inv; }
+        else l *= inv;
+        v0[r] = l;
+    }
+}
+
+// ------------------------------------------------------------------ reconstruction (FP64)
+// cos(n t) for the thread's contiguous chunk of n by the Chebyshev recurrence
+// T_{n+1} = 2 E T_n - T_{n-1}, seeded with two direct evaluations per chunk.
+__global__ void spectral_density_kernel(double const* __restrict__ mu, int64_t M, double const* __restrict__ energy,
+                                        int ne, double a, double b, double* __restrict__ out) {
+    __shared__ double sh[WARPS];
+    int const e = blockIdx.x, c = blockIdx.y;
+    double const E = (energy[e] - b) / a;
+    double const th = acos(E);
+    int64_t const chunk = (M + BLOCK - 1) / BLOCK;
+    int64_t const n0 = threadIdx.x * chunk;
+    int64_t const n1 = min(M, n0 + chunk);
+    double s = 0.0;
+    if (n0 < n1) {
+        double tm1 = cos(static_cast<double>(n0) * th);
+        double t0 = cos(static_cast<double>(n0 + 1) * th);
+        double const* m = mu + (static_cast<int64_t>(c) * M) * 2;
+        s = m[2 * n0] * tm1;
+        for (int64_t n = n0 + 1; n < n1; ++n) {
+            s = fma(m[2 * n], t0, s);
+            double const tn = fma(2.0 * E, t0, -tm1);
+            tm1 = t0;
+            t0 = tn;
+        }
+    }
+    double const tot = block_sum<double>(s, sh);
+    if (threadIdx.x == 0) {
+        double const k = 2.0 / (M_PI * a);
+        out[static_cast<int64_t>(c) * ne + e] = k / sqrt(1.0 - E * E) * tot;
+    }
+}
+
+__global__ void greens_kernel(double const* __restrict__ mu, int64_t M, double const* __restrict__ energy, int ne,
+                              double a, double b, double* __restrict__ out) {
+    __shared__ double shr[WARPS], shi[WARPS];
+    int const e = blockIdx.x, c = blockIdx.y;
+    double const E = (energy[e] - b) / a;
+    double const th = acos(E);
+    int64_t const chunk = (M + BLOCK - 1) / BLOCK;
+    int64_t const n0 = threadIdx.x * chunk;
+    int64_t const n1 = min(M, n0 + chunk);
+    double sr = 0.0, si = 0.0;
+    if (n0 < n1) {
+        // z_n = exp(-i n t), advanced by w = exp(-i t)
+        double zr = cos(static_cast<double>(n0) * th), zi = -sin(static_cast<double>(n0) * th);
+        double const wr = cos(th), wi = -sin(th);
+        double const* m = mu + (static_cast<int64_t>(c) * M) * 2;
+        for (int64_t n = n0; n < n1; ++n) {
+            double const mr = m[2 * n], mi = m[2 * n + 1];
+            sr += mr * zr - mi * zi;
+            si += mr * zi + mi * zr;
+            double const nr = zr * wr - zi * wi;
+            double const ni = zr * wi + zi * wr;
+            zr = nr;
+            zi = ni;
+        }
+    }
+    double const tr = block_sum<double>(sr, shr);
+    __syncthreads();
+    double const ti = block_sum<double>(si, shi);
+    if (threadIdx.x == 0) {
+        // k = -2i / a / sqrt(1 - E^2); g = k * (tr + i ti)
+        double const f = 2.0 / (a * sqrt(1.0 - E * E));
+        double* o = out + (static_cast<int64_t>(c) * ne + e) * 2;
+        o[0] = f * ti;
+        o[1] = -f * tr;
+    }
+}
+
+int grid_for(int64_t n, int block = BLOCK) {
+    int64_t g = (n + block - 1) / block;
+    if (g > 152 * 64) g = 152 * 64;
+    return static_cast<int>(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+bool diag_shape_supported(int vtype, int E, int LPR) {
+#define KPM_CHECK(V, e, l) if (vtype == vcode<V>() && E == e && LPR == l) return true;
+    KPM_SHAPES_F32(KPM_CHECK) KPM_SHAPES_F64(KPM_CHECK) KPM_SHAPES_C64(KPM_CHECK) KPM_SHAPES_C128(KPM_CHECK)
+#undef KPM_CHECK
+    return false;
+}
+
+cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s) {
+#define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return diag_launch<V, e, l>(a, s);
+    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
+#undef KPM_DISPATCH
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_off_step(OffStep const& a, cudaStream_t s) {
+#define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return off_launch<V, e, l>(a, s);
+    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
+#undef KPM_DISPATCH
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_collect_diag(int vtype, double const* acc, int num_systems, int nbatch, int K, int64_t half_M,
+                                int64_t M, int64_t nvec, bool average, double* out, cudaStream_t s) {
+    int const NV = vtype_nv(vtype);
+    (void)average;
+    collect_diag_kernel<<<grid_for(static_cast<int64_t>(num_systems) * nvec * half_M), BLOCK, 0, s>>>(
+        acc, NV, num_systems, nbatch, K, half_M, M, nvec, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_average(double const* per_vec, int num_systems, int64_t nvec, int64_t M, double* out,
+                           cudaStream_t s) {
+    average_kernel<<<grid_for(static_cast<int64_t>(num_systems) * M), BLOCK, 0, s>>>(per_vec, num_systems, nvec, M,
+                                                                                  out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_starters(int vtype, void const* src, void* dst, int32_t const* map,
+                                    int64_t const* sys_offsets, int num_systems, int64_t nvec, int K, int nbatch,
+                                    int64_t rows_total, cudaStream_t s) {
+    (void)nbatch;
+    if (nvec == 0 || rows_total == 0) return cudaSuccess;
+    dim3 grid(grid_for(rows_total) > 4096 ? 4096 : grid_for(rows_total), static_cast<unsigned>(nvec));
+    switch (vtype) {
+        case V_F32: scatter_kernel<float><<<grid, BLOCK, 0, s>>>(static_cast<float const*>(src), static_cast<float*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
+        case V_F64: scatter_kernel<double><<<grid, BLOCK, 0, s>>>(static_cast<double const*>(src), static_cast<double*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
+        case V_C64: scatter_kernel<float2><<<grid, BLOCK, 0, s>>>(static_cast<float2 const*>(src), static_cast<float2*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
+        default: scatter_kernel<double2><<<grid, BLOCK, 0, s>>>(static_cast<double2 const*>(src), static_cast<double2*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_units(int vtype, void* dst, int32_t const* pos, int64_t nvec, int K, int64_t rows_total,
+                             cudaStream_t s) {
+    if (nvec == 0) return cudaSuccess;
+    int const g = static_cast<int>((nvec + 127) / 128);
+    switch (vtype) {
+        case V_F32: set_units_kernel<float><<<g, 128, 0, s>>>(static_cast<float*>(dst), pos, nvec, K, rows_total); break;
+        case V_F64: set_units_kernel<double><<<g, 128, 0, s>>>(static_cast<double*>(dst), pos, nvec, K, rows_total); break;
+        case V_C64: set_units_kernel<float2><<<g, 128, 0, s>>>(static_cast<float2*>(dst), pos, nvec, K, rows_total); break;
+        default: set_units_kernel<double2><<<g, 128, 0, s>>>(static_cast<double2*>(dst), pos, nvec, K, rows_total); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, int ndest, double* out, cudaStream_t s) {
+    if (ndest == 0) return cudaSuccess;
+    int const g = (ndest + 127) / 128;
+    switch (vtype) {
+        case V_F32: gather_rows_kernel<float><<<g, 128, 0, s>>>(static_cast<float const*>(y), dest, ndest, out); break;
+        case V_F64: gather_rows_kernel<double><<<g, 128, 0, s>>>(static_cast<double const*>(y), dest, ndest, out); break;
+        case V_C64: gather_rows_kernel<float2><<<g, 128, 0, s>>>(static_cast<float2 const*>(y), dest, ndest, out); break;
+        default: gather_rows_kernel<double2><<<g, 128, 0, s>>>(static_cast<double2 const*>(y), dest, ndest, out); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lanczos_a(bool cplx, int32_t const* ip, int32_t const* ix, void const* v, void const* v1, void* v0,
+                             Tile const* tiles, int num_tiles, double const* bprev, double* alpha, cudaStream_t s) {
+    if (cplx)
+        lanczos_a_kernel<double2><<<num_tiles, BLOCK, 0, s>>>(ip, ix, static_cast<double2 const*>(v),
+                                                              static_cast<double2 const*>(v1),
+                                                              static_cast<double2*>(v0), tiles, bprev, alpha);
+    else
+        lanczos_a_kernel<double><<<num_tiles, BLOCK, 0, s>>>(ip, ix, static_cast<double const*>(v),
+                                                             static_cast<double const*>(v1), static_cast<double*>(v0),
+                                                             tiles, bprev, alpha);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lanczos_b(bool cplx, void const* v1, void* v0, Tile const* tiles, int num_tiles,
+                             double const* alpha, double* nrm, cudaStream_t s) {
+    if (cplx)
+        lanczos_b_kernel<double2><<<num_tiles, BLOCK, 0, s>>>(static_cast<double2 const*>(v1),
+                                                              static_cast<double2*>(v0), tiles, alpha, nrm);
+    else
+        lanczos_b_kernel<double><<<num_tiles, BLOCK, 0, s>>>(static_cast<double const*>(v1), static_cast<double*>(v0),
+                                                             tiles, alpha, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lanczos_c(bool cplx, void* v0, Tile const* tiles, int num_tiles, double const* nrm,
+                             cudaStream_t s) {
+    if (cplx) lanczos_c_kernel<double2><<<num_tiles, BLOCK, 0, s>>>(static_cast<double2*>(v0), tiles, nrm);
+    else lanczos_c_kernel<double><<<num_tiles, BLOCK, 0, s>>>(static_cast<double*>(v0), tiles, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral_density(double const* mu, int64_t M, int cols, double const* energy, int ne, double a,
+                                    double b, double* out, cudaStream_t s) {
+    if (ne == 0 || cols == 0) return cudaSuccess;
+    spectral_density_kernel<<<dim3(ne, cols), BLOCK, 0, s>>>(mu, M, energy, ne, a, b, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_greens(double const* mu, int64_t M, int cols, double const* energy, int ne, double a, double b,
+                          double* out, cudaStream_t s) {
+    if (ne == 0 || cols == 0) return cudaSuccess;
+    greens_kernel<<<dim3(ne, cols), BLOCK, 0, s>>>(mu, M, energy, ne, a, b, out);
+    return cudaGetLastError();
+}
+
+}  // namespace kpm

@@ -1,0 +1,408 @@
+"""Tight-binding inputs for the KPM engine: lattices, flakes and modifiers.
+
+pybinding itself cannot be imported next to this package (its compiled core is
+not built), so this module restates the part of its model builder that the
+KPM path consumes: a Hamiltonian CSR matrix in pybinding's site order plus the
+site positions and sublattice ranges used by ``find_nearest`` and the
+conductivity's position operator.
+
+Site order follows the reference exactly, because the stochastic DOS assigns
+random-vector entries by site index:
+
+* foundation bounds: lattice coordinates of the shape vertices, truncated and
+  padded by one cell (``cppcore/src/system/Foundation.cpp:6-23``);
+* positions generated sublattice-major, then c, b, a with ``a`` fastest, in
+  float32 (``Foundation.cpp:25-48``);
+* polygon membership by ray casting in float32
+  (``cppcore/src/system/Shape.cpp:54-88``);
+* dangling sites removed until every site keeps ``min_neighbors`` neighbours
+  (``Foundation.cpp:50-101``), which is the k-core of the site graph;
+* final indices: valid sites, sublattice-major (``Foundation.cpp:127-164``);
+* CSR rows hold sorted column indices; hoppings are inserted for the owning
+  sublattice and mirrored as their conjugate (``hamiltonian/Hamiltonian.hpp:74-100``);
+  zero onsite energies are not stored (``HamiltonianModifiers.hpp:143-152``).
+
+The scalar type follows ``cppcore/src/Model.cpp:178-204``: float32 unless a
+modifier asks for complex numbers (complex64) or double precision.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+
+# graphene constants, pybinding/repository/graphene/constants.py:3-8
+GRAPHENE_A = 0.24595
+GRAPHENE_A_CC = 0.142
+GRAPHENE_T = -2.8
+GRAPHENE_BETA = 3.37
+# pybinding/constants.py:11-12
+HBAR = 6.58211899 * 10 ** -16
+PHI0 = 2 * math.pi * HBAR
+
+
+@dataclass
+class System:
+    """Site positions and sublattice layout of a built system (single orbital)."""
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    sub_ranges: dict = field(default_factory=dict)  # name -> (start, end)
+
+    @property
+    def positions(self):
+        return self.x, self.y, self.z
+
+    @property
+    def num_sites(self):
+        return int(self.x.size)
+
+    @property
+    def hamiltonian_size(self):
+        return self.num_sites
+
+    def sublattice_range(self, sublattice=""):
+        """cppcore/src/system/System.cpp:50-66"""
+        if not sublattice:
+            return 0, self.num_sites
+        if sublattice not in self.sub_ranges:
+            raise RuntimeError("There is no sublattice named '{}'".format(sublattice))
+        return self.sub_ranges[sublattice]
+
+    def find_nearest(self, position, sublattice=""):
+        """Index of the site closest to ``position`` (float32 distances, first minimum wins).
+
+        Mirrors ``System::find_nearest`` (``cppcore/src/system/System.cpp:68-82``).
+        """
+        p = np.zeros(3, np.float32)
+        pos = np.asarray(position, dtype=np.float32).ravel()
+        p[:pos.size] = pos
+        start, end = self.sublattice_range(sublattice)
+        dx = self.x[start:end] - p[0]
+        dy = self.y[start:end] - p[1]
+        dz = self.z[start:end] - p[2]
+        d = np.sqrt(dx * dx + dy * dy + dz * dz)
+        return int(start + np.argmin(d))
+
+    def to_hamiltonian_indices(self, system_index):
+        """Single-orbital systems map site ``i`` to Hamiltonian row ``i`` (System.cpp:33-48)."""
+        return np.array([int(system_index)], dtype=np.int32)
+
+    def contains_mask(self, contains):
+        return np.asarray(contains(self.x, self.y, self.z), dtype=bool)
+
+
+@dataclass
+class Model:
+    """The part of ``pybinding.Model`` that the KPM path reads."""
+    hamiltonian: sp.csr_matrix
+    system: System
+    is_complex: bool = False
+    is_double: bool = False
+    name: str = ""
+
+    @property
+    def is_multiorbital(self):
+        return False
+
+
+# --------------------------------------------------------------------------- shapes
+
+def rectangle(x, y=None):
+    """Vertices of ``pb.rectangle`` (pybinding/shape.py:263-279), float32."""
+    y = y or x
+    x0, y0 = x / 2, y / 2
+    return np.array([[x0, y0], [x0, -y0], [-x0, -y0], [-x0, y0]], dtype=np.float32)
+
+
+def polygon_contains(vertices, px, py):
+    """Ray-casting point-in-polygon test in float32 (``Shape.cpp:54-88``)."""
+    vx = np.asarray(vertices[:, 0], np.float32)
+    vy = np.asarray(vertices[:, 1], np.float32)
+    px = np.asarray(px, np.float32)
+    py = np.asarray(py, np.float32)
+    inside = np.zeros(px.shape, dtype=bool)
+    n = vx.size
+    eps = np.finfo(np.float32).eps
+    tiny = np.finfo(np.float32).tiny
+    j = n - 1
+    for i in range(n):
+        x1, x2, y1, y2 = vx[i], vx[j], vy[i], vy[j]
+        diff = abs(np.float32(y1 - y2))
+        scale = abs(np.float32(y1 + y2))
+        if diff <= eps * scale or diff <= tiny:   # num::approx_equal
+            j = i
+            continue
+        k = np.float32((x2 - x1) / (y2 - y1))
+        intersects_y = (y1 > py) != (y2 > py)
+        x_side = k * (py - y1) + x1
+        intersects_x = px > x_side
+        inside ^= intersects_y & intersects_x
+        j = i
+    return inside
+
+
+# --------------------------------------------------------------------------- builder
+
+def _k_core(valid, nbr, min_neighbors):
+    """Remove valid sites until each keeps ``min_neighbors`` valid neighbours.
+
+    ``nbr`` is (num_sites, max_hops) with -1 for hoppings that leave the foundation.
+    Equivalent to the recursive clearing of ``Foundation.cpp:73-101``: both compute
+    the unique k-core of the valid-site graph.
+    """
+    valid = valid.copy()
+    has = nbr >= 0
+    safe = np.where(has, nbr, 0)
+    while True:
+        cnt = np.sum(has & valid[safe], axis=1)
+        drop = valid & (cnt < min_neighbors)
+        if not drop.any():
+            return valid
+        valid &= ~drop
+
+
+def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
+                    is_complex=False, is_double=False, min_neighbors=2,
+                    t=GRAPHENE_T, a=GRAPHENE_A, a_cc=GRAPHENE_A_CC, name="graphene",
+                    float_constants=False):
+    """Monolayer graphene (``repository/graphene/lattice.py:6-66``) cut by a polygon.
+
+    ``float_constants`` derives the lattice vectors in float32 arithmetic, as the
+    C++ test fixture does (``cppcore/tests/fixtures.cpp``, ``min_neighbors=1``);
+    the Python repository lattice computes them in double and sets
+    ``min_neighbors=2``.
+
+    Modifiers are callables in the reference's numpy style:
+    ``onsite(energy, x, y, z, sub)`` and ``hopping(energy, x1, y1, z1, x2, y2, z2)``
+    returning the new energy array.
+    """
+    f32 = np.float32
+    if float_constants:
+        af, accf = f32(a), f32(a_cc)
+        v0 = np.array([af, 0, 0], f32)
+        v1 = np.array([af / f32(2), af / f32(2) * np.sqrt(f32(3)), 0], f32)
+        sub_pos = [np.array([0, -accf / f32(2), 0], f32), np.array([0, accf / f32(2), 0], f32)]
+    else:
+        v0 = np.array([a, 0, 0], f32)
+        v1 = np.array([a / 2, a / 2 * math.sqrt(3), 0], f32)
+        sub_pos = [np.array([0, -a_cc / 2, 0], f32), np.array([0, a_cc / 2, 0], f32)]
+    # hoppings owned by A (non-conjugate) -> B; B holds the conjugates
+    rel_ab = [(0, 0), (1, -1), (0, -1)]
+    rel = [rel_ab, [(-da, -db) for da, db in rel_ab]]
+
+    # Foundation bounds: solve [v0 v1] v = p for each vertex, truncate, pad by one
+    m = np.array([[v0[0], v1[0]], [v0[1], v1[1]]], dtype=np.float64)
+    coords = np.linalg.solve(m, np.asarray(vertices, np.float64).T).T
+    ic = np.trunc(coords).astype(np.int64)
+    lo = ic.min(axis=0) - 1
+    hi = ic.max(axis=0) + 1
+    s0, s1 = int(hi[0] - lo[0] + 1), int(hi[1] - lo[1] + 1)
+
+    # origin = offset + lo0*v0 + lo1*v1 (float32, Lattice.cpp:190-200)
+    origin = np.zeros(3, f32)
+    origin = origin + f32(lo[0]) * v0
+    origin = origin + f32(lo[1]) * v1
+    bb = np.arange(s1)
+    aa = np.arange(s0)
+    xs, ys, zs = [], [], []
+    for n in range(2):
+        ps = origin + sub_pos[n]
+        pb = np.empty((s1, 3), f32)
+        pb[0] = ps
+        pb[1:] = ps[None, :] + bb[1:, None].astype(f32) * v1[None, :]
+        pa = pb[:, None, :] + aa[None, :, None].astype(f32) * v0[None, None, :]
+        xs.append(pa[..., 0].ravel())
+        ys.append(pa[..., 1].ravel())
+        zs.append(pa[..., 2].ravel())
+    x = np.concatenate(xs)
+    y = np.concatenate(ys)
+    z = np.concatenate(zs)
+    block = s0 * s1
+    total = 2 * block
+
+    valid = polygon_contains(np.asarray(vertices, np.float32), x, y)
+
+    # neighbour table in foundation (flat) indices
+    nbr = np.full((total, 3), -1, np.int64)
+    a_idx = np.tile(aa, s1)
+    b_idx = np.repeat(bb, s0)
+    for n in range(2):
+        other = 1 - n
+        for h, (da, db) in enumerate(rel[n]):
+            na, nb = a_idx + da, b_idx + db
+            ok = (na >= 0) & (na < s0) & (nb >= 0) & (nb < s1)
+            tgt = other * block + nb * s0 + na
+            nbr[n * block:(n + 1) * block, h] = np.where(ok, tgt, -1)
+
+    valid = _k_core(valid, nbr, min_neighbors)
+
+    final = np.full(total, -1, np.int64)
+    nvalid = int(valid.sum())
+    final[valid] = np.arange(nvalid)
+    na_valid = int(valid[:block].sum())
+    sub_ranges = {"A": (0, na_valid), "B": (na_valid, nvalid)}
+    sx, sy, sz = x[valid], y[valid], z[valid]
+
+    # hoppings owned by A sites (row = A site, col = B site)
+    a_sites = np.nonzero(valid[:block])[0]
+    rows, cols = [], []
+    for h in range(3):
+        tgt = nbr[a_sites, h]
+        ok = tgt >= 0
+        ok[ok] &= valid[tgt[ok]]
+        rows.append(final[a_sites[ok]])
+        cols.append(final[tgt[ok]])
+    rows = np.concatenate(rows)
+    cols = np.concatenate(cols)
+    sub_of = np.zeros(nvalid, np.int8)
+    sub_of[na_valid:] = 1
+
+    if is_complex:
+        dtype = np.complex128 if is_double else np.complex64
+    else:
+        dtype = np.float64 if is_double else np.float32
+    hop = np.full(rows.size, t, dtype=dtype)
+    for mod in hopping_modifiers:
+        hop = np.asarray(mod(hop, sx[rows], sy[rows], sz[rows], sx[cols], sy[cols], sz[cols]))
+        hop = hop.astype(dtype) if np.iscomplexobj(dtype(0)) else np.real(hop).astype(dtype)
+
+    onsite = np.zeros(nvalid, dtype=dtype)
+    for mod in onsite_modifiers:
+        onsite = np.asarray(mod(onsite, sx, sy, sz, sub_of)).astype(dtype)
+
+    r_all = [rows, cols]
+    c_all = [cols, rows]
+    v_all = [hop, np.conj(hop)]
+    nz = onsite != 0
+    if nz.any():
+        d = np.nonzero(nz)[0]
+        r_all.append(d)
+        c_all.append(d)
+        v_all.append(onsite[d])
+    h = _csr_sorted(np.concatenate(r_all), np.concatenate(c_all), np.concatenate(v_all), nvalid, dtype)
+    system = System(sx, sy, sz, sub_ranges)
+    return Model(h, system, is_complex=is_complex, is_double=is_double, name=name)
+
+
+def _csr_sorted(rows, cols, vals, n, dtype):
+    order = np.lexsort((cols, rows))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    indptr = np.zeros(n + 1, np.int32)
+    np.add.at(indptr, rows + 1, 1)
+    indptr = np.cumsum(indptr).astype(np.int32)
+    m = sp.csr_matrix((vals.astype(dtype), cols.astype(np.int32), indptr), shape=(n, n))
+    m.has_sorted_indices = True
+    return m
+
+
+# --------------------------------------------------------------------------- modifiers
+
+def constant_potential(magnitude):
+    """``pb.constant_potential`` (pybinding/modifier.py:391-402)."""
+    def f(energy, x, y, z, sub):
+        return energy + energy.dtype.type(magnitude)
+    return f
+
+
+def mass_term(delta):
+    """``graphene.mass_term`` (repository/graphene/modifiers.py:9-24)."""
+    def f(energy, x, y, z, sub):
+        e = energy.copy()
+        e[sub == 0] += delta
+        e[sub == 1] -= delta
+        return e
+    return f
+
+
+def constant_magnetic_field(magnitude):
+    """Peierls phase of a perpendicular field (repository/graphene/modifiers.py:62-81).
+
+    Computed in the precision of the numpy inputs as the reference's modifier is
+    (float32 positions, complex64 energies).
+    """
+    scale = 1e-18
+    const = scale * 2 * math.pi / PHI0
+
+    def f(energy, x1, y1, z1, x2, y2, z2):
+        vp_x = 0.5 * magnitude * (y1 + y2)
+        peierls = vp_x * (x1 - x2)
+        return energy * np.exp(1j * const * peierls)
+    return f
+
+
+def strained_hopping(displacement):
+    """Hopping ``t * exp(-beta (d/a_cc - 1))`` for displaced sites
+    (repository/graphene/modifiers.py:84-90); ``displacement(x, y) -> (ux, uy)``."""
+    def f(energy, x1, y1, z1, x2, y2, z2):
+        ux1, uy1 = displacement(x1, y1)
+        ux2, uy2 = displacement(x2, y2)
+        dx = (x1 + ux1) - (x2 + ux2)
+        dy = (y1 + uy1) - (y2 + uy2)
+        dz = z1 - z2
+        d = np.sqrt(dx * dx + dy * dy + dz * dz)
+        return energy * np.exp(-GRAPHENE_BETA * (d / GRAPHENE_A_CC - 1))
+    return f
+
+
+def sinusoidal_strain(amplitude, period):
+    """Smooth in-plane displacement ``u = amplitude * period/(2 pi) * sin(2 pi x/period)``
+    along x: a strain field of peak magnitude ``amplitude``."""
+    def disp(x, y):
+        k = 2 * np.pi / period
+        ux = (amplitude / k) * np.sin(k * x)
+        return ux.astype(x.dtype), np.zeros_like(y)
+    return disp
+
+
+def anderson_disorder(width, seed):
+    """Onsite energies uniform in [-width/2, width/2] from a seeded numpy generator."""
+    def f(energy, x, y, z, sub):
+        rng = np.random.default_rng(seed)
+        return energy + rng.uniform(-width / 2, width / 2, size=energy.shape).astype(energy.dtype)
+    return f
+
+
+# --------------------------------------------------------------------------- synthetic configs
+
+GRAPHENE_SITE_DENSITY = 4 / (math.sqrt(3) * GRAPHENE_A ** 2)  # sites per nm^2
+
+
+def graphene_flake(num_sites, aspect=1.0, **kw):
+    """A rectangular graphene flake with about ``num_sites`` sites."""
+    area = num_sites / GRAPHENE_SITE_DENSITY
+    w = math.sqrt(area * aspect)
+    h = area / w
+    return build_honeycomb(rectangle(w, h), **kw)
+
+
+def simple_cubic_periodic(L, t=-1.0, onsite=None, dtype=np.float32):
+    """Simple cubic L^3 lattice with periodic boundaries, 6 hoppings per site.
+
+    Site index = (z*L + y)*L + x. ``onsite`` is an optional array of L^3 energies.
+    The periodic wrap makes the Hamiltonian real at k = 0.
+    """
+    n = L ** 3
+    idx = np.arange(n, dtype=np.int64)
+    xi = idx % L
+    yi = (idx // L) % L
+    zi = idx // (L * L)
+    rows, cols = [], []
+    for dx, dy, dz in [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]:
+        j = (((zi + dz) % L) * L + (yi + dy) % L) * L + (xi + dx) % L
+        rows.append(idx)
+        cols.append(j)
+    rows = np.concatenate(rows)
+    cols = np.concatenate(cols)
+    vals = np.full(rows.size, t, dtype)
+    if onsite is not None:
+        nz = np.nonzero(onsite)[0]
+        rows = np.concatenate([rows, nz])
+        cols = np.concatenate([cols, nz])
+        vals = np.concatenate([vals, np.asarray(onsite, dtype)[nz]])
+    h = _csr_sorted(rows, cols, vals, n, dtype)
+    f32 = np.float32
+    system = System(xi.astype(f32), yi.astype(f32), zi.astype(f32), {"A": (0, n)})
+    return Model(h, system, name="cubic")

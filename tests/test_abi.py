@@ -1,0 +1,140 @@
+"""The C ABI library builds, loads and exports every entry point of include/kpm_gb300.h.
+
+These run without a GPU: only host-side entry points are called (argument
+checks, kernel damping coefficients), never the recursion.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from pybinding_gb300 import _native
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "kpm_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^[A-Za-z_][\w\s\*]*?\b(kpm_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    assert "kpm_create" in names and "kpm_moments_diag" in names and "kpm_calc_dos" in names
+    assert len(names) >= 18
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(declared_functions()) <= set(_native.SIGNATURES), "binding table lacks a declared function"
+
+
+def test_damping_matches_oracle(oracle):
+    for kern, lam in (("jackson", 4.0), ("lorentz", 4.0), ("lorentz", 3.0), ("dirichlet", 4.0)):
+        for n in (2, 10, 2050):
+            np.testing.assert_array_equal(_native.damping_coefficients(kern, lam, n), oracle.damping(kern, lam, n))
+    for sb in (0.0174, 0.05, 0.0031, 1e-4):
+        for kern in ("jackson", "lorentz", "dirichlet"):
+            assert _native.required_num_moments(kern, 4.0, sb) == oracle.required_num_moments(kern, 4.0, sb)
+
+
+def test_round_num_moments(oracle):
+    for n in range(0, 40):
+        assert _native.round_num_moments(n) == oracle.round_num_moments(n)
+
+
+def _small_h(dtype=np.float32):
+    h = sp.diags([np.ones(9), np.ones(9)], [-1, 1], shape=(10, 10), format="csr").astype(dtype)
+    h.sort_indices()
+    return h
+
+
+def _create(h, cfg=None, offsets=None):
+    cfg = cfg or _native.make_config()
+    ip = np.ascontiguousarray(h.indptr, np.int32)
+    ix = np.ascontiguousarray(h.indices, np.int32)
+    v = np.ascontiguousarray(h.data)
+    off = None if offsets is None else np.ascontiguousarray(offsets, np.int64)
+    handle = C.c_void_p()
+    rc = _native.lib().kpm_create(_native.SCALAR_CODE[v.dtype], h.shape[0], _native.ptr(ip), _native.ptr(ix),
+                                  _native.ptr(v), 1 if off is None else off.size - 1, _native.ptr(off),
+                                  C.byref(cfg), C.byref(handle))
+    msg = _native.lib().kpm_last_error().decode()
+    if rc == 0:
+        _native.lib().kpm_destroy(handle)
+    return rc, msg
+
+
+def test_create_rejects_bad_energy_range():
+    """kpm/Core.cpp:20-22"""
+    rc, msg = _create(_small_h(), _native.make_config(energy_range=(1.0, -1.0)))
+    assert rc == _native.KPM_ERR_VALUE and msg == "KPM: Invalid energy range specified (min > max)."
+
+
+def test_create_rejects_nan():
+    """hamiltonian/Hamiltonian.hpp:133-140"""
+    h = _small_h(np.float64)
+    h.data[3] = np.nan
+    rc, msg = _create(h)
+    assert rc == _native.KPM_ERR_RUNTIME and "NaN or INF" in msg
+
+
+def test_create_rejects_bad_csr():
+    h = _small_h()
+    h.indices[0] = 42
+    rc, msg = _create(h)
+    assert rc == _native.KPM_ERR_VALUE and "out of range" in msg
+    h = _small_h()
+    rc, msg = _create(h, offsets=[0, 5, 10])  # hoppings 4<->5 cross the block boundary
+    assert rc == _native.KPM_ERR_VALUE and "system block" in msg
+    rc, msg = _create(h, offsets=[0, 10, 10])
+    assert rc == _native.KPM_ERR_VALUE
+
+
+def test_lorentz_lambda_checked():
+    rc, msg = _create(_small_h(), _native.make_config(kernel="lorentz", kernel_param=-1.0))
+    assert rc == _native.KPM_ERR_VALUE and "lambda must be positive" in msg
+
+
+def test_compute_without_gpu_fails_cleanly():
+    """Creating an engine is host-only; the first device call reports a CUDA error."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    eng = _native.Engine(_small_h(), _native.make_config())
+    with pytest.raises(RuntimeError, match="CUDA"):
+        eng.calc_dos(np.linspace(-1, 1, 5), 0.1, 1)
+    eng.close()
+
+
+def test_optimized_hamiltonian_bit_exact(oracle):
+    """The engine's reorder (host C++) equals create_reordered bit for bit
+    (kpm/OptimizedHamiltonian.cpp:75-152), f32 and c64, b == 0 and b != 0."""
+    from tests import models as TM
+    cases = [(TM.cpp_fixture_model(), (-6.25, 8.25)), (TM.cpp_fixture_model_plain(), (-12.0, 10.0)),
+             (TM.graphene("magnetic_field", 3), (-8.5, 8.5)), (TM.graphene("const_potential", 3), (-8.0, 9.0))]
+    for m, rng in cases:
+        h = m.hamiltonian
+        eng = _native.Engine(h, _native.make_config(energy_range=rng))
+        a, b = oracle.scale(*rng)
+        assert eng.scaling_factors() == (a, b)
+        n = h.shape[0]
+        for src, dest in (([0], [0]), ([n // 2], [n // 3, n // 4]), ([n - 1, 1], [2, n - 2])):
+            for reorder in (True, False):
+                got = eng.optimized_hamiltonian(src, dest, reorder)
+                ref = oracle.optimize(h, src, dest, a, b, reorder)
+                assert np.array_equal(got["h2"].indptr, ref["h2"].indptr)
+                assert np.array_equal(got["h2"].indices, ref["h2"].indices)
+                gv, rv = got["h2"].data, ref["h2"].data
+                assert gv.dtype == rv.dtype and np.array_equal(gv.view(np.uint8), rv.view(np.uint8))
+                assert np.array_equal(got["reorder_map"], ref["reorder_map"])
+                assert np.array_equal(got["slices"], ref["slices"])
+                assert np.array_equal(got["src"], ref["src"]) and np.array_equal(got["dest"], ref["dest"])
+                assert (got["src_offset"], got["dest_offset"]) == (ref["src_offset"], ref["dest_offset"])
+        eng.close()

@@ -1,0 +1,228 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the oracle, the
+reference's FP64 NumPy KPM, and the reference's golden arrays.
+
+Error measure for moments: max_n |mu_n - mu_n^ref| / max_n |mu_n^ref|.
+Tolerances: FP64 recursion <= 1e-10 (the spec bar); FP32 recursion
+vectors with FP64 moment sums <= 1e-5 at these sizes (the measured error is
+printed); reconstructed functions against the reference goldens at the
+reference's own test tolerances.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from pybinding_gb300 import _native, kpm, kpm_batch, lattice as L, lorentz_kernel
+from tests import models as TM
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(got, ref):
+    return float(np.max(np.abs(np.asarray(got) - np.asarray(ref))) / np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("tag", ["c128", "f64"])
+def test_fp64_moments_match_reference_python_impl(python_impl, tag):
+    """FP64 recursion == reference _PythonImpl (chebyshev.py:498-520) on identical starters, <= 1e-10."""
+    d = python_impl
+    n = d[tag + "_indptr"].size - 1
+    h = sp.csr_matrix((d[tag + "_data"], d[tag + "_indices"], d[tag + "_indptr"]), shape=(n, n))
+    ref = d[tag + "_moments"]
+    eng = _native.Engine(h, _native.make_config(energy_range=tuple(d[tag + "_bounds"])))
+    assert eng.scaling_factors() == tuple(d[tag + "_ab"])
+    got = eng.moments_diag(ref.shape[1], d[tag + "_starters"][None])[0]
+    assert got.shape == ref.shape
+    err = rel_err(got, ref)
+    print("fp64 moment error vs _PythonImpl [%s]: %.3e" % (tag, err))
+    assert err <= 1e-10
+    # the same vectors one at a time (K = 1 kernel shape) agree too
+    one = eng.moments_diag(ref.shape[1], d[tag + "_starters"][1:2][None])[0, 0]
+    assert rel_err(one, ref[1]) <= 1e-10
+
+
+def _disordered_flake(n_sites, seed, dtype=np.float32):
+    m = L.graphene_flake(n_sites, onsite_modifiers=[L.anderson_disorder(1.0, seed)])
+    return m.hamiltonian.astype(dtype)
+
+
+@pytest.mark.parametrize("nvec", [64, 13, 3])
+def test_fp32_batched_moments_vs_fp64_oracle(oracle, nvec):
+    """FP32 vectors + FP64 moment sums against the FP64 oracle on the same H and starters."""
+    h = _disordered_flake(6000, 3)
+    rng = (-9.0, 9.0)
+    M = 514
+    a, b = oracle.scale(*rng)
+    starters = oracle.random_starters(h.shape[0], nvec, np.float32)
+    eng = _native.Engine(h, _native.make_config(energy_range=rng))
+    got = eng.moments_diag(M, starters[None])[0]
+    r = oracle.optimize(h.astype(np.float64), [0], [0], a, b)
+    st = oracle.reorder_vector(starters.astype(np.float64), r["reorder_map"])
+    ref = oracle.moments_diag(r["h2"], st, M, slices=r["slices"])
+    err = rel_err(got, ref)
+    print("fp32-recursion moment error vs fp64 oracle (nvec=%d, M=%d): %.3e" % (nvec, M, err))
+    assert err <= 1e-5
+    # FP64 mode of the same engine meets the FP64 bar
+    eng64 = _native.Engine(h, _native.make_config(energy_range=rng, precision="fp64"))
+    got64 = eng64.moments_diag(M, starters[None])[0]
+    assert rel_err(got64, ref) <= 1e-10
+
+
+def test_complex_fp32_moments_vs_fp64_oracle(oracle):
+    m = L.graphene_flake(4000, hopping_modifiers=[L.constant_magnetic_field(100)], is_complex=True)
+    h = m.hamiltonian
+    rng = (-8.7, 8.7)
+    a, b = oracle.scale(*rng)
+    M = 258
+    starters = oracle.random_starters(h.shape[0], 8, np.complex64)
+    got = _native.Engine(h, _native.make_config(energy_range=rng)).moments_diag(M, starters[None])[0]
+    r = oracle.optimize(h.astype(np.complex128), [0], [0], a, b)
+    ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters.astype(np.complex128), r["reorder_map"]), M,
+                              slices=r["slices"])
+    err = rel_err(got, ref)
+    print("c64-recursion moment error vs c128 oracle: %.3e" % err)
+    assert err <= 1e-5
+
+
+@pytest.mark.parametrize("name", list(TM.DOS_MODELS))
+def test_dos_matches_reference_golden(baselines, name):
+    """tests/test_kpm.py:146-165 through the pb.kpm-compatible API (rtol 1e-3)."""
+    kind, size = TM.DOS_MODELS[name]
+    model = TM.graphene(kind, size)
+    energy = np.linspace(0, 2, 25)
+    for cfg in [dict(optimal_size=False, interleaved=False), dict(optimal_size=True, interleaved=True)]:
+        k = kpm(model, kernel=lorentz_kernel(), silent=True, matrix_format="ELL", **cfg)
+        dos = k.calc_dos(energy, broadening=0.15)
+        np.testing.assert_allclose(dos.data, baselines["dos[%s]" % name], rtol=1e-3, atol=1e-6)
+
+
+@pytest.mark.parametrize("name", list(TM.LDOS_MODELS))
+def test_ldos_matches_reference_golden(baselines, name):
+    """tests/test_kpm.py:25-47 (rtol 1e-3, atol 1e-6)"""
+    kind, size = TM.LDOS_MODELS[name]
+    model = TM.graphene(kind, size)
+    energy = np.linspace(0, 2, 25)
+    for cfg in [dict(matrix_format="CSR", optimal_size=False, interleaved=False),
+                dict(matrix_format="CSR", optimal_size=True, interleaved=False),
+                dict(matrix_format="ELL", optimal_size=True, interleaved=True)]:
+        k = kpm(model, kernel=lorentz_kernel(), silent=True, **cfg)
+        ldos = k.calc_ldos(energy, broadening=0.15, position=[0, 0.07], reduce=False)
+        np.testing.assert_allclose(ldos.data, baselines["ldos[%s]" % name], rtol=1e-3, atol=1e-6)
+
+
+def test_ldos_equals_oracle_and_multi_index(oracle):
+    """Several LDOS columns in one batch; each equals the oracle's Core::ldos."""
+    m = TM.graphene("const_potential", 6)
+    h = m.hamiltonian.astype(np.float64)
+    n = h.shape[0]
+    idx = [n // 2, n // 4, n // 2, 7, n - 3]
+    energy = np.linspace(-3, 3, 31)
+    k = kpm(L.Model(h, m.system), energy_range=(-9, 9), kernel=lorentz_kernel())
+    got = k.impl.engine.calc_ldos(idx, energy, 0.2)
+    ref = oracle.core_ldos(h, idx, energy, 0.2, energy_range=(-9, 9), kernel="lorentz")
+    # the reference's 2/pi prefactor is a float constant (reconstruct.hpp:27); the engine uses exact pi
+    assert rel_err(got, ref) < 1e-7
+    np.testing.assert_allclose(got[:, 0], got[:, 2], rtol=1e-12)
+
+
+def test_greens_function(oracle):
+    """cppcore/tests/test_kpm.cpp:217-260: LDOS = -Im G_ii / pi; G(i,[j..])[0] = G(j,i) for real H;
+    equal to the oracle's Core::greens_vector."""
+    m = TM.cpp_fixture_model()
+    h = m.hamiltonian.astype(np.float64)
+    n = h.shape[0]
+    i, j = n // 2, n // 4
+    energy = np.linspace(-0.3, 0.3, 10)
+    k = kpm(L.Model(h, m.system))
+    gs = k.calc_greens(i, [j, j + 1, j + 2], energy, 0.8)
+    assert len(gs) == 3
+    g = k.calc_greens(j, i, energy, 0.8)
+    np.testing.assert_allclose(gs[0], g, rtol=1e-6, atol=1e-9)
+    g_ii = k.calc_greens(i, i, energy, 0.8)
+    ldos = k.impl.engine.calc_ldos([i], energy, 0.8)[:, 0]
+    np.testing.assert_allclose(ldos, -g_ii.imag / np.pi, rtol=1e-9, atol=1e-12)
+    emin, emax = k.impl.energy_bounds
+    cfg = dict(energy_range=(np.float32(emin), np.float32(emax)))
+    eng = _native.Engine(h, _native.make_config(**cfg))
+    got = eng.calc_greens(i, [j, j + 1, j + 2], energy, 0.8)
+    ref = oracle.core_greens(h, i, [j, j + 1, j + 2], energy, 0.8, **cfg)
+    assert rel_err(got, ref) < 1e-9
+
+
+def test_moments_api(oracle):
+    """tests/test_kpm.py:50-84 (moments == manual LDOS) and KPM.cpp:19-53 errors."""
+    m = TM.graphene("pristine", 5)
+    h = m.hamiltonian.astype(np.float64)
+    n = h.shape[0]
+    cfg = dict(energy_range=(-9.0, 9.0))
+    k = kpm(L.Model(h, m.system), **cfg)
+    alpha = np.zeros(n)
+    alpha[n // 3] = 1
+    mom = k.moments(100, alpha)
+    ref = oracle.core_moments(h, 100, alpha, **cfg)
+    assert rel_err(mom, ref) < 1e-10
+    rng = np.random.default_rng(1)
+    beta = rng.standard_normal(n)
+    op = sp.random(n, n, density=0.01, random_state=2, format="csr")
+    got = k.moments(64, alpha, beta, op)
+    ref = oracle.core_moments(h, 64, alpha, beta, op, **cfg)
+    assert rel_err(got, ref) < 1e-10
+    got = k.moments(64, alpha, None, op)
+    ref = oracle.core_moments(h, 64, alpha, None, op, **cfg)
+    assert rel_err(got, ref) < 1e-10
+    with pytest.raises(RuntimeError, match="Size mismatch"):
+        k.moments(10, [1, 2, 3])
+    with pytest.raises(RuntimeError, match="Hamiltonian is real, but the given argument 'alpha' is complex"):
+        k.moments(10, 1j * alpha)
+
+
+def test_ragged_batch_equals_single_systems(oracle):
+    """A ragged batch of uneven flakes gives each flake's own moments and DOS."""
+    hs = [_disordered_flake(n, s, np.float64) for n, s in ((1500, 1), (3700, 2), (800, 3))]
+    models = [L.Model(h, None) for h in hs]
+    rng = (-9.0, 9.0)
+    nvec, M = 8, 130
+    starters = [oracle.random_starters(h.shape[0], nvec, np.float64) for h in hs]
+    batch = kpm_batch(models, energy_range=rng)
+    flat = np.concatenate([s.ravel() for s in starters])
+    a, b = oracle.scale(*rng)
+    moms = batch.engine.moments_diag(M, flat)
+    for s, h in enumerate(hs):
+        r = oracle.optimize(h, [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s], r["reorder_map"]), M,
+                                  slices=r["slices"])
+        assert rel_err(moms[s], ref) <= 1e-10
+    energy = np.linspace(-2, 2, 11)
+    dos = batch.calc_dos(energy, 0.2, num_random=2)
+    for s, h in enumerate(hs):
+        ref, _ = oracle.core_dos(h, energy, 0.2, 2, energy_range=rng)
+        np.testing.assert_allclose(dos[s].data, ref, rtol=1e-6, atol=1e-10)
+
+
+def test_lanczos_bounds_and_multi_system():
+    """FP64 GPU Lanczos: extremes within the convergence target, per system of a batch."""
+    hs = [_disordered_flake(n, s, np.float64) for n, s in ((300, 4), (700, 5))]
+    batch = kpm_batch([L.Model(h, None) for h in hs])
+    for s, h in enumerate(hs):
+        mn, mx, loops = batch.engine.energy_bounds(s)
+        ev = np.linalg.eigvalsh(h.toarray())
+        assert mn == pytest.approx(ev[0], rel=2e-3) and mx == pytest.approx(ev[-1], rel=2e-3)
+        assert 0 < loops < 1000
+
+
+def test_minimum_moments_and_single_row():
+    h = sp.csr_matrix(np.array([[0.5]]))
+    eng = _native.Engine(h, _native.make_config(energy_range=(-1.0, 1.0)))
+    mu = eng.moments_diag(2, np.ones((1, 1, 1)))[0, 0]
+    assert mu.shape == (2,)
+    a, b = eng.scaling_factors()
+    assert mu[0] == pytest.approx(0.5) and mu[1].real == pytest.approx((0.5 - b) / a)
+
+
+def test_report_and_stats():
+    m = TM.graphene("const_potential", 8)
+    k = kpm(m, kernel=lorentz_kernel())
+    k.calc_dos(np.linspace(-1, 1, 5), 0.2, 2)
+    s = k.stats
+    assert s.num_moments > 0 and s.moments_time > 0 and s.eps > 0
+    r = k.report(shortform=True)
+    assert "eps" in r and r.count("[") >= 3
