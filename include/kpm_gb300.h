@@ -127,8 +127,10 @@ int kpm_scaling_factors(kpm_engine* engine, int32_t system, double* a, double* b
  * collectors of kpm/default/collectors.cpp:6-36), run on the GPU for every
  * system at once.
  *   starters: for each system s, num_vectors vectors of length rows_s in the
- *             ORIGINAL site order, stored [s][vector][site] (the engine's
- *             scalar type, complex interleaved); the engine reorders them.
+ *             ORIGINAL site order, stored [s][vector][site] in the
+ *             Hamiltonian's scalar type (the one given to kpm_create; complex
+ *             interleaved): exactly num_vectors * rows elements. The engine
+ *             reorders them and converts them to the recursion precision.
  *   num_moments: rounded up so that (M - 2) % 4 == 0 (kpm/Kernel.hpp:9-13);
  *             the rounded count is written to *num_moments_out.
  *   out: per system [s][vector][M] moments, undamped, as complex double

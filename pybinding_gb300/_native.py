@@ -187,22 +187,30 @@ class Engine:
         return a.value, b.value
 
     def moments_diag(self, num_moments, starters, average=False, on_device_ptr=None, num_vectors=None):
-        """Diagonal moments for supplied starters ``[system][vector][site]`` (host array or device ptr)."""
+        """Diagonal moments for supplied starters ``[system][vector][site]``.
+
+        ``starters`` is a host array (converted to the Hamiltonian's dtype), or
+        ``on_device_ptr`` is the address of a device buffer that already holds
+        ``num_vectors * rows`` elements of the Hamiltonian's dtype in that layout.
+        """
         nout = C.c_int64()
         rounded = round_num_moments(num_moments)
         if on_device_ptr is not None:
+            if num_vectors is None or int(num_vectors) < 1:
+                raise ValueError("num_vectors is required with a device pointer")
             nvec = int(num_vectors)
-            src = C.c_void_p(on_device_ptr)
-            dev = 1
+            src, dev, keep = C.c_void_p(int(on_device_ptr)), 1, None
         else:
-            s = np.ascontiguousarray(starters)
-            nvec = s.size // self.rows
-            src = ptr(s)
-            dev = 0
+            keep = np.ascontiguousarray(starters, dtype=self.dtype)
+            if keep.size == 0 or keep.size % self.rows:
+                raise ValueError("starters must hold num_vectors * %d elements" % self.rows)
+            nvec = keep.size // self.rows
+            src, dev = ptr(keep), 0
         cols = self.num_systems if average else self.num_systems * nvec
         out = np.empty((cols, rounded), np.complex128)
         check(lib().kpm_moments_diag(self._h, num_moments, nvec, src, dev, int(bool(average)), ptr(out),
                                      C.byref(nout)))
+        del keep
         shape = (self.num_systems, rounded) if average else (self.num_systems, nvec, rounded)
         return out.reshape(shape)
 

@@ -728,15 +728,16 @@ struct kpm_engine {
             KPM_CUDA(cudaMemcpyAsync(d_pos.p, units->data(), sizeof(int32_t) * units->size(), cudaMemcpyHostToDevice, stream));
             KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, sh.K, rows, stream));
         } else {
-            size_t const in_bytes = static_cast<size_t>(nvec) * rows * vb;
+            // starters are in the Hamiltonian's scalar type; the scatter converts them
+            size_t const in_bytes = static_cast<size_t>(nvec) * rows * scalar_bytes(stype);
             void const* src = starters;
             if (!on_device) {
                 d_stage.ensure(in_bytes);
                 KPM_CUDA(cudaMemcpyAsync(d_stage.p, starters, in_bytes, cudaMemcpyHostToDevice, stream));
                 src = d_stage.p;
             }
-            KPM_CUDA(kpm::launch_scatter_starters(vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(), nsys,
-                                                  nvec, sh.K, sh.nbatch, rows, stream));
+            KPM_CUDA(kpm::launch_scatter_starters(stype, vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(),
+                                                  nsys, nvec, sh.K, sh.nbatch, rows, stream));
         }
         KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
         KPM_CUDA(cudaEventRecord(ev0, stream));
@@ -785,6 +786,7 @@ struct kpm_engine {
         last_shape = sh;
     }
     Shape last_shape{};
+    double last_gemm_time = 0;
 
     void reset_stats(int64_t M, bool diagonal, bool opt, double multiplier, int64_t active_rows_nnz_rows) {
         (void)active_rows_nnz_rows;
@@ -959,33 +961,28 @@ int kpm_calc_dos(kpm_engine* e, const double* energy, int64_t ne, double broaden
             Mmax = std::max(Mmax, Ms[s]);
         }
         e->optimize({0}, {0});
-        // the reference's random starters: one default-seeded mt19937 per system (Starter.cpp:48-84)
-        int const vb = kpm::vtype_bytes(e->vtype);
-        std::vector<unsigned char> st(static_cast<size_t>(num_random) * e->rows * vb);
-        with_vtype(e->vtype, [&](auto zc) {
-            using Tc = decltype(zc);
-            auto* o = reinterpret_cast<Tc*>(st.data());
+        // the reference's random starters: one default-seeded mt19937 per system (Starter.cpp:48-84),
+        // in the Hamiltonian's scalar type
+        std::vector<unsigned char> st(static_cast<size_t>(num_random) * e->rows * scalar_bytes(e->stype));
+        with_scalar(e->stype, [&](auto zi) {
+            using Tin = decltype(zi);
+            using R = real_of<Tin>;
+            auto* o = reinterpret_cast<Tin*>(st.data());
             for (int s = 0; s < e->nsys; ++s) {
                 int64_t const n = e->sys_rows(s);
-                Tc* base = o + e->sys_off[s] * num_random;
-                with_scalar(e->stype, [&](auto zi) {
-                    using Tin = decltype(zi);
-                    using R = real_of<Tin>;
-                    std::mt19937 gen;
-                    std::uniform_real_distribution<R> dist;
-                    for (int64_t v = 0; v < num_random; ++v)
-                        for (int64_t i = 0; i < n; ++i) {
-                            Tin val;
-                            if constexpr (is_cplx_v<Tin>) {
-                                std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
-                                std::complex<R> const k(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
-                                val = std::exp(k * dist(gen));
-                            } else {
-                                val = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
-                            }
-                            base[v * n + i] = convert<Tc>(val);
+                Tin* base = o + e->sys_off[s] * num_random;
+                std::mt19937 gen;
+                std::uniform_real_distribution<R> dist;
+                for (int64_t v = 0; v < num_random; ++v)
+                    for (int64_t i = 0; i < n; ++i) {
+                        if constexpr (is_cplx_v<Tin>) {
+                            std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
+                            std::complex<R> const k(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
+                            base[v * n + i] = std::exp(k * dist(gen));
+                        } else {
+                            base[v * n + i] = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
                         }
-                });
+                    }
             }
         });
         e->run_diag(Mmax, num_random, st.data(), false, nullptr, false);
@@ -1167,12 +1164,12 @@ int kpm_moments(kpm_engine* e, int64_t num_moments, const double* alpha, int64_t
         e->optimize({0}, {0});
         int const vt = e->vtype;
         int const vb = kpm::vtype_bytes(vt);
-        // alpha in the engine's vector type, original order
-        std::vector<unsigned char> st(static_cast<size_t>(n) * vb);
-        with_vtype(vt, [&](auto zc) {
-            using Tc = decltype(zc);
-            auto* o = reinterpret_cast<Tc*>(st.data());
-            for (int64_t i = 0; i < n; ++i) o[i] = from_cd<Tc>(cd(alpha[2 * i], alpha[2 * i + 1]));
+        // alpha in the Hamiltonian's scalar type (force_cast, collectors.cpp:38-49), original order
+        std::vector<unsigned char> st(static_cast<size_t>(n) * scalar_bytes(e->stype));
+        with_scalar(e->stype, [&](auto zi) {
+            using Ts = decltype(zi);
+            auto* o = reinterpret_cast<Ts*>(st.data());
+            for (int64_t i = 0; i < n; ++i) o[i] = from_cd<Ts>(cd(alpha[2 * i], alpha[2 * i + 1]));
         });
         std::vector<double> mu(static_cast<size_t>(2 * M));
         if (beta_size == 0 && op_rows == 0) {
@@ -1209,12 +1206,13 @@ int kpm_moments(kpm_engine* e, int64_t num_moments, const double* alpha, int64_t
             });
             e->d_gamma.ensure(gam.size());
             KPM_CUDA(cudaMemcpyAsync(e->d_gamma.p, gam.data(), gam.size(), cudaMemcpyHostToDevice, e->stream));
-            e->d_x0.ensure(st.size());
-            e->d_x1.ensure(st.size());
+            size_t const vbytes = static_cast<size_t>(n) * vb;
+            e->d_x0.ensure(vbytes);
+            e->d_x1.ensure(vbytes);
             e->d_stage.ensure(st.size());
             KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, st.data(), st.size(), cudaMemcpyHostToDevice, e->stream));
-            KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, st.size(), e->stream));
-            KPM_CUDA(kpm::launch_scatter_starters(vt, e->d_stage.p, e->d_x0.p, e->d_map.as<int32_t>(),
+            KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, vbytes, e->stream));
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, e->d_stage.p, e->d_x0.p, e->d_map.as<int32_t>(),
                                                   e->d_sysoff.as<int64_t>(), 1, 1, 1, 1, n, e->stream));
             kpm_engine::Shape sh{1, 1, 1, 1, 4096};
             int const ntiles = e->build_tiles(sh, true);
@@ -1272,9 +1270,195 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
                           double broadening, double temperature, int64_t num_random, int64_t num_points,
                           int32_t gemm_mode, double* out) {
     return guarded([&] {
-        (void)e; (void)left; (void)right; (void)chem; (void)nmu; (void)broadening; (void)temperature;
-        (void)num_random; (void)num_points; (void)gemm_mode; (void)out;
-        fail(KPM_ERR_RUNTIME, "conductivity is not available in this build");
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "conductivity needs a single-system engine");
+        if (!left || !right || (nmu > 0 && (!chem || !out))) fail(KPM_ERR_VALUE, "null argument");
+        if (num_random < 1 || num_points < 2) fail(KPM_ERR_VALUE, "num_random >= 1 and num_points >= 2 required");
+        if (gemm_mode != 0) fail(KPM_ERR_VALUE, "unknown gemm_mode");
+        double const t0 = now_s();
+        auto const sc = e->scale(0);
+        int64_t const M = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / sc.a);
+        e->optimize({0}, {0});
+        int64_t const n = e->rows;
+        int const vt = e->vtype;
+        int const vb = kpm::vtype_bytes(vt);
+        int const W = e->W;
+        // Velocity operators V = H o (x_i - x_j) in H's scalar type (kpm/Moments.cpp:132-155).
+        // Left: applied to the random starter in the original order (Starter.cpp:66,78).
+        // Right: applied to every collected vector, aligned with the reordered ELL of H~.
+        std::vector<int32_t> hcol(static_cast<size_t>(n) * W);
+        KPM_CUDA(cudaMemcpy(hcol.data(), e->d_col.p, hcol.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        std::vector<unsigned char> vr_ell(static_cast<size_t>(n) * W * vb, 0);
+        std::vector<unsigned char> starters_l, starters_r;
+        int64_t K = 1;
+        {   // vectors per batch: both sides keep M x n x K vectors
+            size_t free_b = 0, total_b = 0;
+            KPM_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            double const per_vec = 2.0 * static_cast<double>(M) * n * vb;
+            int64_t kmax = static_cast<int64_t>(0.5 * static_cast<double>(free_b) / per_vec);
+            if (kmax < 1) fail(KPM_ERR_RUNTIME, "not enough device memory for the conductivity moments");
+            for (int64_t k : {16, 8, 4, 2, 1}) {
+                kpm_engine::Shape sh = e->pick_shape(k);
+                if (k <= kmax && k <= num_random && sh.K == k) { K = k; break; }
+            }
+        }
+        kpm_engine::Shape sh = e->pick_shape(K);
+        if (sh.K != K || sh.nbatch != 1) { K = 1; sh = kpm_engine::Shape{1, 1, 1, 1, 4096}; }
+        int64_t const nrand_pad = ((num_random + K - 1) / K) * K;
+        size_t const ssize = static_cast<size_t>(scalar_bytes(e->stype));
+        starters_l.assign(static_cast<size_t>(nrand_pad) * n * ssize, 0);
+        starters_r.assign(static_cast<size_t>(nrand_pad) * n * ssize, 0);
+        with_scalar(e->stype, [&](auto zi) {
+            using T = decltype(zi);
+            using R = real_of<T>;
+            auto const* hv = reinterpret_cast<T const*>(e->values.data());
+            std::vector<T> vl(e->indices.size());
+            for (int64_t r = 0; r < n; ++r)
+                for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) {
+                    int32_t const c = e->indices[k];
+                    vl[k] = hv[k] * static_cast<T>(left[r] - left[c]);
+                    T const vrv = hv[k] * static_cast<T>(right[r] - right[c]);
+                    int32_t const nr = e->map[r], nc = e->map[c];
+                    int j = 0;
+                    while (j < W && hcol[static_cast<size_t>(nr) * W + j] != nc) ++j;
+                    if (j == W) fail(KPM_ERR_RUNTIME, "internal: velocity entry outside the H~ pattern");
+                    with_vtype(vt, [&](auto zc) {
+                        using Tc = decltype(zc);
+                        reinterpret_cast<Tc*>(vr_ell.data())[static_cast<size_t>(nr) * W + j] = convert<Tc>(vrv);
+                    });
+                }
+            // both starters own a default-seeded generator, so left and right draw the same r
+            std::mt19937 gen;
+            std::uniform_real_distribution<R> dist;
+            auto* sl = reinterpret_cast<T*>(starters_l.data());
+            auto* sr = reinterpret_cast<T*>(starters_r.data());
+            std::vector<T> rv(n);
+            for (int64_t v = 0; v < num_random; ++v) {
+                for (int64_t i = 0; i < n; ++i) {
+                    if constexpr (is_cplx_v<T>) {
+                        std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
+                        std::complex<R> const kk(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
+                        rv[i] = std::exp(kk * dist(gen));
+                    } else {
+                        rv[i] = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
+                    }
+                }
+                for (int64_t r = 0; r < n; ++r) {
+                    T acc = T(0);
+                    for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) acc += vl[k] * rv[e->indices[k]];
+                    sl[v * n + r] = acc;
+                    sr[v * n + r] = rv[r];
+                }
+            }
+        });
+        // device buffers
+        size_t const vec_bytes = static_cast<size_t>(n) * K * vb;
+        DBuf d_v2, d_L, d_R, d_mu_acc, d_samples, d_sum, d_chem, d_res;
+        d_v2.ensure(vr_ell.size());
+        KPM_CUDA(cudaMemcpyAsync(d_v2.p, vr_ell.data(), vr_ell.size(), cudaMemcpyHostToDevice, e->stream));
+        d_L.ensure(vec_bytes * M);
+        d_R.ensure(vec_bytes * M);
+        e->d_x0.ensure(vec_bytes);
+        e->d_x1.ensure(vec_bytes);
+        e->d_stage.ensure(static_cast<size_t>(K) * n * ssize);
+        d_mu_acc.ensure(sizeof(double) * 2 * M * M);
+        KPM_CUDA(cudaMemsetAsync(d_mu_acc.p, 0, sizeof(double) * 2 * M * M, e->stream));
+        int const ntiles = e->build_tiles(sh, true);
+        double rec_time = 0;
+        auto recursion = [&](unsigned char const* host_starters, bool right_side) {
+            KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, host_starters, static_cast<size_t>(K) * n * ssize,
+                                     cudaMemcpyHostToDevice, e->stream));
+            KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, vec_bytes, e->stream));
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, e->d_stage.p, e->d_x0.p, e->d_map.as<int32_t>(),
+                                                  e->d_sysoff.as<int64_t>(), 1, K, static_cast<int>(K), 1, n, e->stream));
+            kpm::DenseStep a{};
+            a.vtype = vt;
+            a.E = sh.E;
+            a.LPR = sh.LPR;
+            a.col = e->d_col.as<int32_t>();
+            a.val = e->d_val.p;
+            a.val2 = right_side ? d_v2.p : nullptr;
+            a.W = W;
+            a.tiles = e->d_tiles.as<Tile>();
+            a.num_tiles = ntiles;
+            unsigned char* store = static_cast<unsigned char*>(right_side ? d_R.p : d_L.p);
+            KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
+            // init: r1 = H~ r0 / 2, store r0 (or V r0) as row 0; steps n = 2..M-1 store row n-1;
+            // one extra step stores row M-1 (its recursion output is not used)
+            void* r0 = e->d_x0.p;
+            void* r1 = e->d_x1.p;
+            for (int64_t step = 1; step <= M; ++step) {
+                a.init = step == 1;
+                a.x = step == 1 ? r0 : r1;
+                a.y = step == 1 ? r1 : r0;
+                void* row = store + vec_bytes * (step - 1);
+                a.zx = right_side ? nullptr : row;
+                a.zv = right_side ? row : nullptr;
+                KPM_CUDA(kpm::launch_dense_step(a, e->stream));
+                if (step > 1) std::swap(r0, r1);
+            }
+            KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+            float ms = 0;
+            KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+            rec_time += ms * 1e-3;
+        };
+        double gemm_time = 0;
+        for (int64_t b = 0; b < nrand_pad / K; ++b) {
+            recursion(starters_l.data() + static_cast<size_t>(b) * K * n * ssize, false);
+            recursion(starters_r.data() + static_cast<size_t>(b) * K * n * ssize, true);
+            KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
+            // mu += L R^H: inner dimension = rows x K (rows n of both stores are [row][K])
+            KPM_CUDA(kpm::launch_mu_gemm_fp64(vt, d_L.p, d_R.p, M, n * K, d_mu_acc.as<double>(), e->stream));
+            KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
+            KPM_CUDA(cudaStreamSynchronize(e->stream));
+            float ms = 0;
+            KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+            gemm_time += ms * 1e-3;
+        }
+        // normalise, halve row/column 0 (the collectors store T_0 / 2), damp g_m g_n (Kernel.hpp:48-56)
+        std::vector<double> mu(static_cast<size_t>(2 * M * M));
+        KPM_CUDA(cudaMemcpy(mu.data(), d_mu_acc.p, sizeof(double) * mu.size(), cudaMemcpyDeviceToHost));
+        auto g = damping(e->cfg.kernel, e->cfg.kernel_param, M);
+        for (int64_t c = 0; c < M; ++c)
+            for (int64_t r = 0; r < M; ++r) {
+                double f = g[r] * g[c] / static_cast<double>(num_random);
+                if (r == 0) f *= 0.5;
+                if (c == 0) f *= 0.5;
+                mu[2 * (c * M + r)] *= f;
+                mu[2 * (c * M + r) + 1] *= f;
+            }
+        KPM_CUDA(cudaMemcpy(d_mu_acc.p, mu.data(), sizeof(double) * mu.size(), cudaMemcpyHostToDevice));
+        // energy samples: bounds.linspaced(num_points) scaled (reconstruct.hpp:101-103)
+        auto const& bs = e->sys[0];
+        std::vector<double> samples(num_points), chem_s(nmu);
+        for (int64_t i = 0; i < num_points; ++i)
+            samples[i] = (bs.emin + (bs.emax - bs.emin) * static_cast<double>(i) / static_cast<double>(num_points - 1) - sc.b) / sc.a;
+        samples[num_points - 1] = (bs.emax - sc.b) / sc.a;
+        for (int64_t j = 0; j < nmu; ++j) chem_s[j] = (chem[j] - sc.b) / sc.a;
+        double const smax = *std::max_element(samples.begin(), samples.end());
+        double const smin = *std::min_element(samples.begin(), samples.end());
+        double const coeff = (smax - smin) / static_cast<double>(2 * num_points);
+        double const inv_kbt = sc.a / (static_cast<double>(8.6173303e-5f) * temperature);
+        double const prefix = 4.0 / (sc.a * sc.a);
+        d_samples.ensure(sizeof(double) * num_points);
+        d_sum.ensure(sizeof(double) * 2 * num_points);
+        d_chem.ensure(sizeof(double) * std::max<int64_t>(nmu, 1));
+        d_res.ensure(sizeof(double) * 2 * std::max<int64_t>(nmu, 1));
+        KPM_CUDA(cudaMemcpyAsync(d_samples.p, samples.data(), sizeof(double) * num_points, cudaMemcpyHostToDevice, e->stream));
+        KPM_CUDA(cudaMemcpyAsync(d_chem.p, chem_s.data(), sizeof(double) * nmu, cudaMemcpyHostToDevice, e->stream));
+        KPM_CUDA(kpm::launch_kubo_sum(d_mu_acc.as<double>(), M, d_samples.as<double>(), static_cast<int>(num_points),
+                                      d_sum.as<double>(), e->stream));
+        KPM_CUDA(kpm::launch_kubo_integrate(d_sum.as<double>(), d_samples.as<double>(), static_cast<int>(num_points),
+                                            d_chem.as<double>(), static_cast<int>(nmu), inv_kbt, coeff, prefix,
+                                            d_res.as<double>(), e->stream));
+        KPM_CUDA(cudaMemcpyAsync(out, d_res.p, sizeof(double) * 2 * nmu, cudaMemcpyDeviceToHost, e->stream));
+        KPM_CUDA(cudaStreamSynchronize(e->stream));
+        e->st.moments_time = rec_time + gemm_time;
+        e->reset_stats(M, false, false, static_cast<double>(num_random) * 2, 0);
+        e->finish_stats();
+        e->last_gemm_time = gemm_time;
+        e->calc_time = now_s() - t0;
     });
 }
 

@@ -60,7 +60,42 @@ struct OffStep {
     double* acc;
 };
 
+// Dense-collection step for the Kubo-Bastin moments (kpm/default/collectors.cpp:78-107):
+// y <- H~ x - y (or H~ x / 2 when init) and, per row, optionally
+//   zx[r] = x[r]                       (store T_{n-1}: the left vectors)
+//   zv[r] = sum_j val2[r][j] x[c_j]    (store V T_{n-1}: the right vectors)
+struct DenseStep {
+    int vtype;
+    int E, LPR;
+    const int32_t* col;
+    const void* val;
+    const void* val2;         // nullable
+    int W;
+    const void* x;
+    void* y;
+    void* zx;                 // nullable, [rows][K]
+    void* zv;                 // nullable, [rows][K]
+    const Tile* tiles;
+    int num_tiles;
+    bool init;
+};
+
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s);
+cudaError_t launch_dense_step(DenseStep const& a, cudaStream_t s);
+
+// mu[n * M + m] += sum_i A[m * I + i] * conj(B[n * I + i]) in FP64 (complex double mu),
+// A and B in vtype; split over I with FP64 atomics.
+cudaError_t launch_mu_gemm_fp64(int vtype, void const* A, void const* B, int64_t M, int64_t I, double* mu,
+                                cudaStream_t s);
+
+// Kubo-Bastin (kpm/reconstruct.hpp:90-143) in FP64:
+// sum_nm[e] = 1/(1-en^2)^2 * sum_{m,n} mu(m,n) (A_n T_m + conj(A_m) T_n), en = scaled sample e
+cudaError_t launch_kubo_sum(double const* mu, int64_t M, double const* scaled_samples, int ns, double* sum_nm,
+                            cudaStream_t s);
+// out[j] = prefix * coeff * sum_e w_e fd(en_e, mu_j) sum_nm[e]
+cudaError_t launch_kubo_integrate(double const* sum_nm, double const* scaled_samples, int ns,
+                                  double const* scaled_mu, int nmu, double inv_kbt, double coeff, double prefix,
+                                  double* out, cudaStream_t s);
 cudaError_t launch_off_step(OffStep const& a, cudaStream_t s);
 bool diag_shape_supported(int vtype, int E, int LPR);
 
@@ -77,9 +112,10 @@ cudaError_t launch_average(double const* per_vec, int num_systems, int64_t nvec,
 cudaError_t launch_set_units(int vtype, void* dst, int32_t const* pos, int64_t nvec, int K, int64_t rows_total,
                              cudaStream_t s);
 
-// scatter host-order starters into the reordered, batched device layout:
+// scatter host-order starters (scalar type `stype`, same codes as VType) into the
+// reordered, batched device layout of type `vtype`:
 // dst[(b * rows_total + map[g]) * K + j] = src[(s, v, i)], v = b*K + j
-cudaError_t launch_scatter_starters(int vtype, void const* src, void* dst, int32_t const* map,
+cudaError_t launch_scatter_starters(int stype, int vtype, void const* src, void* dst, int32_t const* map,
                                     int64_t const* sys_offsets, int num_systems, int64_t nvec,
                                     int K, int nbatch, int64_t rows_total, cudaStream_t s);
 

@@ -21,6 +21,7 @@
 // GB300's FP64 rate is ~1/300 of its FP32 rate.
 #include "kpm_internal.h"
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 
@@ -281,6 +282,217 @@ off_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
     }
 }
 
+// ------------------------------------------------------------------ dense collection step
+template<class V, int E, int LPR, bool INIT>
+__global__ void __launch_bounds__(BLOCK)
+dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V const* __restrict__ val2, int W,
+                  V const* __restrict__ x, V* __restrict__ y, V* __restrict__ zx, V* __restrict__ zv,
+                  Tile const* __restrict__ tiles) {
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;
+    using P = Pack<V, E>;
+    Tile const t = tiles[blockIdx.x];
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    for (int r = t.row_begin + slot; r < t.row_end; r += RPP) {
+        V sum[E], sv[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(sv[e]); }
+        int32_t const* cp = col + static_cast<int64_t>(r) * W;
+        V const* vp = val + static_cast<int64_t>(r) * W;
+        for (int j = 0; j < W; ++j) {
+            int32_t const c = __ldg(cp + j);
+            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
+            V const a = vp[j];
+#pragma unroll
+            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+            if (zv != nullptr) {
+                V const b = val2[static_cast<int64_t>(r) * W + j];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sv[e], b, xv.v[e]);
+            }
+        }
+        int64_t const off = static_cast<int64_t>(r) * K;
+        P* yp = reinterpret_cast<P*>(y + off) + lane;
+        P yn;
+        if (INIT) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) yn.v[e] = vhalf(sum[e]);
+        } else {
+            P const yo = *yp;
+#pragma unroll
+            for (int e = 0; e < E; ++e) yn.v[e] = vsub(sum[e], yo.v[e]);
+        }
+        *yp = yn;
+        if (zx != nullptr) reinterpret_cast<P*>(zx + off)[lane] = reinterpret_cast<P const*>(x + off)[lane];
+        if (zv != nullptr) {
+            P o;
+#pragma unroll
+            for (int e = 0; e < E; ++e) o.v[e] = sv[e];
+            reinterpret_cast<P*>(zv + off)[lane] = o;
+        }
+    }
+}
+
+template<class V, int E, int LPR>
+cudaError_t dense_launch(DenseStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    auto const* val = static_cast<V const*>(a.val);
+    auto const* val2 = static_cast<V const*>(a.val2);
+    auto const* x = static_cast<V const*>(a.x);
+    auto* y = static_cast<V*>(a.y);
+    auto* zx = static_cast<V*>(a.zx);
+    auto* zv = static_cast<V*>(a.zv);
+    if (a.init)
+        dense_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.tiles);
+    else
+        dense_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.tiles);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ FP64 moments-matrix GEMM (split over I)
+__device__ __forceinline__ double2 to_cd(float v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ double2 to_cd(double v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ double2 to_cd(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_cd(double2 v) { return v; }
+
+constexpr int GT = 32;  // output tile and inner chunk
+
+template<class V>
+__global__ void __launch_bounds__(BLOCK)
+mu_gemm_kernel(V const* __restrict__ A, V const* __restrict__ B, int64_t M, int64_t I, int64_t chunk,
+               double* __restrict__ mu) {
+    __shared__ double2 As[GT][GT + 1];
+    __shared__ double2 Bs[GT][GT + 1];
+    int64_t const m0 = blockIdx.x * GT, n0 = blockIdx.y * GT;
+    int64_t const i_begin = blockIdx.z * chunk;
+    int64_t const i_end = min(I, i_begin + chunk);
+    int const tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 2x2 outputs per thread
+    double2 acc[2][2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) acc[p][q] = make_double2(0.0, 0.0);
+    for (int64_t i0 = i_begin; i0 < i_end; i0 += GT) {
+        for (int idx = threadIdx.x; idx < GT * GT; idx += BLOCK) {
+            int const rr = idx / GT, ii = idx % GT;
+            int64_t const gi = i0 + ii;
+            As[ii][rr] = (m0 + rr < M && gi < i_end) ? to_cd(A[(m0 + rr) * I + gi]) : make_double2(0.0, 0.0);
+            Bs[ii][rr] = (n0 + rr < M && gi < i_end) ? to_cd(B[(n0 + rr) * I + gi]) : make_double2(0.0, 0.0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int ii = 0; ii < GT; ++ii) {
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                double2 const a = As[ii][tx + 16 * p];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    double2 const b = Bs[ii][ty + 16 * q];
+                    // a * conj(b)
+                    acc[p][q].x = fma(a.x, b.x, fma(a.y, b.y, acc[p][q].x));
+                    acc[p][q].y = fma(a.y, b.x, fma(-a.x, b.y, acc[p][q].y));
+                }
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            int64_t const m = m0 + tx + 16 * p, n = n0 + ty + 16 * q;
+            if (m < M && n < M) {
+                atomicAdd(mu + 2 * (n * M + m), acc[p][q].x);
+                atomicAdd(mu + 2 * (n * M + m) + 1, acc[p][q].y);
+            }
+        }
+}
+
+// ------------------------------------------------------------------ Kubo-Bastin
+__global__ void __launch_bounds__(BLOCK)
+kubo_sum_kernel(double const* __restrict__ mu, int64_t M, double const* __restrict__ samples,
+                double* __restrict__ sum_nm) {
+    extern __shared__ double Tm[];  // M values cos(m theta)
+    __shared__ double shr[WARPS], shi[WARPS];
+    int const e = blockIdx.x;
+    double const en = samples[e];
+    double const th = acos(en);
+    double const sq = sqrt(1.0 - en * en);
+    for (int64_t m = threadIdx.x; m < M; m += BLOCK) Tm[m] = cos(static_cast<double>(m) * th);
+    __syncthreads();
+    double re = 0.0, im = 0.0;
+    int const warp = threadIdx.x / 32, wl = threadIdx.x % 32;
+    // sum_n A_n u_n, u_n = sum_m mu(m,n) T_m (column n contiguous in m)
+    for (int64_t n = warp; n < M; n += WARPS) {
+        double ur = 0.0, ui = 0.0;
+        double const* c = mu + 2 * n * M;
+        for (int64_t m = wl; m < M; m += 32) {
+            ur = fma(c[2 * m], Tm[m], ur);
+            ui = fma(c[2 * m + 1], Tm[m], ui);
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            ur += __shfl_xor_sync(0xffffffffu, ur, off);
+            ui += __shfl_xor_sync(0xffffffffu, ui, off);
+        }
+        if (wl == 0) {
+            double const nr = static_cast<double>(n);
+            double sn, cn;
+            sincos(nr * th, &sn, &cn);
+            // A_n = (en - i n sq) (cn + i sn)
+            double const ar = en * cn + nr * sq * sn;
+            double const ai = en * sn - nr * sq * cn;
+            re += ar * ur - ai * ui;
+            im += ar * ui + ai * ur;
+        }
+    }
+    // sum_m conj(A_m) v_m, v_m = sum_n mu(m,n) T_n
+    for (int64_t m = threadIdx.x; m < M; m += BLOCK) {
+        double vr = 0.0, vi = 0.0;
+        for (int64_t n = 0; n < M; ++n) {
+            vr = fma(mu[2 * (n * M + m)], Tm[n], vr);
+            vi = fma(mu[2 * (n * M + m) + 1], Tm[n], vi);
+        }
+        double const mr = static_cast<double>(m);
+        double sm, cm;
+        sincos(mr * th, &sm, &cm);
+        double const ar = en * cm + mr * sq * sm;
+        double const ai = -(en * sm - mr * sq * cm);  // conj(A_m)
+        re += ar * vr - ai * vi;
+        im += ar * vi + ai * vr;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, off);
+        im += __shfl_xor_sync(0xffffffffu, im, off);
+    }
+    if (wl == 0) { shr[warp] = re; shi[warp] = im; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tr = 0.0, ti = 0.0;
+        for (int w = 0; w < WARPS; ++w) { tr += shr[w]; ti += shi[w]; }
+        double const k = 1.0 / ((1.0 - en * en) * (1.0 - en * en));
+        sum_nm[2 * e] = k * tr;
+        sum_nm[2 * e + 1] = k * ti;
+    }
+}
+
+__global__ void kubo_integrate_kernel(double const* __restrict__ sum_nm, double const* __restrict__ samples, int ns,
+                                      double const* __restrict__ chem, int nmu, double inv_kbt, double coeff,
+                                      double prefix, double* __restrict__ out) {
+    int const j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nmu) return;
+    double const mu = chem[j];
+    double tr = 0.0, ti = 0.0;
+    for (int e = 0; e < ns; ++e) {
+        double const fd = 1.0 / (1.0 + exp((samples[e] - mu) * inv_kbt));
+        double const w = (e == 0 || e == ns - 1) ? 1.0 : 2.0;
+        tr += w * fd * sum_nm[2 * e];
+        ti += w * fd * sum_nm[2 * e + 1];
+    }
+    out[2 * j] = prefix * coeff * tr;
+    out[2 * j + 1] = prefix * coeff * ti;
+}
+
 template<class V, int E, int LPR>
 cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
@@ -375,8 +587,18 @@ __global__ void average_kernel(double const* __restrict__ per_vec, int num_syste
 }
 
 // ------------------------------------------------------------------ starters scatter
-template<class V>
-__global__ void scatter_kernel(V const* __restrict__ src, V* __restrict__ dst, int32_t const* __restrict__ map,
+__device__ __forceinline__ void cvt(float& d, float v) { d = v; }
+__device__ __forceinline__ void cvt(double& d, float v) { d = v; }
+__device__ __forceinline__ void cvt(float& d, double v) { d = static_cast<float>(v); }
+__device__ __forceinline__ void cvt(double& d, double v) { d = v; }
+__device__ __forceinline__ void cvt(float2& d, float2 v) { d = v; }
+__device__ __forceinline__ void cvt(double2& d, float2 v) { d = make_double2(v.x, v.y); }
+__device__ __forceinline__ void cvt(float2& d, double2 v) { d = make_float2(static_cast<float>(v.x), static_cast<float>(v.y)); }
+__device__ __forceinline__ void cvt(double2& d, double2 v) { d = v; }
+
+// src in the Hamiltonian's scalar type S, dst in the recursion type V
+template<class S, class V>
+__global__ void scatter_kernel(S const* __restrict__ src, V* __restrict__ dst, int32_t const* __restrict__ map,
                                int64_t const* __restrict__ sys_off, int num_systems, int64_t nvec, int K,
                                int64_t rows_total) {
     int64_t const v = blockIdx.y;
@@ -389,7 +611,8 @@ __global__ void scatter_kernel(V const* __restrict__ src, V* __restrict__ dst, i
         }
         int64_t const off = sys_off[lo];
         int64_t const rows_s = sys_off[lo + 1] - off;
-        V const value = src[off * nvec + v * rows_s + (g - off)];
+        V value;
+        cvt(value, src[off * nvec + v * rows_s + (g - off)]);
         int64_t const b = v / K, j = v % K;
         dst[(b * rows_total + map[g]) * K + j] = value;
     }
@@ -579,6 +802,50 @@ cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s) {
     return cudaErrorInvalidValue;
 }
 
+cudaError_t launch_dense_step(DenseStep const& a, cudaStream_t s) {
+#define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return dense_launch<V, e, l>(a, s);
+    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
+#undef KPM_DISPATCH
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_mu_gemm_fp64(int vtype, void const* A, void const* B, int64_t M, int64_t I, double* mu,
+                                cudaStream_t s) {
+    int64_t const tiles = ((M + GT - 1) / GT) * ((M + GT - 1) / GT);
+    int64_t splits = std::max<int64_t>(1, (152 * 8 + tiles - 1) / tiles);
+    int64_t chunk = (I + splits - 1) / splits;
+    chunk = ((chunk + GT - 1) / GT) * GT;
+    splits = (I + chunk - 1) / chunk;
+    dim3 grid(static_cast<unsigned>((M + GT - 1) / GT), static_cast<unsigned>((M + GT - 1) / GT),
+              static_cast<unsigned>(splits));
+    switch (vtype) {
+        case V_F32: mu_gemm_kernel<float><<<grid, BLOCK, 0, s>>>(static_cast<float const*>(A), static_cast<float const*>(B), M, I, chunk, mu); break;
+        case V_F64: mu_gemm_kernel<double><<<grid, BLOCK, 0, s>>>(static_cast<double const*>(A), static_cast<double const*>(B), M, I, chunk, mu); break;
+        case V_C64: mu_gemm_kernel<float2><<<grid, BLOCK, 0, s>>>(static_cast<float2 const*>(A), static_cast<float2 const*>(B), M, I, chunk, mu); break;
+        default: mu_gemm_kernel<double2><<<grid, BLOCK, 0, s>>>(static_cast<double2 const*>(A), static_cast<double2 const*>(B), M, I, chunk, mu); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kubo_sum(double const* mu, int64_t M, double const* samples, int ns, double* sum_nm,
+                            cudaStream_t s) {
+    size_t const smem = sizeof(double) * static_cast<size_t>(M);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kubo_sum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    kubo_sum_kernel<<<ns, BLOCK, smem, s>>>(mu, M, samples, sum_nm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kubo_integrate(double const* sum_nm, double const* samples, int ns, double const* chem, int nmu,
+                                  double inv_kbt, double coeff, double prefix, double* out, cudaStream_t s) {
+    if (nmu == 0) return cudaSuccess;
+    kubo_integrate_kernel<<<(nmu + 127) / 128, 128, 0, s>>>(sum_nm, samples, ns, chem, nmu, inv_kbt, coeff, prefix, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_off_step(OffStep const& a, cudaStream_t s) {
 #define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return off_launch<V, e, l>(a, s);
     KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
@@ -602,18 +869,23 @@ cudaError_t launch_average(double const* per_vec, int num_systems, int64_t nvec,
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_starters(int vtype, void const* src, void* dst, int32_t const* map,
+cudaError_t launch_scatter_starters(int stype, int vtype, void const* src, void* dst, int32_t const* map,
                                     int64_t const* sys_offsets, int num_systems, int64_t nvec, int K, int nbatch,
                                     int64_t rows_total, cudaStream_t s) {
     (void)nbatch;
     if (nvec == 0 || rows_total == 0) return cudaSuccess;
+    if (vtype_complex(stype) != vtype_complex(vtype)) return cudaErrorInvalidValue;
     dim3 grid(grid_for(rows_total) > 4096 ? 4096 : grid_for(rows_total), static_cast<unsigned>(nvec));
-    switch (vtype) {
-        case V_F32: scatter_kernel<float><<<grid, BLOCK, 0, s>>>(static_cast<float const*>(src), static_cast<float*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
-        case V_F64: scatter_kernel<double><<<grid, BLOCK, 0, s>>>(static_cast<double const*>(src), static_cast<double*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
-        case V_C64: scatter_kernel<float2><<<grid, BLOCK, 0, s>>>(static_cast<float2 const*>(src), static_cast<float2*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
-        default: scatter_kernel<double2><<<grid, BLOCK, 0, s>>>(static_cast<double2 const*>(src), static_cast<double2*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total); break;
-    }
+#define KPM_SC(S, V) scatter_kernel<S, V><<<grid, BLOCK, 0, s>>>(static_cast<S const*>(src), static_cast<V*>(dst), map, sys_offsets, num_systems, nvec, K, rows_total)
+    if (stype == V_F32 && vtype == V_F32) KPM_SC(float, float);
+    else if (stype == V_F32 && vtype == V_F64) KPM_SC(float, double);
+    else if (stype == V_F64 && vtype == V_F32) KPM_SC(double, float);
+    else if (stype == V_F64 && vtype == V_F64) KPM_SC(double, double);
+    else if (stype == V_C64 && vtype == V_C64) KPM_SC(float2, float2);
+    else if (stype == V_C64 && vtype == V_C128) KPM_SC(float2, double2);
+    else if (stype == V_C128 && vtype == V_C64) KPM_SC(double2, float2);
+    else KPM_SC(double2, double2);
+#undef KPM_SC
     return cudaGetLastError();
 }
 

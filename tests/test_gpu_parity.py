@@ -226,3 +226,32 @@ def test_report_and_stats():
     assert s.num_moments > 0 and s.moments_time > 0 and s.eps > 0
     r = k.report(shortform=True)
     assert "eps" in r and r.count("[") >= 3
+
+
+@pytest.mark.parametrize("name", list(TM.COND_MODELS))
+def test_conductivity_matches_reference_golden(baselines, name):
+    """tests/test_kpm.py:176-197 (energy_range [-9, 9], Lorentz, T = 0, 200 points; rtol 1e-2, atol 1e-5)"""
+    kind, size = TM.COND_MODELS[name]
+    model = TM.graphene(kind, size)
+    energy = np.linspace(-2, 2, 25)
+    for cfg in [dict(optimal_size=False, interleaved=False), dict(optimal_size=True, interleaved=True)]:
+        k = kpm(model, energy_range=[-9, 9], kernel=lorentz_kernel(), silent=True, matrix_format="ELL", **cfg)
+        sigma = k.calc_conductivity(energy, broadening=0.5, temperature=0, num_points=200)
+        np.testing.assert_allclose(sigma.data, baselines["conductivity[%s]" % name], rtol=1e-2, atol=1e-5)
+
+
+def test_conductivity_fp64_equals_oracle(oracle):
+    """FP64 Kubo-Bastin (dense moments + mu_mn GEMM + reconstruction) against the oracle's Core::conductivity."""
+    m = TM.graphene("magnetic_field", 6)
+    h = m.hamiltonian.astype(np.complex128)
+    x, y = m.system.x, m.system.y
+    chem = np.linspace(-1.9, 2.1, 9)
+    cfg = dict(energy_range=(-9.0, 9.0), kernel="jackson")
+    eng = _native.Engine(h, _native.make_config(**cfg))
+    for left, right, nrand in ((x, x, 3), (x, y, 2)):
+        got = eng.calc_conductivity(left, right, chem, 0.6, 0.0, nrand, 100)
+        ref = oracle.core_conductivity(h, left, right, chem, 0.6, 0.0, nrand, 100, matrix_format="ELL",
+                                       optimal_size=False, interleaved=False, **cfg)
+        err = rel_err(got, ref)
+        print("conductivity fp64 vs oracle: %.3e" % err)
+        assert err < 1e-9
