@@ -260,7 +260,9 @@ def run_gpu(args, rank, world, local_rank):
     avg_launch = rec / launches
     nrows = rows
     vec_bytes = 3 * nrows * R * 4
-    alg_bytes = nnz * (4 + 4) + 4 * (nrows + 1) + vec_bytes
+    # per step: matrix once (FP32 hi/lo value pair + int32 column per non-zero, row extents),
+    # x read once, y_old read once, y_new written once
+    alg_bytes = nnz * (8 + 4) + 4 * (nrows + 1) + vec_bytes
     achieved = alg_bytes / avg_launch / 1e9
     peaks = {}
     try:

@@ -62,7 +62,8 @@ typedef struct kpm_config {
     int32_t interleaved;      /* AlgorithmConfig::interleaved */
     double lanczos_precision; /* percent, default 0.002 */
     int32_t precision;        /* KPM_PREC_* */
-    int32_t batch_width;      /* vectors per recursion block; 0 = autotuned */
+    int32_t batch_width;      /* vectors per recursion block (upper bound); 0 = 256-byte rows */
+    int32_t tile_rows;        /* rows per thread block tile; 0 = autotuned on the first call */
 } kpm_config;
 
 /* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */

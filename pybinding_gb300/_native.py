@@ -29,7 +29,7 @@ class Config(C.Structure):
     _fields_ = [("min_energy", C.c_double), ("max_energy", C.c_double), ("kernel", C.c_int32),
                 ("kernel_param", C.c_double), ("matrix_format", C.c_int32), ("optimal_size", C.c_int32),
                 ("interleaved", C.c_int32), ("lanczos_precision", C.c_double), ("precision", C.c_int32),
-                ("batch_width", C.c_int32)]
+                ("batch_width", C.c_int32), ("tile_rows", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -104,7 +104,8 @@ def check(rc):
 
 
 def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, matrix_format="ELL",
-                optimal_size=True, interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0):
+                optimal_size=True, interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0,
+                tile_rows=0):
     c = Config()
     lib().kpm_config_default(C.byref(c))
     c.min_energy, c.max_energy = float(energy_range[0]), float(energy_range[1])
@@ -116,6 +117,7 @@ def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, mat
     c.lanczos_precision = float(lanczos_precision)
     c.precision = PRECISION_CODE[precision]
     c.batch_width = int(batch_width)
+    c.tile_rows = int(tile_rows)
     return c
 
 

@@ -116,12 +116,13 @@ class GpuImpl:
     """The ``impl`` object of :class:`KPM`: ``_cpp.KPM`` semantics on the CUDA engine."""
 
     def __init__(self, model, energy_range=(0, 0), kernel=None, matrix_format="ELL", optimal_size=True,
-                 interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0, **_):
+                 interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0, tile_rows=0, **_):
         self.kernel = kernel if kernel is not None else jackson_kernel()
         self._cfg_args = dict(energy_range=tuple(energy_range), kernel=self.kernel.name,
                               kernel_param=self.kernel.param, matrix_format=matrix_format,
                               optimal_size=optimal_size, interleaved=interleaved,
-                              lanczos_precision=lanczos_precision, precision=precision, batch_width=batch_width)
+                              lanczos_precision=lanczos_precision, precision=precision, batch_width=batch_width,
+                              tile_rows=tile_rows)
         self._model = model
         self._engine = _native.Engine(model.hamiltonian, _native.make_config(**self._cfg_args))
 
@@ -336,7 +337,8 @@ class KPMBatch:
         args = dict(energy_range=tuple(energy_range or (0, 0)), kernel=self.kernel.name,
                     kernel_param=self.kernel.param)
         args.update({k: v for k, v in kwargs.items() if k in ("matrix_format", "optimal_size", "interleaved",
-                                                              "lanczos_precision", "precision", "batch_width")})
+                                                              "lanczos_precision", "precision", "batch_width",
+                                                              "tile_rows")})
         self.engine = _native.Engine(h, _native.make_config(**args), system_offsets=self.offsets)
 
     def scaling_factors(self):

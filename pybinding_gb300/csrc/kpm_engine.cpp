@@ -605,25 +605,34 @@ struct kpm_engine {
         map.assign(rows, 0);
         std::vector<int32_t> oip{0}, oix;
         W = 0;
+        // H~ in FP64 (the scaled values of create_reordered evaluated in double), then stored in the
+        // recursion type: FP64 as is, FP32 as (hi, lo) pairs
+        bool const cpx = kpm::vtype_complex(vtype);
+        std::vector<cd> oval_c;
+        std::vector<double> oval_r;
+        with_scalar(stype, [&](auto zi) {
+            using Tin = decltype(zi);
+            for (int s = 0; s < nsys; ++s) {
+                std::vector<int32_t> sl = (s == 0) ? src : std::vector<int32_t>{0};
+                if (cpx) reorder_system<cd, Tin>(s, sl, scale(s), reorders(), oip, oix, oval_c, s == 0 ? &slices : nullptr);
+                else reorder_system<double, Tin>(s, sl, scale(s), reorders(), oip, oix, oval_r, s == 0 ? &slices : nullptr);
+            }
+        });
+        for (int64_t r = 0; r < rows; ++r) W = std::max(W, oip[r + 1] - oip[r]);
+        W = std::max(W, 1);
+        int const vs = kpm::vtype_vs(vtype);
+        std::vector<int32_t> col(static_cast<size_t>(rows) * W);
         with_vtype(vtype, [&](auto zc) {
             using Tc = decltype(zc);
-            std::vector<Tc> oval;
-            with_scalar(stype, [&](auto zi) {
-                using Tin = decltype(zi);
-                for (int s = 0; s < nsys; ++s) {
-                    std::vector<int32_t> sl = (s == 0) ? src : std::vector<int32_t>{0};
-                    reorder_system<Tc, Tin>(s, sl, scale(s), reorders(), oip, oix, oval, s == 0 ? &slices : nullptr);
-                }
-            });
-            for (int64_t r = 0; r < rows; ++r) W = std::max(W, oip[r + 1] - oip[r]);
-            W = std::max(W, 1);
-            std::vector<int32_t> col(static_cast<size_t>(rows) * W);
-            std::vector<Tc> val(static_cast<size_t>(rows) * W, Tc(0));
+            std::vector<Tc> val(static_cast<size_t>(rows) * W * vs, Tc(0));
             for (int64_t r = 0; r < rows; ++r) {
                 int j = 0;
                 for (int32_t k = oip[r]; k < oip[r + 1]; ++k, ++j) {
                     col[r * W + j] = oix[k];
-                    val[r * W + j] = oval[k];
+                    cd const h = cpx ? oval_c[k] : cd(oval_r[k], 0.0);
+                    Tc const hi = from_cd<Tc>(h);
+                    val[(r * W + j) * vs] = hi;
+                    if (vs == 2) val[(r * W + j) * vs + 1] = from_cd<Tc>(h - to_cd(hi));
                 }
                 for (; j < W; ++j) col[r * W + j] = static_cast<int32_t>(r);
             }
@@ -686,6 +695,50 @@ struct kpm_engine {
         return sh;
     }
 
+    // Autotuner: the tile height (rows per block) of a launch shape is picked by timing
+    // the diagonal kernel on this engine's matrix. It runs the INIT form (x0 -> x1, a
+    // pure function of x0), so the recursion that follows is unaffected; the
+    // accumulator slot it touches is cleared again by the caller. Cached per shape.
+    struct TuneKey {
+        int vtype, E, LPR, nbatch;
+        int64_t rows;
+        bool operator==(TuneKey const& o) const {
+            return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows;
+        }
+    };
+    std::vector<std::pair<TuneKey, int>> tuned;
+    std::vector<std::pair<int, double>> last_tuning;  // (rows per tile, ms) of the last tuning run
+
+    int tune_tile_rows(Shape sh, bool sys0, kpm::DiagStep base) {
+        TuneKey const key{vtype, sh.E, sh.LPR, sh.nbatch, rows};
+        for (auto const& t : tuned)
+            if (t.first == key) return t.second;
+        int const rpp = 256 / sh.LPR;
+        int best = rpp * 16;
+        int64_t const work = rows * sh.K * sh.nbatch;
+        if (work >= (int64_t{1} << 22)) {  // small problems are latency bound: keep the default
+            double best_ms = 1e30;
+            last_tuning.clear();
+            for (int rpt : {4, 8, 16, 32, 64}) {
+                sh.rows_per_tile = rpp * rpt;
+                base.num_tiles = build_tiles(sh, sys0);
+                base.tiles = d_tiles.as<Tile>();
+                base.init = true;
+                KPM_CUDA(kpm::launch_diag_step(base, stream));  // warm
+                KPM_CUDA(cudaEventRecord(ev0, stream));
+                for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
+                KPM_CUDA(cudaEventRecord(ev1, stream));
+                KPM_CUDA(cudaEventSynchronize(ev1));
+                float ms = 0;
+                KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+                last_tuning.push_back({sh.rows_per_tile, ms / 3});
+                if (ms < best_ms) { best_ms = ms; best = sh.rows_per_tile; }
+            }
+        }
+        tuned.push_back({key, best});
+        return best;
+    }
+
     int build_tiles(Shape const& sh, bool sys0_only) {
         std::vector<Tile> tiles;
         int const ns = sys0_only ? 1 : nsys;
@@ -707,7 +760,7 @@ struct kpm_engine {
                   bool opt_rows) {
         if (M < 2 || (M - 2) % 4 != 0) fail(KPM_ERR_VALUE, "num_moments must satisfy (M - 2) % 4 == 0");
         if (nvec < 1) fail(KPM_ERR_VALUE, "num_vectors must be >= 1");
-        Shape const sh = pick_shape(nvec);
+        Shape sh = pick_shape(nvec);
         int const vb = kpm::vtype_bytes(vtype);
         int const NV = kpm::vtype_nv(vtype);
         bool const sys0 = units != nullptr;
@@ -720,7 +773,7 @@ struct kpm_engine {
         size_t const step_acc = static_cast<size_t>(ns) * sh.nbatch * sh.K * NV;
         d_acc.ensure(sizeof(double) * step_acc * half);
         d_mu.ensure(sizeof(double) * 2 * ns * nvec * M);
-        int const ntiles = build_tiles(sh, sys0);
+        int ntiles = build_tiles(sh, sys0);
 
         KPM_CUDA(cudaMemsetAsync(d_x0.p, 0, vbytes, stream));
         if (units) {
@@ -739,8 +792,6 @@ struct kpm_engine {
             KPM_CUDA(kpm::launch_scatter_starters(stype, vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(),
                                                   nsys, nvec, sh.K, sh.nbatch, rows, stream));
         }
-        KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
-        KPM_CUDA(cudaEventRecord(ev0, stream));
         kpm::DiagStep a{};
         a.vtype = vtype;
         a.E = sh.E;
@@ -753,6 +804,19 @@ struct kpm_engine {
         a.num_tiles = ntiles;
         a.nbatch = sh.nbatch;
         a.row_limit = static_cast<int32_t>(rows);
+        a.x = d_x0.p;
+        a.y = d_x1.p;
+        a.acc = d_acc.as<double>();
+        if (cfg.tile_rows > 0) {
+            sh.rows_per_tile = cfg.tile_rows;
+        } else {
+            sh.rows_per_tile = tune_tile_rows(sh, sys0, a);
+        }
+        ntiles = build_tiles(sh, sys0);
+        a.tiles = d_tiles.as<Tile>();
+        a.num_tiles = ntiles;
+        KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
+        KPM_CUDA(cudaEventRecord(ev0, stream));
         // r1 = H~ r0 / 2 with mu0, mu1 sums
         a.x = d_x0.p;
         a.y = d_x1.p;
@@ -810,7 +874,7 @@ struct kpm_engine {
         st.opt_nnz = onnz;
         st.vec = vec;
         st.opt_vec = ovec;
-        st.matrix_memory = static_cast<int64_t>(rows) * W * (kpm::vtype_bytes(vtype) + 4);
+        st.matrix_memory = static_cast<int64_t>(rows) * W * (kpm::vtype_vs(vtype) * kpm::vtype_bytes(vtype) + 4);
         st.vector_memory = static_cast<int64_t>(rows) * kpm::vtype_bytes(vtype);
     }
     void finish_stats() { st.eps = st.moments_time > 0 ? st.multiplier * st.opt_nnz / st.moments_time : 0.0; }
@@ -860,6 +924,7 @@ void kpm_config_default(kpm_config* c) {
     c->lanczos_precision = 0.002;
     c->precision = KPM_PREC_AUTO;
     c->batch_width = 0;
+    c->tile_rows = 0;
 }
 
 int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const int32_t* indices, const void* values,
@@ -1288,7 +1353,8 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         // Right: applied to every collected vector, aligned with the reordered ELL of H~.
         std::vector<int32_t> hcol(static_cast<size_t>(n) * W);
         KPM_CUDA(cudaMemcpy(hcol.data(), e->d_col.p, hcol.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
-        std::vector<unsigned char> vr_ell(static_cast<size_t>(n) * W * vb, 0);
+        int const vs = kpm::vtype_vs(vt);
+        std::vector<unsigned char> vr_ell(static_cast<size_t>(n) * W * vs * vb, 0);
         std::vector<unsigned char> starters_l, starters_r;
         int64_t K = 1;
         {   // vectors per batch: both sides keep M x n x K vectors
@@ -1317,14 +1383,17 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
                 for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) {
                     int32_t const c = e->indices[k];
                     vl[k] = hv[k] * static_cast<T>(left[r] - left[c]);
-                    T const vrv = hv[k] * static_cast<T>(right[r] - right[c]);
+                    cd const vrv = to_cd(hv[k]) * static_cast<double>(right[r] - right[c]);
                     int32_t const nr = e->map[r], nc = e->map[c];
                     int j = 0;
                     while (j < W && hcol[static_cast<size_t>(nr) * W + j] != nc) ++j;
                     if (j == W) fail(KPM_ERR_RUNTIME, "internal: velocity entry outside the H~ pattern");
                     with_vtype(vt, [&](auto zc) {
                         using Tc = decltype(zc);
-                        reinterpret_cast<Tc*>(vr_ell.data())[static_cast<size_t>(nr) * W + j] = convert<Tc>(vrv);
+                        Tc* o = reinterpret_cast<Tc*>(vr_ell.data()) + (static_cast<size_t>(nr) * W + j) * vs;
+                        Tc const hi = from_cd<Tc>(vrv);
+                        o[0] = hi;
+                        if (vs == 2) o[1] = from_cd<Tc>(vrv - to_cd(hi));
                     });
                 }
             // both starters own a default-seeded generator, so left and right draw the same r

@@ -14,6 +14,8 @@ inline bool vtype_complex(int vt) { return vt == V_C64 || vt == V_C128; }
 inline bool vtype_double(int vt) { return vt == V_F64 || vt == V_C128; }
 // moment sums per vector: real: (|x|^2, <y|x>), complex: (|x|^2, Re<y|x>, Im<y|x>)
 inline int vtype_nv(int vt) { return vtype_complex(vt) ? 3 : 2; }
+// matrix values per ELL entry: FP32 types store (hi, lo) pairs of an FP64 value
+inline int vtype_vs(int vt) { return vtype_double(vt) ? 1 : 2; }
 
 // A tile: rows [row_begin, row_end) of one system for one batch of vectors.
 struct Tile {
@@ -27,7 +29,7 @@ struct DiagStep {
     int vtype;
     int E, LPR;               // K = E * LPR vectors per batch
     const int32_t* col;       // [rows_total][W]
-    const void* val;          // [rows_total][W], vtype
+    const void* val;          // [rows_total][W][vs], vtype (vs = vtype_vs)
     int W;
     const void* x;            // [nbatch][rows_total][K]
     void* y;

@@ -31,11 +31,16 @@ namespace {
 constexpr int BLOCK = 256;
 constexpr int WARPS = BLOCK / 32;
 
+// VS: matrix values per entry. FP32 recursions store each value of H~ as an
+// unevaluated sum hi + lo of two FP32 numbers (hi = fl32(h), lo = fl32(h - hi),
+// h computed in FP64). A plain FP32 H~ shifts the spectrum coherently (every
+// hopping carries the same relative rounding) and that bias dominates the FP32
+// moment error; the pair removes it for one extra FMA per entry.
 template<class V> struct Tr;
-template<> struct Tr<float> { using R = float; static constexpr bool C = false; };
-template<> struct Tr<double> { using R = double; static constexpr bool C = false; };
-template<> struct Tr<float2> { using R = float; static constexpr bool C = true; };
-template<> struct Tr<double2> { using R = double; static constexpr bool C = true; };
+template<> struct Tr<float> { using R = float; static constexpr bool C = false; static constexpr int VS = 2; };
+template<> struct Tr<double> { using R = double; static constexpr bool C = false; static constexpr int VS = 1; };
+template<> struct Tr<float2> { using R = float; static constexpr bool C = true; static constexpr int VS = 2; };
+template<> struct Tr<double2> { using R = double; static constexpr bool C = true; static constexpr int VS = 1; };
 
 __device__ __forceinline__ void vzero(float& a) { a = 0.f; }
 __device__ __forceinline__ void vzero(double& a) { a = 0.0; }
@@ -138,18 +143,24 @@ diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
 #pragma unroll
     for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
 
+    constexpr int VS = Tr<V>::VS;
     for (int r = t.row_begin + slot; r < row_end; r += RPP) {
         V sum[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) vzero(sum[e]);
         int32_t const* cp = col + static_cast<int64_t>(r) * W;
-        V const* vp = val + static_cast<int64_t>(r) * W;
+        V const* vp = val + static_cast<int64_t>(r) * W * VS;
         for (int j = 0; j < W; ++j) {
             int32_t const c = __ldg(cp + j);
-            V const a = vp[j];
             P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
+            V const a = vp[j * VS];
 #pragma unroll
             for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+            if (VS == 2) {
+                V const lo = vp[j * VS + 1];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sum[e], lo, xv.v[e]);
+            }
         }
         P const xr = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane);
         P* yp = reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane;
@@ -222,18 +233,22 @@ off_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
     R dre[E], dim[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) { dre[e] = R(0); dim[e] = R(0); }
+    constexpr int VS = Tr<V>::VS;
     for (int r = t.row_begin + slot; r < row_end; r += RPP) {
         V sum[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) vzero(sum[e]);
         int32_t const* cp = col + static_cast<int64_t>(r) * W;
-        V const* vp = val + static_cast<int64_t>(r) * W;
+        V const* vp = val + static_cast<int64_t>(r) * W * VS;
         for (int j = 0; j < W; ++j) {
             int32_t const c = __ldg(cp + j);
-            V const a = vp[j];
             P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
 #pragma unroll
-            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+            for (int v = 0; v < VS; ++v) {
+                V const a = vp[j * VS + v];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+            }
         }
         P* yp = reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane;
         P yn;
@@ -298,18 +313,22 @@ dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V 
         V sum[E], sv[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(sv[e]); }
+        constexpr int VS = Tr<V>::VS;
         int32_t const* cp = col + static_cast<int64_t>(r) * W;
-        V const* vp = val + static_cast<int64_t>(r) * W;
+        V const* vp = val + static_cast<int64_t>(r) * W * VS;
         for (int j = 0; j < W; ++j) {
             int32_t const c = __ldg(cp + j);
             P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
-            V const a = vp[j];
 #pragma unroll
-            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
-            if (zv != nullptr) {
-                V const b = val2[static_cast<int64_t>(r) * W + j];
+            for (int v = 0; v < VS; ++v) {
+                V const a = vp[j * VS + v];
 #pragma unroll
-                for (int e = 0; e < E; ++e) vfma(sv[e], b, xv.v[e]);
+                for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+                if (zv != nullptr) {
+                    V const b = val2[(static_cast<int64_t>(r) * W + j) * VS + v];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) vfma(sv[e], b, xv.v[e]);
+                }
             }
         }
         int64_t const off = static_cast<int64_t>(r) * K;
