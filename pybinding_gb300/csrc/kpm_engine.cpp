@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -706,34 +707,38 @@ struct kpm_engine {
             return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows;
         }
     };
-    std::vector<std::pair<TuneKey, int>> tuned;
-    std::vector<std::pair<int, double>> last_tuning;  // (rows per tile, ms) of the last tuning run
+    struct Tuned { int rows_per_tile, unroll; };
+    std::vector<std::pair<TuneKey, Tuned>> tuned;
+    std::vector<std::array<double, 3>> last_tuning;  // (rows per tile, unroll, ms) of the last tuning run
 
-    int tune_tile_rows(Shape sh, bool sys0, kpm::DiagStep base) {
+    Tuned tune_diag(Shape sh, bool sys0, kpm::DiagStep base) {
         TuneKey const key{vtype, sh.E, sh.LPR, sh.nbatch, rows};
         for (auto const& t : tuned)
             if (t.first == key) return t.second;
         int const rpp = 256 / sh.LPR;
-        int best = rpp * 16;
+        Tuned best{rpp * 16, 1};
         int64_t const work = rows * sh.K * sh.nbatch;
         if (work >= (int64_t{1} << 22)) {  // small problems are latency bound: keep the default
             double best_ms = 1e30;
             last_tuning.clear();
-            for (int rpt : {4, 8, 16, 32, 64}) {
-                sh.rows_per_tile = rpp * rpt;
-                base.num_tiles = build_tiles(sh, sys0);
-                base.tiles = d_tiles.as<Tile>();
-                base.init = true;
-                KPM_CUDA(kpm::launch_diag_step(base, stream));  // warm
-                KPM_CUDA(cudaEventRecord(ev0, stream));
-                for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
-                KPM_CUDA(cudaEventRecord(ev1, stream));
-                KPM_CUDA(cudaEventSynchronize(ev1));
-                float ms = 0;
-                KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                last_tuning.push_back({sh.rows_per_tile, ms / 3});
-                if (ms < best_ms) { best_ms = ms; best = sh.rows_per_tile; }
-            }
+            for (int unroll : {1, 2})
+                for (int rpt : {4, 8, 16, 32, 64}) {
+                    if (rpt < 2 * unroll) continue;
+                    sh.rows_per_tile = rpp * rpt;
+                    base.num_tiles = build_tiles(sh, sys0);
+                    base.tiles = d_tiles.as<Tile>();
+                    base.init = true;
+                    base.unroll = unroll;
+                    KPM_CUDA(kpm::launch_diag_step(base, stream));  // warm
+                    KPM_CUDA(cudaEventRecord(ev0, stream));
+                    for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
+                    KPM_CUDA(cudaEventRecord(ev1, stream));
+                    KPM_CUDA(cudaEventSynchronize(ev1));
+                    float ms = 0;
+                    KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+                    last_tuning.push_back({static_cast<double>(sh.rows_per_tile), static_cast<double>(unroll), ms / 3});
+                    if (ms < best_ms) { best_ms = ms; best = Tuned{sh.rows_per_tile, unroll}; }
+                }
         }
         tuned.push_back({key, best});
         return best;
@@ -810,7 +815,9 @@ struct kpm_engine {
         if (cfg.tile_rows > 0) {
             sh.rows_per_tile = cfg.tile_rows;
         } else {
-            sh.rows_per_tile = tune_tile_rows(sh, sys0, a);
+            Tuned const tu = tune_diag(sh, sys0, a);
+            sh.rows_per_tile = tu.rows_per_tile;
+            a.unroll = tu.unroll;
         }
         ntiles = build_tiles(sh, sys0);
         a.tiles = d_tiles.as<Tile>();

@@ -40,6 +40,7 @@ struct DiagStep {
     int nbatch;
     double* acc;
     bool init;
+    int unroll = 1;           // rows per thread per iteration (1 or 2), chosen by the autotuner
 };
 
 // Off-diagonal step: y <- H~ x - y (or H~ x / 2 when init), optional fused dot

@@ -62,6 +62,10 @@ __device__ __forceinline__ void vfma(double2& acc, double2 a, double2 x) {
     acc.y = fma(a.x, x.y, acc.y);
     acc.y = fma(a.y, x.x, acc.y);
 }
+__device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+__device__ __forceinline__ double vadd(double a, double b) { return a + b; }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 vadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float vsub(float a, float b) { return a - b; }
 __device__ __forceinline__ double vsub(double a, double b) { return a - b; }
 __device__ __forceinline__ float2 vsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -120,69 +124,91 @@ __device__ __forceinline__ void st_stream(P* p, P const& v) {
 }
 
 // ------------------------------------------------------------------ diagonal step
-template<class V, int E, int LPR, bool INIT>
-__global__ void __launch_bounds__(BLOCK)
-diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
-                 V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
-                 Tile const* __restrict__ tiles, int32_t row_limit, int nbatch, double* __restrict__ acc) {
+// One row of y <- H~ x - y for this lane's E vectors. The row's entries are taken
+// in chunks of 4 with every load of a chunk issued before its first use, so a row
+// costs two dependent memory round trips (indices, then gathers) rather than one
+// per entry; x[r] and y_old[r] are issued ahead of the index loads.
+template<class V, int E, int LPR, bool INIT, int U>
+__device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
+                                          V const* __restrict__ x, V* __restrict__ y, int const (&rr)[U],
+                                          bool const (&live)[U], int lane, typename Tr<V>::R (&m2)[E],
+                                          typename Tr<V>::R (&m3r)[E], typename Tr<V>::R (&m3i)[E]) {
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int VS = Tr<V>::VS;
+    using P = Pack<V, E>;
+    P xr[U], yo[U];
+    V sum[U][E], lo[U][E];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (!live[u]) continue;
+        xr[u] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(rr[u]) * K) + lane);
+        if (!INIT) yo[u] = ld_stream(reinterpret_cast<P const*>(y + static_cast<int64_t>(rr[u]) * K) + lane);
+#pragma unroll
+        for (int e = 0; e < E; ++e) { vzero(sum[u][e]); vzero(lo[u][e]); }
+    }
+    for (int j0 = 0; j0 < W; j0 += 4) {
+        int32_t c[U][4];
+        P xv[U][4];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                c[u][q] = (live[u] && j0 + q < W) ? __ldg(col + static_cast<int64_t>(rr[u]) * W + j0 + q) : 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (live[u] && j0 + q < W)
+                    xv[u][q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[u][q]) * K) + lane);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (!(live[u] && j0 + q < W)) continue;
+                V const* vp = val + (static_cast<int64_t>(rr[u]) * W + j0 + q) * VS;
+                V const a = vp[0];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sum[u][e], a, xv[u][q].v[e]);
+                if (VS == 2) {
+                    V const b = vp[1];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) vfma(lo[u][e], b, xv[u][q].v[e]);
+                }
+            }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (!live[u]) continue;
+        P yn;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            V const s = (VS == 2) ? vadd(sum[u][e], lo[u][e]) : sum[u][e];
+            yn.v[e] = INIT ? vhalf(s) : vsub(s, yo[u].v[e]);
+        }
+        st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(rr[u]) * K) + lane, yn);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            m2[e] += vsq(xr[u].v[e]);
+            m3r[e] += vdre(yn.v[e], xr[u].v[e]);
+            if (CPLX) m3i[e] += vdim(yn.v[e], xr[u].v[e]);
+        }
+    }
+}
+
+// Persistent form: block b takes tiles b, b+G, b+2G, ... so that all blocks sweep the
+// rows together in one narrow window (the x rows that neighbouring rows gather stay in
+// L2; a contiguous range per block would keep G distant windows alive and re-read x
+// from DRAM). Moment partials stay in registers and are reduced over the block and
+// added to the FP64 accumulator only when the tile's (system, batch) changes and at
+// the end.
+template<class V, int E, int LPR>
+__device__ __forceinline__ void diag_flush(typename Tr<V>::R (&m2)[E], typename Tr<V>::R (&m3r)[E],
+                                           typename Tr<V>::R (&m3i)[E], typename Tr<V>::R* red, double* a) {
     using R = typename Tr<V>::R;
     constexpr bool CPLX = Tr<V>::C;
     constexpr int K = E * LPR;
-    constexpr int RPP = BLOCK / LPR;  // rows per pass of the block
     constexpr int NV = CPLX ? 3 : 2;
-    using P = Pack<V, E>;
-
-    Tile const t = tiles[blockIdx.x];
-    int const lane = threadIdx.x % LPR;
-    int const slot = threadIdx.x / LPR;
-    V const* __restrict__ x = x_all + t.batch * batch_stride;
-    V* __restrict__ y = y_all + t.batch * batch_stride;
-    int const row_end = min(t.row_end, row_limit);
-
-    R m2[E], m3r[E], m3i[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
-
-    constexpr int VS = Tr<V>::VS;
-    for (int r = t.row_begin + slot; r < row_end; r += RPP) {
-        V sum[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) vzero(sum[e]);
-        int32_t const* cp = col + static_cast<int64_t>(r) * W;
-        V const* vp = val + static_cast<int64_t>(r) * W * VS;
-        for (int j = 0; j < W; ++j) {
-            int32_t const c = __ldg(cp + j);
-            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
-            V const a = vp[j * VS];
-#pragma unroll
-            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
-            if (VS == 2) {
-                V const lo = vp[j * VS + 1];
-#pragma unroll
-                for (int e = 0; e < E; ++e) vfma(sum[e], lo, xv.v[e]);
-            }
-        }
-        P const xr = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane);
-        P* yp = reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane;
-        P yn;
-        if (INIT) {
-#pragma unroll
-            for (int e = 0; e < E; ++e) yn.v[e] = vhalf(sum[e]);
-        } else {
-            P const yo = ld_stream(yp);
-#pragma unroll
-            for (int e = 0; e < E; ++e) yn.v[e] = vsub(sum[e], yo.v[e]);
-        }
-        st_stream(yp, yn);
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            m2[e] += vsq(xr.v[e]);
-            m3r[e] += vdre(yn.v[e], xr.v[e]);
-            if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
-        }
-    }
-
-    // reduce over the rows of the block: lanes with equal (threadIdx % LPR) hold the same vectors
 #pragma unroll
     for (int off = LPR; off < 32; off <<= 1) {
 #pragma unroll
@@ -192,25 +218,76 @@ diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
             if (CPLX) m3i[e] += __shfl_xor_sync(0xffffffffu, m3i[e], off);
         }
     }
-    __shared__ R red[WARPS][K][NV];
     int const warp = threadIdx.x / 32;
     int const wl = threadIdx.x % 32;
+    __syncthreads();  // the previous flush has finished reading `red`
     if (wl < LPR) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            red[warp][wl * E + e][0] = m2[e];
-            red[warp][wl * E + e][1] = m3r[e];
-            if (CPLX) red[warp][wl * E + e][NV - 1] = m3i[e];
+            R* rw = red + (warp * K + wl * E + e) * NV;
+            rw[0] = m2[e];
+            rw[1] = m3r[e];
+            if (CPLX) rw[NV - 1] = m3i[e];
         }
     }
     __syncthreads();
-    double* a = acc + static_cast<int64_t>(t.system * nbatch + t.batch) * K * NV;
     for (int i = threadIdx.x; i < K * NV; i += BLOCK) {
-        R s = R(0);
+        R sum = R(0);
 #pragma unroll
-        for (int w = 0; w < WARPS; ++w) s += red[w][i / NV][i % NV];
-        atomicAdd(a + i, static_cast<double>(s));
+        for (int w = 0; w < WARPS; ++w) sum += red[w * K * NV + i];
+        atomicAdd(a + i, static_cast<double>(sum));
     }
+#pragma unroll
+    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+}
+
+template<class V, int E, int LPR, bool INIT, int U>
+__global__ void __launch_bounds__(BLOCK)
+diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
+                 V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+                 Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
+                 double* __restrict__ acc) {
+    using R = typename Tr<V>::R;
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;  // rows per pass of the block
+    constexpr int NV = CPLX ? 3 : 2;
+    __shared__ R red[WARPS * K * NV];
+
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    int const G = gridDim.x;
+
+    R m2[E], m3r[E], m3i[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+    int cur_sys = -1, cur_batch = -1;
+
+    for (int ti = blockIdx.x; ti < num_tiles; ti += G) {
+        Tile const t = tiles[ti];
+        if (t.system != cur_sys || t.batch != cur_batch) {
+            if (cur_sys >= 0)
+                diag_flush<V, E, LPR>(m2, m3r, m3i, red,
+                                      acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+            cur_sys = t.system;
+            cur_batch = t.batch;
+        }
+        V const* __restrict__ x = x_all + t.batch * batch_stride;
+        V* __restrict__ y = y_all + t.batch * batch_stride;
+        int const row_end = min(t.row_end, row_limit);
+        for (int r = t.row_begin + slot; r < row_end; r += RPP * U) {
+            int rr[U];
+            bool live[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                rr[u] = r + u * RPP;
+                live[u] = rr[u] < row_end;
+            }
+            diag_rows<V, E, LPR, INIT, U>(col, val, W, x, y, rr, live, lane, m2, m3r, m3i);
+        }
+    }
+    if (cur_sys >= 0)
+        diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
 }
 
 // ------------------------------------------------------------------ off-diagonal step
@@ -512,19 +589,55 @@ __global__ void kubo_integrate_kernel(double const* __restrict__ sum_nm, double 
     out[2 * j + 1] = prefix * coeff * ti;
 }
 
-template<class V, int E, int LPR>
-cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
-    if (a.num_tiles == 0) return cudaSuccess;
+int persistent_grid(void const* fn, int num_tiles) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    // occupancy per kernel, queried once (the recursion launches the same kernels thousands of times)
+    static void const* fns[64];
+    static int occ[64];
+    static int nfns = 0;
+    int per_sm = 0;
+    for (int i = 0; i < nfns; ++i)
+        if (fns[i] == fn) per_sm = occ[i];
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BLOCK, 0) != cudaSuccess || per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+        if (nfns < 64) { fns[nfns] = fn; occ[nfns] = per_sm; ++nfns; }
+    }
+    return std::max(1, std::min(num_tiles, sms * per_sm));
+}
+
+template<class V, int E, int LPR, int U>
+cudaError_t diag_launch_u(DiagStep const& a, cudaStream_t s) {
     auto const* val = static_cast<V const*>(a.val);
     auto const* x = static_cast<V const*>(a.x);
     auto* y = static_cast<V*>(a.y);
-    if (a.init)
-        diag_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride,
-                                                                        a.tiles, a.row_limit, a.nbatch, a.acc);
-    else
-        diag_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride,
-                                                                         a.tiles, a.row_limit, a.nbatch, a.acc);
+    if (a.init) {
+        auto fn = diag_step_kernel<V, E, LPR, true, U>;
+        int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
+        fn<<<g, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit, a.nbatch,
+                               a.acc);
+    } else {
+        auto fn = diag_step_kernel<V, E, LPR, false, U>;
+        int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
+        fn<<<g, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit, a.nbatch,
+                               a.acc);
+    }
     return cudaGetLastError();
+}
+
+template<class V, int E, int LPR>
+cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2>(a, s);
+    return diag_launch_u<V, E, LPR, 1>(a, s);
 }
 
 template<class V, int E, int LPR>
