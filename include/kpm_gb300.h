@@ -206,6 +206,33 @@ int kpm_optimized_hamiltonian(kpm_engine* engine, const int32_t* src, int64_t n_
  * counterpart (the reference has no device). Initialises the device. */
 int kpm_get_stream(kpm_engine* engine, void** stream);
 
+/*
+ * Diagonal moments for callers that cannot allocate device memory. It has no
+ * counterpart in the reference. cudaMalloc/cudaFree can synchronize the device,
+ * and frameworks that own all device memory (their own pool, a fixed budget)
+ * cannot accept allocations made behind their back; this call makes none.
+ * The caller passes device buffers for everything: the scaled matrix H~ as
+ * padded row-major ELL (col [rows][width] int32, val [rows][width][vs] of
+ * vector_type, vs = 2 for KPM_F32/KPM_C64 -- each value as its FP32 high and
+ * low parts -- and vs = 1 for KPM_F64/KPM_C128), the starters r0 [rows][K]
+ * (K = num_vectors, interleaved per row; overwritten), a second vector buffer
+ * r1 of the same size (overwritten), and out [K][num_moments] complex double.
+ * num_vectors is 1 or a block of 32..512 bytes per row. The recursion's
+ * scratch (tile list + per-step FP64 moment sums) is a fixed 4 MiB device
+ * array inside this library, held by every GPU that loads it until the
+ * process exits: calls needing more (about 16 bytes per 1024/K rows plus
+ * num_moments/2 * K * 2 (real) or 3 (complex) doubles) are rejected with
+ * KPM_ERR_VALUE and a message. The first call on each device looks up that
+ * array's device address with the device current; make that first call
+ * before any stream capture. Every call shares the array, so calls that
+ * overlap on the GPU race; the call clears what must start at zero. Work is
+ * queued on `stream` (a cudaStream_t; NULL = default stream) and the call
+ * returns without waiting for it.
+ */
+int kpm_moments_diag_noalloc(int32_t vector_type, int64_t rows, int32_t width, const int32_t* col,
+                             const void* val, int64_t num_vectors, void* r0, void* r1, int64_t num_moments,
+                             double* out, void* stream);
+
 /* Damping coefficients g_n of a kernel (kpm/Kernel.cpp:6-50). */
 int kpm_damping_coefficients(int32_t kernel, double kernel_param, int64_t num_moments, double* out);
 

@@ -61,6 +61,7 @@ SIGNATURES = {
     "kpm_report": (_I32, [_P, _I32, _P, _I64]),
     "kpm_optimized_hamiltonian": (_I32, [_P, _P, _I64, _P, _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "kpm_get_stream": (_I32, [_P, _P]),
+    "kpm_moments_diag_noalloc": (_I32, [_I32, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P, _P]),
     "kpm_damping_coefficients": (_I32, [_I32, _D, _I64, _P]),
     "kpm_required_num_moments": (_I64, [_I32, _D, _D]),
 }

@@ -914,6 +914,10 @@ struct kpm_engine {
     }
 };
 
+namespace kpm {
+void set_last_error(std::string const& msg) { g_last_error = msg; }
+}  // namespace kpm
+
 // ====================================================================== C ABI
 extern "C" {
 

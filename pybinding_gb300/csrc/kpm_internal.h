@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <string>
 
 namespace kpm {
 
@@ -144,5 +145,8 @@ cudaError_t launch_spectral_density(double const* mu, int64_t M, int cols, doubl
 // Green's: out[c * ne + e] = -2i/(a sqrt(1-E^2)) sum_n mu[c*M+n] exp(-i n acos E) (complex)
 cudaError_t launch_greens(double const* mu, int64_t M, int cols, double const* energy, int ne, double a,
                           double b, double* out, cudaStream_t s);
+
+// Record the message that kpm_last_error() returns on this thread.
+void set_last_error(std::string const& msg);
 
 }  // namespace kpm
