@@ -256,12 +256,14 @@ def run_gpu(args, rank, world, local_rank):
 
     # dominant kernel: the recursion step, timed by the engine's events on its own stream
     rec = float(np.median(rec_times))
-    launches = M // 2  # init + M/2 - 1 steps
+    fuse = int(eng.stats().steps_per_launch)
+    launches = 1 + (M // 2 - 1) // fuse  # init + recursion launches
     avg_launch = rec / launches
     nrows = rows
-    vec_bytes = 3 * nrows * R * 4
-    # per step: matrix once (FP32 hi/lo value pair + int32 column per non-zero, row extents),
-    # x read once, y_old read once, y_new written once
+    # per launch: matrix once (FP32 hi/lo value pair + int32 column per non-zero, row extents);
+    # one step reads x and y_old and writes y_new (3 vector passes), a fused two-step launch
+    # reads P and Q and writes both (4 vector passes for 2 steps)
+    vec_bytes = (3 if fuse == 1 else 4) * nrows * R * 4
     alg_bytes = nnz * (8 + 4) + 4 * (nrows + 1) + vec_bytes
     achieved = alg_bytes / avg_launch / 1e9
     peaks = {}
@@ -273,7 +275,8 @@ def run_gpu(args, rank, world, local_rank):
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "diag_step_traffic.json")))
-        traffic = prof.get("dram_bytes_per_launch_scaled_to_bench")
+        if prof.get("steps_per_launch", 1) == fuse:
+            traffic = prof.get("dram_bytes_per_launch_scaled_to_bench")
     except (OSError, ValueError):
         pass
 
@@ -330,7 +333,8 @@ def run_gpu(args, rank, world, local_rank):
                "moment_error_vs_fp64": err,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
-                            "kernel": "diag_step_kernel<float,4,16>", "alg_bytes_per_launch": alg_bytes,
+                            "kernel": "diag_step_kernel<float,4,16>" if fuse == 1 else "diag_pair_kernel<float,4,16>",
+                            "steps_per_launch": fuse, "alg_bytes_per_launch": alg_bytes,
                             "avg_launch_ms": avg_launch * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
                "cpu_baseline": {"value": cpu["value"], "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": cpu["sample"]},

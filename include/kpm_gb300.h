@@ -64,6 +64,7 @@ typedef struct kpm_config {
     int32_t precision;        /* KPM_PREC_* */
     int32_t batch_width;      /* vectors per recursion block (upper bound); 0 = 256-byte rows */
     int32_t tile_rows;        /* rows per thread block tile; 0 = autotuned on the first call */
+    int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, or 0 = chosen by timing */
 } kpm_config;
 
 /* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */
@@ -82,6 +83,7 @@ typedef struct kpm_stats {
     double bounds_time;       /* seconds: Lanczos */
     int32_t lanczos_loops;
     double eps;               /* opt_nnz * multiplier / moments_time */
+    int32_t steps_per_launch; /* Chebyshev steps per recursion launch used last (1 or 2) */
 } kpm_stats;
 
 typedef struct kpm_engine kpm_engine;

@@ -29,7 +29,7 @@ class Config(C.Structure):
     _fields_ = [("min_energy", C.c_double), ("max_energy", C.c_double), ("kernel", C.c_int32),
                 ("kernel_param", C.c_double), ("matrix_format", C.c_int32), ("optimal_size", C.c_int32),
                 ("interleaved", C.c_int32), ("lanczos_precision", C.c_double), ("precision", C.c_int32),
-                ("batch_width", C.c_int32), ("tile_rows", C.c_int32)]
+                ("batch_width", C.c_int32), ("tile_rows", C.c_int32), ("fuse_steps", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -38,7 +38,7 @@ class Stats(C.Structure):
                 ("opt_nnz", C.c_int64), ("vec", C.c_int64), ("opt_vec", C.c_int64), ("multiplier", C.c_double),
                 ("matrix_memory", C.c_int64), ("vector_memory", C.c_int64), ("hamiltonian_time", C.c_double),
                 ("moments_time", C.c_double), ("bounds_time", C.c_double), ("lanczos_loops", C.c_int32),
-                ("eps", C.c_double)]
+                ("eps", C.c_double), ("steps_per_launch", C.c_int32)]
 
 
 # every exported symbol of include/kpm_gb300.h with (restype, argtypes)
@@ -106,7 +106,7 @@ def check(rc):
 
 def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, matrix_format="ELL",
                 optimal_size=True, interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0,
-                tile_rows=0):
+                tile_rows=0, fuse_steps=0):
     c = Config()
     lib().kpm_config_default(C.byref(c))
     c.min_energy, c.max_energy = float(energy_range[0]), float(energy_range[1])
@@ -119,6 +119,7 @@ def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, mat
     c.precision = PRECISION_CODE[precision]
     c.batch_width = int(batch_width)
     c.tile_rows = int(tile_rows)
+    c.fuse_steps = int(fuse_steps)
     return c
 
 

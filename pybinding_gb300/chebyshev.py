@@ -338,7 +338,7 @@ class KPMBatch:
                     kernel_param=self.kernel.param)
         args.update({k: v for k, v in kwargs.items() if k in ("matrix_format", "optimal_size", "interleaved",
                                                               "lanczos_precision", "precision", "batch_width",
-                                                              "tile_rows")})
+                                                              "tile_rows", "fuse_steps")})
         self.engine = _native.Engine(h, _native.make_config(**args), system_offsets=self.offsets)
 
     def scaling_factors(self):

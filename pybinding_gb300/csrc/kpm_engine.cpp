@@ -298,6 +298,19 @@ struct kpm_engine {
 
     // recursion buffers
     DBuf d_x0, d_x1, d_acc, d_tiles, d_mu, d_mu_avg, d_stage, d_pos, d_gamma, d_energy, d_out;
+    std::vector<int32_t> h_col;  // host copy of the device ELL column indices
+
+    // two-steps-per-launch state: one partition per candidate tile height
+    struct PairPlan {
+        int rows_per_tile = 0;
+        int num_tiles = 0;
+        DBuf d_tiles, d_items, d_band, d_flags;
+    };
+    std::vector<std::unique_ptr<PairPlan>> pair_plans;
+    int pair_key_nbatch = -1, pair_key_lpr = -1;
+    int64_t pair_key_rows = -1;
+    int pair_seq = 0;
+    DBuf d_pair_counters, d_pair_error;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -308,6 +321,8 @@ struct kpm_engine {
     bool last_bounds_lanczos = false;
 
     ~kpm_engine() {
+        if (ev_t0) cudaEventDestroy(ev_t0);
+        if (ev_t1) cudaEventDestroy(ev_t1);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -328,6 +343,8 @@ struct kpm_engine {
         KPM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         KPM_CUDA(cudaEventCreate(&ev0));
         KPM_CUDA(cudaEventCreate(&ev1));
+        KPM_CUDA(cudaEventCreate(&ev_t0));
+        KPM_CUDA(cudaEventCreate(&ev_t1));
     }
 
     void set_h(int st_, int64_t n, int32_t const* ip, int32_t const* ix, void const* v, int ns, int64_t const* offs) {
@@ -637,6 +654,7 @@ struct kpm_engine {
                 }
                 for (; j < W; ++j) col[r * W + j] = static_cast<int32_t>(r);
             }
+            h_col = col;
             d_col.ensure(col.size() * sizeof(int32_t));
             d_val.ensure(val.size() * sizeof(Tc));
             KPM_CUDA(cudaMemcpyAsync(d_col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
@@ -663,6 +681,7 @@ struct kpm_engine {
         opt_src = src;
         opt_dest = dest;
         opt_valid = true;
+        pair_plans.clear();
         st.hamiltonian_time = now_s() - t0;
     }
 
@@ -708,6 +727,9 @@ struct kpm_engine {
         }
     };
     struct Tuned { int rows_per_tile, unroll; };
+    // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
+    struct FuseChoice { int steps, rows_per_tile; };
+    std::vector<std::pair<TuneKey, FuseChoice>> fuse_tuned;
     std::vector<std::pair<TuneKey, Tuned>> tuned;
     std::vector<std::array<double, 3>> last_tuning;  // (rows per tile, unroll, ms) of the last tuning run
 
@@ -742,6 +764,93 @@ struct kpm_engine {
         }
         tuned.push_back({key, best});
         return best;
+    }
+
+    // Partition for the two-step kernel: tiles of `tpr` rows (per system, per batch), the
+    // band of tiles each tile's rows touch (phase B of a tile waits for phase A of its band),
+    // and the work queue in which B_t follows A_{max band hi over tiles <= t}.
+    PairPlan* pair_plan(Shape const& sh, int tpr) {
+        if (pair_key_nbatch != sh.nbatch || pair_key_lpr != sh.LPR || pair_key_rows != rows) {
+            pair_plans.clear();
+            pair_key_nbatch = sh.nbatch;
+            pair_key_lpr = sh.LPR;
+            pair_key_rows = rows;
+        }
+        for (auto& pp : pair_plans)
+            if (pp->rows_per_tile == tpr) return pp.get();
+        auto pp = std::make_unique<PairPlan>();
+        pp->rows_per_tile = tpr;
+        std::vector<Tile> tiles;
+        std::vector<int64_t> base(nsys + 1, 0);  // row tiles before system s
+        for (int s = 0; s < nsys; ++s) base[s + 1] = base[s] + (sys_rows(s) + tpr - 1) / tpr;
+        // row-tile hull per row tile: tiles its rows read, widened by the tiles that read its rows
+        // (equal for a Hermitian pattern; both are covered so that any pattern is safe)
+        int64_t const RT = base[nsys];
+        std::vector<int64_t> lo(RT), hi(RT);
+        for (int64_t i = 0; i < RT; ++i) { lo[i] = i; hi[i] = i; }
+        for (int s = 0; s < nsys; ++s)
+            for (int64_t q = sys_off[s]; q < sys_off[s + 1]; ++q) {
+                int64_t const tq = base[s] + (q - sys_off[s]) / tpr;
+                for (int j = 0; j < W; ++j) {
+                    int64_t const c = h_col[static_cast<size_t>(q) * W + j];
+                    int64_t const tc = base[s] + (c - sys_off[s]) / tpr;
+                    lo[tq] = std::min(lo[tq], tc); hi[tq] = std::max(hi[tq], tc);
+                    lo[tc] = std::min(lo[tc], tq); hi[tc] = std::max(hi[tc], tq);
+                }
+            }
+        std::vector<int32_t> band;
+        for (int s = 0; s < nsys; ++s)
+            for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += tpr) {
+                int64_t const r1 = std::min(sys_off[s + 1], r + tpr);
+                int64_t const rt = base[s] + (r - sys_off[s]) / tpr;
+                for (int b = 0; b < sh.nbatch; ++b) {
+                    tiles.push_back({static_cast<int32_t>(r), static_cast<int32_t>(r1), s, b});
+                    band.push_back(static_cast<int32_t>(lo[rt] * sh.nbatch + b));
+                    band.push_back(static_cast<int32_t>(hi[rt] * sh.nbatch + b));
+                }
+            }
+        int const T = static_cast<int>(tiles.size());
+        std::vector<int32_t> items;
+        items.reserve(2 * T);
+        // B_t is queued `lag` phase-A items after the last A it needs, so that those are
+        // usually finished when B_t is handed out (about the number of blocks in flight)
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int32_t const lag = 2 * sms;
+        int32_t hstar = -1;
+        std::vector<int32_t> hs(T);
+        for (int t = 0; t < T; ++t) {
+            hstar = std::max(hstar, band[2 * t + 1]);
+            hs[t] = std::min<int32_t>(T - 1, hstar + lag);
+        }
+        int pb = 0;
+        for (int k = 0; k < T; ++k) {
+            items.push_back(2 * k);
+            while (pb < T && hs[pb] <= k) items.push_back(2 * pb++ + 1);
+        }
+        while (pb < T) items.push_back(2 * pb++ + 1);
+        pp->num_tiles = T;
+        pp->d_tiles.ensure(sizeof(Tile) * T);
+        pp->d_items.ensure(sizeof(int32_t) * 2 * T);
+        pp->d_band.ensure(sizeof(int32_t) * 2 * T);
+        pp->d_flags.ensure(sizeof(int32_t) * T);
+        KPM_CUDA(cudaMemcpyAsync(pp->d_tiles.p, tiles.data(), sizeof(Tile) * T, cudaMemcpyHostToDevice, stream));
+        KPM_CUDA(cudaMemcpyAsync(pp->d_items.p, items.data(), sizeof(int32_t) * 2 * T, cudaMemcpyHostToDevice, stream));
+        KPM_CUDA(cudaMemcpyAsync(pp->d_band.p, band.data(), sizeof(int32_t) * 2 * T, cudaMemcpyHostToDevice, stream));
+        KPM_CUDA(cudaMemsetAsync(pp->d_flags.p, 0, sizeof(int32_t) * T, stream));
+        KPM_CUDA(cudaStreamSynchronize(stream));
+        pair_plans.push_back(std::move(pp));
+        return pair_plans.back().get();
+    }
+
+    int next_seq() {
+        if (pair_seq >= (1 << 30)) {  // restart the sequence: clear every plan's flags
+            for (auto& pp : pair_plans)
+                KPM_CUDA(cudaMemsetAsync(pp->d_flags.p, 0, sizeof(int32_t) * pp->num_tiles, stream));
+            pair_seq = 0;
+        }
+        return ++pair_seq;
     }
 
     int build_tiles(Shape const& sh, bool sys0_only) {
@@ -833,7 +942,8 @@ struct kpm_engine {
         a.init = false;
         void* r0 = d_x0.p;
         void* r1 = d_x1.p;
-        for (int64_t n = 2; n <= half; ++n) {
+        int64_t n = 2;
+        auto single_step = [&]() {
             a.x = r1;
             a.y = r0;
             a.acc = d_acc.as<double>() + step_acc * (n - 1);
@@ -846,11 +956,91 @@ struct kpm_engine {
             }
             KPM_CUDA(kpm::launch_diag_step(a, stream));
             std::swap(r0, r1);
+            ++n;
+        };
+        // two steps per launch: P = r0 (T_{n-2} -> T_n), Q = r1 (T_{n-1} -> T_{n+1}); the
+        // roles are unchanged after the pair, so no swap
+        d_pair_error.ensure(sizeof(int));
+        KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
+        int64_t const max_pairs = std::max<int64_t>(1, half / 2);
+        d_pair_counters.ensure(sizeof(unsigned) * max_pairs);
+        KPM_CUDA(cudaMemsetAsync(d_pair_counters.p, 0, sizeof(unsigned) * max_pairs, stream));
+        int64_t pair_index = 0;
+        auto pair_step = [&](PairPlan* pp) {
+            kpm::DiagPair q{};
+            q.vtype = vtype;
+            q.E = sh.E;
+            q.LPR = sh.LPR;
+            q.col = d_col.as<int32_t>();
+            q.val = d_val.p;
+            q.W = W;
+            q.P = r0;
+            q.Q = r1;
+            q.batch_stride = bstride;
+            q.tiles = pp->d_tiles.as<Tile>();
+            q.items = pp->d_items.as<int32_t>();
+            q.band = pp->d_band.as<int32_t>();
+            q.num_tiles = pp->num_tiles;
+            q.nbatch = sh.nbatch;
+            q.flags = pp->d_flags.as<int>();
+            q.seq = next_seq();
+            q.counter = d_pair_counters.as<unsigned>() + pair_index++;
+            q.accA = d_acc.as<double>() + step_acc * (n - 1);
+            q.accB = d_acc.as<double>() + step_acc * n;
+            q.error = d_pair_error.as<int>();
+            q.spin_limit = 1 << 24;  // x ~64 ns sleeps: gives up after about a second
+            KPM_CUDA(kpm::launch_diag_pair(q, stream));
+            n += 2;
+        };
+        int const rpp = 256 / sh.LPR;
+        bool const can_pair = !opt_rows && cfg.fuse_steps != 1;
+        FuseChoice choice{1, 0};
+        TuneKey const fkey{vtype, sh.E, sh.LPR, sh.nbatch, rows};
+        bool have_choice = false;
+        for (auto const& f : fuse_tuned)
+            if (f.first == fkey) { choice = f.second; have_choice = true; }
+        if (can_pair && cfg.fuse_steps == 2 && !have_choice) {
+            choice = FuseChoice{2, cfg.tile_rows > 0 ? cfg.tile_rows : rpp * 8};
+            have_choice = true;
         }
+        if (can_pair && !have_choice) {
+            // time each candidate on the first steps of this recursion (any partition gives the
+            // same result), then keep the fastest per two steps
+            std::vector<FuseChoice> cands{{1, 0}};
+            for (int rpt : {4, 8, 16, 32}) cands.push_back({2, rpp * rpt});
+            double best = 1e30;
+            if (half - 1 >= 2 * static_cast<int64_t>(cands.size()) + 2) {
+                for (auto const& c : cands) {
+                    PairPlan* pp = c.steps == 2 ? pair_plan(sh, c.rows_per_tile) : nullptr;
+                    KPM_CUDA(cudaEventRecord(ev_t0, stream));
+                    if (pp) pair_step(pp); else { single_step(); single_step(); }
+                    KPM_CUDA(cudaEventRecord(ev_t1, stream));
+                    KPM_CUDA(cudaEventSynchronize(ev_t1));
+                    float ms = 0;
+                    KPM_CUDA(cudaEventElapsedTime(&ms, ev_t0, ev_t1));
+                    if (ms < best) { best = ms; choice = c; }
+                }
+                fuse_tuned.push_back({fkey, choice});
+            } else {
+                choice = FuseChoice{1, 0};
+            }
+        }
+        if (cfg.fuse_steps == 2 && can_pair && choice.steps != 2)
+            choice = FuseChoice{2, cfg.tile_rows > 0 ? cfg.tile_rows : rpp * 8};
+        if (choice.steps == 2 && can_pair) {
+            PairPlan* pp = pair_plan(sh, choice.rows_per_tile);
+            while (n + 1 <= half) pair_step(pp);
+        }
+        while (n <= half) single_step();
+        last_fuse = choice.steps;
         KPM_CUDA(cudaEventRecord(ev1, stream));
         KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
                                           d_mu.as<double>(), stream));
+        int pair_err = 0;
+        KPM_CUDA(cudaMemcpyAsync(&pair_err, d_pair_error.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         KPM_CUDA(cudaStreamSynchronize(stream));
+        if (pair_err)
+            fail(KPM_ERR_TIMEOUT, "a two-step recursion launch gave up waiting for a neighbouring tile; results discarded");
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         st.moments_time = ms * 1e-3;
@@ -858,6 +1048,8 @@ struct kpm_engine {
     }
     Shape last_shape{};
     double last_gemm_time = 0;
+    int last_fuse = 1;
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
 
     void reset_stats(int64_t M, bool diagonal, bool opt, double multiplier, int64_t active_rows_nnz_rows) {
         (void)active_rows_nnz_rows;
@@ -884,7 +1076,10 @@ struct kpm_engine {
         st.matrix_memory = static_cast<int64_t>(rows) * W * (kpm::vtype_vs(vtype) * kpm::vtype_bytes(vtype) + 4);
         st.vector_memory = static_cast<int64_t>(rows) * kpm::vtype_bytes(vtype);
     }
-    void finish_stats() { st.eps = st.moments_time > 0 ? st.multiplier * st.opt_nnz / st.moments_time : 0.0; }
+    void finish_stats() {
+        st.eps = st.moments_time > 0 ? st.multiplier * st.opt_nnz / st.moments_time : 0.0;
+        st.steps_per_launch = last_fuse;
+    }
 
     // ---------------------------------------------------------------- reconstruction
     void spectral(double const* d_moments_cd, int64_t M, int cols, double const* energy, int64_t ne, ScaleAB sc,
@@ -936,6 +1131,7 @@ void kpm_config_default(kpm_config* c) {
     c->precision = KPM_PREC_AUTO;
     c->batch_width = 0;
     c->tile_rows = 0;
+    c->fuse_steps = 0;
 }
 
 int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const int32_t* indices, const void* values,
@@ -954,6 +1150,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
+        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
         *out = e.release();
     });

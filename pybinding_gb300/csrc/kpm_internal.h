@@ -84,7 +84,36 @@ struct DenseStep {
     bool init;
 };
 
+// Two recursion steps in one launch (steps n and n+1; P = T_{n-2} -> T_n, Q = T_{n-1} -> T_{n+1}).
+// items: [2 * num_tiles] work items (tile * 2 + phase) in dependency order; band: [num_tiles][2]
+// tile range whose phase A must finish before phase B of the tile; flags: [num_tiles] sequence
+// number of the last finished phase A (persist across launches; seq grows per launch);
+// counter: item dispenser of this launch, zeroed beforehand.
+struct DiagPair {
+    int vtype;
+    int E, LPR;
+    const int32_t* col;
+    const void* val;
+    int W;
+    void* P;
+    void* Q;
+    int64_t batch_stride;
+    const Tile* tiles;
+    const int32_t* items;
+    const int32_t* band;
+    int num_tiles;
+    int nbatch;
+    int* flags;
+    int seq;
+    unsigned* counter;
+    double* accA;
+    double* accB;
+    int* error;
+    int spin_limit;
+};
+
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s);
+cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s);
 cudaError_t launch_dense_step(DenseStep const& a, cudaStream_t s);
 
 // mu[n * M + m] += sum_i A[m * I + i] * conj(B[n * I + i]) in FP64 (complex double mu),

@@ -108,6 +108,14 @@ __device__ __forceinline__ P ld_ro(P const* p) {  // read-only path (L1 cached):
     return r;
 }
 template<class P>
+__device__ __forceinline__ P ld_l2(P const* p) {  // coherent at L2 (bypasses L1): data written in this launch
+    using T = typename Raw<sizeof(P)>::T;
+    T t = __ldcg(reinterpret_cast<T const*>(p));
+    P r;
+    memcpy(&r, &t, sizeof(P));
+    return r;
+}
+template<class P>
 __device__ __forceinline__ P ld_stream(P const* p) {  // streamed once: y_old
     using T = typename Raw<sizeof(P)>::T;
     T t = __ldcs(reinterpret_cast<T const*>(p));
@@ -128,7 +136,7 @@ __device__ __forceinline__ void st_stream(P* p, P const& v) {
 // in chunks of 4 with every load of a chunk issued before its first use, so a row
 // costs two dependent memory round trips (indices, then gathers) rather than one
 // per entry; x[r] and y_old[r] are issued ahead of the index loads.
-template<class V, int E, int LPR, bool INIT, int U>
+template<class V, int E, int LPR, bool INIT, int U, bool XCOH = false>
 __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
                                           V const* __restrict__ x, V* __restrict__ y, int const (&rr)[U],
                                           bool const (&live)[U], int lane, typename Tr<V>::R (&m2)[E],
@@ -142,7 +150,8 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, V con
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         if (!live[u]) continue;
-        xr[u] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(rr[u]) * K) + lane);
+        P const* xp = reinterpret_cast<P const*>(x + static_cast<int64_t>(rr[u]) * K) + lane;
+        xr[u] = XCOH ? ld_l2(xp) : ld_ro(xp);
         if (!INIT) yo[u] = ld_stream(reinterpret_cast<P const*>(y + static_cast<int64_t>(rr[u]) * K) + lane);
 #pragma unroll
         for (int e = 0; e < E; ++e) { vzero(sum[u][e]); vzero(lo[u][e]); }
@@ -159,8 +168,10 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, V con
         for (int u = 0; u < U; ++u)
 #pragma unroll
             for (int q = 0; q < 4; ++q)
-                if (live[u] && j0 + q < W)
-                    xv[u][q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[u][q]) * K) + lane);
+                if (live[u] && j0 + q < W) {
+                    P const* xp = reinterpret_cast<P const*>(x + static_cast<int64_t>(c[u][q]) * K) + lane;
+                    xv[u][q] = XCOH ? ld_l2(xp) : ld_ro(xp);
+                }
 #pragma unroll
         for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -633,6 +644,134 @@ cudaError_t diag_launch_u(DiagStep const& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+
+// ------------------------------------------------------------------ two steps per launch
+// Phase A of tile t computes T_n on its rows (x = Q = T_{n-1}, y = P = T_{n-2} -> T_n);
+// phase B computes T_{n+1} (x = P = T_n, y = Q = T_{n-1} -> T_{n+1}). Phase B of t reads
+// T_n on every row its rows touch and overwrites Q rows that phase A of those tiles
+// gathers, so it waits until phase A of tiles band[t] = [lo, hi] is done. Work items
+// come from a queue in which B_t follows A_hi, dispensed by an atomic counter to blocks
+// that start on them at once: a waiting block only waits on phase-A items already being
+// processed by running blocks, and phase A never waits. Waits give up after a bounded
+// number of polls and raise *error (the host reports a timeout).
+__device__ __forceinline__ int ld_acquire(int const* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+template<class V, int E, int LPR>
+__global__ void __launch_bounds__(BLOCK, 4)
+diag_pair_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V* __restrict__ P_all,
+                 V* __restrict__ Q_all, int64_t batch_stride, Tile const* __restrict__ tiles,
+                 int32_t const* __restrict__ items, int32_t const* __restrict__ band, int num_tiles, int nbatch,
+                 int* __restrict__ flags, int seq, unsigned* __restrict__ counter, double* __restrict__ accA,
+                 double* __restrict__ accB, int* __restrict__ error, int spin_limit) {
+    using R = typename Tr<V>::R;
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;
+    constexpr int NV = CPLX ? 3 : 2;
+    __shared__ R red[WARPS * K * NV];
+    __shared__ int s_item[2];
+    __shared__ int s_ok;
+
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    int const total = 2 * num_tiles;
+    R aA2[E], aA3r[E], aA3i[E], aB2[E], aB3r[E], aB3i[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        aA2[e] = R(0); aA3r[e] = R(0); aA3i[e] = R(0);
+        aB2[e] = R(0); aB3r[e] = R(0); aB3i[e] = R(0);
+    }
+    int curA_sys = -1, curA_b = -1, curB_sys = -1, curB_b = -1;
+    for (int iter = 0;; ++iter) {
+        int const buf = iter & 1;
+        // A ticket is taken only when the block is free to work on it: an item held in
+        // reserve by a busy block would delay every B item that waits on it.
+        if (threadIdx.x == 0) {
+            unsigned const ticket = atomicAdd(counter, 1u);
+            s_item[buf] = ticket < static_cast<unsigned>(total) ? items[ticket] : -1;
+        }
+        __syncthreads();
+        int const item = s_item[buf];
+        if (item < 0) break;
+        int const t = item >> 1;
+        Tile const tl = tiles[t];
+        V* P = P_all + tl.batch * batch_stride;
+        V* Q = Q_all + tl.batch * batch_stride;
+        if ((item & 1) == 0) {  // phase A
+            if (tl.system != curA_sys || tl.batch != curA_b) {
+                if (curA_sys >= 0)
+                    diag_flush<V, E, LPR>(aA2, aA3r, aA3i, red,
+                                          accA + static_cast<int64_t>(curA_sys * nbatch + curA_b) * K * NV);
+                curA_sys = tl.system;
+                curA_b = tl.batch;
+            }
+            for (int r = tl.row_begin + slot; r < tl.row_end; r += RPP) {
+                int rr[1] = {r};
+                bool live[1] = {true};
+                diag_rows<V, E, LPR, false, 1, false>(col, val, W, Q, P, rr, live, lane, aA2, aA3r, aA3i);
+            }
+            __syncthreads();  // every row of the tile is stored
+            if (threadIdx.x == 0) {
+                __threadfence();
+                st_release(flags + t, seq);
+            }
+        } else {  // phase B
+            if (threadIdx.x < 32) {
+                int const lo = band[2 * t], hi = band[2 * t + 1];
+                bool ok = true;
+                for (int u = lo + static_cast<int>(threadIdx.x); u <= hi && ok; u += 32) {
+                    int polls = 0;
+                    while (ld_acquire(flags + u) < seq) {
+                        if (++polls > spin_limit) { ok = false; break; }
+                        __nanosleep(64);
+                    }
+                }
+                ok = __all_sync(0xffffffffu, ok);
+                if (threadIdx.x == 0) s_ok = ok ? 1 : 0;
+            }
+            __syncthreads();
+            if (!s_ok) {
+                if (threadIdx.x == 0) atomicExch(error, 1);
+                continue;
+            }
+            if (tl.system != curB_sys || tl.batch != curB_b) {
+                if (curB_sys >= 0)
+                    diag_flush<V, E, LPR>(aB2, aB3r, aB3i, red,
+                                          accB + static_cast<int64_t>(curB_sys * nbatch + curB_b) * K * NV);
+                curB_sys = tl.system;
+                curB_b = tl.batch;
+            }
+            for (int r = tl.row_begin + slot; r < tl.row_end; r += RPP) {
+                int rr[1] = {r};
+                bool live[1] = {true};
+                diag_rows<V, E, LPR, false, 1, true>(col, val, W, P, Q, rr, live, lane, aB2, aB3r, aB3i);
+            }
+        }
+    }
+    if (curA_sys >= 0)
+        diag_flush<V, E, LPR>(aA2, aA3r, aA3i, red, accA + static_cast<int64_t>(curA_sys * nbatch + curA_b) * K * NV);
+    if (curB_sys >= 0)
+        diag_flush<V, E, LPR>(aB2, aB3r, aB3i, red, accB + static_cast<int64_t>(curB_sys * nbatch + curB_b) * K * NV);
+}
+
+template<class V, int E, int LPR>
+cudaError_t pair_launch(DiagPair const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    auto fn = diag_pair_kernel<V, E, LPR>;
+    int const g = persistent_grid(reinterpret_cast<void const*>(fn), 2 * a.num_tiles);
+    fn<<<g, BLOCK, 0, s>>>(a.col, static_cast<V const*>(a.val), a.W, static_cast<V*>(a.P), static_cast<V*>(a.Q),
+                           a.batch_stride, a.tiles, a.items, a.band, a.num_tiles, a.nbatch, a.flags, a.seq,
+                           a.counter, a.accA, a.accB, a.error, a.spin_limit);
+    return cudaGetLastError();
+}
+
 template<class V, int E, int LPR>
 cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
@@ -925,6 +1064,13 @@ bool diag_shape_supported(int vtype, int E, int LPR) {
     KPM_SHAPES_F32(KPM_CHECK) KPM_SHAPES_F64(KPM_CHECK) KPM_SHAPES_C64(KPM_CHECK) KPM_SHAPES_C128(KPM_CHECK)
 #undef KPM_CHECK
     return false;
+}
+
+cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s) {
+#define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return pair_launch<V, e, l>(a, s);
+    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
+#undef KPM_DISPATCH
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s) {

@@ -255,3 +255,29 @@ def test_conductivity_fp64_equals_oracle(oracle):
         err = rel_err(got, ref)
         print("conductivity fp64 vs oracle: %.3e" % err)
         assert err < 1e-9
+
+
+@pytest.mark.parametrize("fuse", [1, 2])
+@pytest.mark.parametrize("dtype,nvec,tol", [(np.float32, 64, 1e-5), (np.float64, 8, 1e-10),
+                                            (np.complex128, 8, 1e-10), (np.complex64, 4, 1e-5)])
+def test_one_and_two_steps_per_launch(oracle, fuse, dtype, nvec, tol):
+    """Single-step and fused two-step launches both match the FP64 oracle (ragged batch of 2 flakes)."""
+    hs = [_disordered_flake(n, s, np.float64) for n, s in ((20000, 8), (9000, 9))]
+    if np.iscomplexobj(np.zeros(1, dtype)):
+        hs = [(h + 1j * sp.triu(h, 1) * 0.1 - 1j * sp.tril(h, -1) * 0.1).tocsr() for h in hs]
+    hs = [h.astype(dtype) for h in hs]
+    rng = (-9.5, 9.5)
+    M = 258
+    a, b = oracle.scale(*rng)
+    starters = [oracle.random_starters(h.shape[0], nvec, dtype) for h in hs]
+    batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, fuse_steps=fuse)
+    moms = batch.engine.moments_diag(M, np.concatenate([st.ravel() for st in starters]))
+    assert batch.engine.stats().num_moments == M
+    for s, h in enumerate(hs):
+        h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
+        r = oracle.optimize(h64, [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(h64.dtype), r["reorder_map"]), M,
+                                  slices=r["slices"])
+        err = rel_err(moms[s], ref)
+        print("fuse=%d %s nvec=%d system %d: %.3e" % (fuse, np.dtype(dtype).name, nvec, s, err))
+        assert err <= tol
