@@ -175,7 +175,11 @@ int kpm_moments(kpm_engine* engine, int64_t num_moments, const double* alpha, in
 
 /* Kubo-Bastin conductivity (system 0): kpm::Core::conductivity (Core.cpp:119-150).
  * left/right: float32 site coordinates of the two directions (KPM.cpp:131-149).
- * gemm_mode: 0 = FP64 moments matrix, 1 = split-bf16 tensor-core GEMM.
+ * gemm_mode: 0 = moments matrix mu_mn = sum L_m conj(R_n) in FP64 on the CUDA cores;
+ *            1 = on the tensor cores (tcgen05 kind::tf32, every FP32 operand split into
+ *                tf32 hi + lo, three products per pair, FP64 sums across slices): the
+ *                collected vectors are stored as FP32 planes, which halves their memory
+ *                for complex128; mu agrees with mode 0 to ~1e-6 relative.
  * out: num_mu complex (the caller takes the real part). */
 int kpm_calc_conductivity(kpm_engine* engine, const float* left_coords, const float* right_coords,
                           const double* chemical_potential, int64_t num_mu, double broadening,

@@ -116,8 +116,12 @@ class GpuImpl:
     """The ``impl`` object of :class:`KPM`: ``_cpp.KPM`` semantics on the CUDA engine."""
 
     def __init__(self, model, energy_range=(0, 0), kernel=None, matrix_format="ELL", optimal_size=True,
-                 interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0, tile_rows=0, **_):
+                 interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0, tile_rows=0,
+                 moments_gemm="fp64", **_):
+        if moments_gemm not in ("fp64", "tensor"):
+            raise ValueError("moments_gemm must be 'fp64' or 'tensor'")
         self.kernel = kernel if kernel is not None else jackson_kernel()
+        self._gemm_mode = 1 if moments_gemm == "tensor" else 0
         self._cfg_args = dict(energy_range=tuple(energy_range), kernel=self.kernel.name,
                               kernel_param=self.kernel.param, matrix_format=matrix_format,
                               optimal_size=optimal_size, interleaved=interleaved,
@@ -204,10 +208,12 @@ class GpuImpl:
         return Deferred(lambda: self.calc_ldos(energy, broadening, position, sublattice))
 
     def calc_conductivity(self, chemical_potential, broadening, temperature, direction, num_random, num_points,
-                          gemm_mode=0):
+                          gemm_mode=None):
         """``KPM::calc_conductivity`` (KPM.cpp:131-149); returns the real part."""
         if len(direction) != 2 or any(c not in "xyz" for c in direction):
             raise RuntimeError("Invalid direction: must be 'xx', 'xy', 'zz', or similar.")
+        if gemm_mode is None:
+            gemm_mode = self._gemm_mode
         pos = dict(zip("xyz", self._model.system.positions))
         out = self._engine.calc_conductivity(pos[direction[0]], pos[direction[1]], chemical_potential, broadening,
                                              temperature, num_random, num_points, gemm_mode)
@@ -310,7 +316,9 @@ def kpm(model, energy_range=None, kernel="default", num_threads="auto", silent=F
 
     Extra keyword arguments of ``_cpp.kpm`` are accepted: ``matrix_format``,
     ``optimal_size``, ``interleaved``, ``lanczos_precision``; plus the GPU knobs
-    ``precision`` ("auto", "fp64", "fp32") and ``batch_width``. ``num_threads``
+    ``precision`` ("auto", "fp64", "fp32"), ``batch_width`` and ``moments_gemm``
+    ("fp64": the conductivity's moments matrix on the FP64 CUDA cores; "tensor": on
+    the tensor cores from FP32 planes, three-product TF32 split). ``num_threads``
     and ``silent`` are accepted for compatibility (the GPU needs no CPU threads
     and prints no progress).
     """

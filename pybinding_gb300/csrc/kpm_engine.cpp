@@ -1547,7 +1547,8 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "conductivity needs a single-system engine");
         if (!left || !right || (nmu > 0 && (!chem || !out))) fail(KPM_ERR_VALUE, "null argument");
         if (num_random < 1 || num_points < 2) fail(KPM_ERR_VALUE, "num_random >= 1 and num_points >= 2 required");
-        if (gemm_mode != 0) fail(KPM_ERR_VALUE, "unknown gemm_mode");
+        if (gemm_mode != 0 && gemm_mode != 1) fail(KPM_ERR_VALUE, "gemm_mode must be 0 (FP64) or 1 (tensor cores)");
+        bool const tc = gemm_mode == 1;
         double const t0 = now_s();
         auto const sc = e->scale(0);
         int64_t const M = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / sc.a);
@@ -1565,10 +1566,12 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         std::vector<unsigned char> vr_ell(static_cast<size_t>(n) * W * vs * vb, 0);
         std::vector<unsigned char> starters_l, starters_r;
         int64_t K = 1;
+        // tensor-core GEMM: the collected vectors are kept as FP32 planes (re [, im])
+        int const planes = kpm::vtype_complex(vt) ? 2 : 1;
         {   // vectors per batch: both sides keep M x n x K vectors
             size_t free_b = 0, total_b = 0;
             KPM_CUDA(cudaMemGetInfo(&free_b, &total_b));
-            double const per_vec = 2.0 * static_cast<double>(M) * n * vb;
+            double const per_vec = 2.0 * static_cast<double>(M) * n * (tc ? 4 * planes : vb);
             int64_t kmax = static_cast<int64_t>(0.5 * static_cast<double>(free_b) / per_vec);
             if (kmax < 1) fail(KPM_ERR_RUNTIME, "not enough device memory for the conductivity moments");
             for (int64_t k : {16, 8, 4, 2, 1}) {
@@ -1633,8 +1636,18 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         DBuf d_v2, d_L, d_R, d_mu_acc, d_samples, d_sum, d_chem, d_res;
         d_v2.ensure(vr_ell.size());
         KPM_CUDA(cudaMemcpyAsync(d_v2.p, vr_ell.data(), vr_ell.size(), cudaMemcpyHostToDevice, e->stream));
-        d_L.ensure(vec_bytes * M);
-        d_R.ensure(vec_bytes * M);
+        // plane row stride: 16-byte multiple for the tensor maps
+        int64_t const ld = ((n * K + 3) / 4) * 4;
+        if (tc && (M > (int64_t{1} << 20) || n * K > (int64_t{1} << 31) - 64))
+            fail(KPM_ERR_VALUE, "gemm_mode=1 needs num_moments <= 2^20 and rows x vectors < 2^31");
+        size_t const plane_bytes = sizeof(float) * static_cast<size_t>(ld) * M;
+        d_L.ensure(tc ? plane_bytes * planes : vec_bytes * M);
+        d_R.ensure(tc ? plane_bytes * planes : vec_bytes * M);
+        DBuf d_err;
+        if (tc) {
+            d_err.ensure(sizeof(int));
+            KPM_CUDA(cudaMemsetAsync(d_err.p, 0, sizeof(int), e->stream));
+        }
         e->d_x0.ensure(vec_bytes);
         e->d_x1.ensure(vec_bytes);
         e->d_stage.ensure(static_cast<size_t>(K) * n * ssize);
@@ -1668,9 +1681,17 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
                 a.init = step == 1;
                 a.x = step == 1 ? r0 : r1;
                 a.y = step == 1 ? r1 : r0;
-                void* row = store + vec_bytes * (step - 1);
-                a.zx = right_side ? nullptr : row;
-                a.zv = right_side ? row : nullptr;
+                if (tc) {
+                    auto* re = reinterpret_cast<float*>(store) + ld * (step - 1);
+                    a.zre = re;
+                    a.zim = planes == 2 ? re + ld * M : nullptr;
+                    a.zx = nullptr;
+                    a.zv = nullptr;
+                } else {
+                    void* row = store + vec_bytes * (step - 1);
+                    a.zx = right_side ? nullptr : row;
+                    a.zv = right_side ? row : nullptr;
+                }
                 KPM_CUDA(kpm::launch_dense_step(a, e->stream));
                 if (step > 1) std::swap(r0, r1);
             }
@@ -1686,12 +1707,25 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
             recursion(starters_r.data() + static_cast<size_t>(b) * K * n * ssize, true);
             KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
             // mu += L R^H: inner dimension = rows x K (rows n of both stores are [row][K])
-            KPM_CUDA(kpm::launch_mu_gemm_fp64(vt, d_L.p, d_R.p, M, n * K, d_mu_acc.as<double>(), e->stream));
+            if (tc) {
+                auto const* lre = d_L.as<float>();
+                auto const* rre = d_R.as<float>();
+                KPM_CUDA(kpm::launch_mu_gemm_tc(planes == 2, lre, planes == 2 ? lre + ld * M : nullptr, rre,
+                                                planes == 2 ? rre + ld * M : nullptr, M, n * K, ld, 1,
+                                                d_mu_acc.as<double>(), d_err.as<int>(), e->stream));
+            } else {
+                KPM_CUDA(kpm::launch_mu_gemm_fp64(vt, d_L.p, d_R.p, M, n * K, d_mu_acc.as<double>(), e->stream));
+            }
             KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
             KPM_CUDA(cudaStreamSynchronize(e->stream));
             float ms = 0;
             KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
             gemm_time += ms * 1e-3;
+        }
+        if (tc) {
+            int herr = 0;
+            KPM_CUDA(cudaMemcpy(&herr, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (herr != 0) fail(KPM_ERR_TIMEOUT, "tensor-core moments GEMM: a bounded device wait expired");
         }
         // normalise, halve row/column 0 (the collectors store T_0 / 2), damp g_m g_n (Kernel.hpp:48-56)
         std::vector<double> mu(static_cast<size_t>(2 * M * M));

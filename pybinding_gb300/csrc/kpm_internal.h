@@ -79,6 +79,8 @@ struct DenseStep {
     void* y;
     void* zx;                 // nullable, [rows][K]
     void* zv;                 // nullable, [rows][K]
+    float* zre;               // nullable: FP32 planes [rows][K] of the collected vector (V r when
+    float* zim;               // val2 is set, else r); zim for complex types only
     const Tile* tiles;
     int num_tiles;
     bool init;
@@ -120,6 +122,13 @@ cudaError_t launch_dense_step(DenseStep const& a, cudaStream_t s);
 // A and B in vtype; split over I with FP64 atomics.
 cudaError_t launch_mu_gemm_fp64(int vtype, void const* A, void const* B, int64_t M, int64_t I, double* mu,
                                 cudaStream_t s);
+
+// mu += L R^H on tensor cores (tcgen05 kind::tf32, three-product hi/lo split; FP64 atomics).
+// Operands are FP32 planes [M][ld] (row m = vector L_m / R_m over I = rows x vectors
+// elements, 16-byte aligned, ld * 4 a multiple of 16); cplx adds the imaginary planes.
+// mu is complex double [n * M + m]. err is set when a bounded device wait gives up.
+cudaError_t launch_mu_gemm_tc(bool cplx, float const* a_re, float const* a_im, float const* b_re, float const* b_im,
+                              int64_t M, int64_t I, int64_t ld, int group_kb, double* mu, int* err, cudaStream_t s);
 
 // Kubo-Bastin (kpm/reconstruct.hpp:90-143) in FP64:
 // sum_nm[e] = 1/(1-en^2)^2 * sum_{m,n} mu(m,n) (A_n T_m + conj(A_m) T_n), en = scaled sample e

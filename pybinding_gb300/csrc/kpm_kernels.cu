@@ -42,6 +42,13 @@ template<> struct Tr<double> { using R = double; static constexpr bool C = false
 template<> struct Tr<float2> { using R = float; static constexpr bool C = true; static constexpr int VS = 2; };
 template<> struct Tr<double2> { using R = double; static constexpr bool C = true; static constexpr int VS = 1; };
 
+__device__ __forceinline__ float re32(float a) { return a; }
+__device__ __forceinline__ float re32(double a) { return static_cast<float>(a); }
+__device__ __forceinline__ float re32(float2 a) { return a.x; }
+__device__ __forceinline__ float re32(double2 a) { return static_cast<float>(a.x); }
+__device__ __forceinline__ float im32(float2 a) { return a.y; }
+__device__ __forceinline__ float im32(double2 a) { return static_cast<float>(a.y); }
+
 __device__ __forceinline__ void vzero(float& a) { a = 0.f; }
 __device__ __forceinline__ void vzero(double& a) { a = 0.0; }
 __device__ __forceinline__ void vzero(float2& a) { a = make_float2(0.f, 0.f); }
@@ -390,7 +397,7 @@ template<class V, int E, int LPR, bool INIT>
 __global__ void __launch_bounds__(BLOCK)
 dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V const* __restrict__ val2, int W,
                   V const* __restrict__ x, V* __restrict__ y, V* __restrict__ zx, V* __restrict__ zv,
-                  Tile const* __restrict__ tiles) {
+                  float* __restrict__ zre, float* __restrict__ zim, Tile const* __restrict__ tiles) {
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;
     using P = Pack<V, E>;
@@ -412,7 +419,7 @@ dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V 
                 V const a = vp[j * VS + v];
 #pragma unroll
                 for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
-                if (zv != nullptr) {
+                if (val2 != nullptr) {
                     V const b = val2[(static_cast<int64_t>(r) * W + j) * VS + v];
 #pragma unroll
                     for (int e = 0; e < E; ++e) vfma(sv[e], b, xv.v[e]);
@@ -431,6 +438,20 @@ dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V 
             for (int e = 0; e < E; ++e) yn.v[e] = vsub(sum[e], yo.v[e]);
         }
         *yp = yn;
+        if (zre != nullptr) {  // FP32 planes for the tensor-core moments GEMM: V r (right) or r (left)
+            P o;
+            if (val2 != nullptr) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) o.v[e] = sv[e];
+            } else {
+                o = reinterpret_cast<P const*>(x + off)[lane];
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                zre[off + lane * E + e] = re32(o.v[e]);
+                if constexpr (Tr<V>::C) zim[off + lane * E + e] = im32(o.v[e]);
+            }
+        }
         if (zx != nullptr) reinterpret_cast<P*>(zx + off)[lane] = reinterpret_cast<P const*>(x + off)[lane];
         if (zv != nullptr) {
             P o;
@@ -451,9 +472,11 @@ cudaError_t dense_launch(DenseStep const& a, cudaStream_t s) {
     auto* zx = static_cast<V*>(a.zx);
     auto* zv = static_cast<V*>(a.zv);
     if (a.init)
-        dense_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.tiles);
+        dense_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.zre,
+                                                                         a.zim, a.tiles);
     else
-        dense_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.tiles);
+        dense_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.zre,
+                                                                          a.zim, a.tiles);
     return cudaGetLastError();
 }
 

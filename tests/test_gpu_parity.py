@@ -281,3 +281,44 @@ def test_one_and_two_steps_per_launch(oracle, fuse, dtype, nvec, tol):
         err = rel_err(moms[s], ref)
         print("fuse=%d %s nvec=%d system %d: %.3e" % (fuse, np.dtype(dtype).name, nvec, s, err))
         assert err <= tol
+
+
+@pytest.mark.parametrize("name", sorted(TM.COND_MODELS))
+def test_conductivity_tensor_core_gemm_matches_reference_golden(baselines, name):
+    """The tensor-core moments GEMM against the same goldens as the FP64 one (tests/test_kpm.py:176-197)."""
+    kind, size = TM.COND_MODELS[name]
+    model = TM.graphene(kind, size)
+    energy = np.linspace(-2, 2, 25)
+    k = kpm(model, energy_range=[-9, 9], kernel=lorentz_kernel(), silent=True, moments_gemm="tensor")
+    sigma = k.calc_conductivity(energy, broadening=0.5, temperature=0, num_points=200)
+    np.testing.assert_allclose(sigma.data, baselines["conductivity[%s]" % name], rtol=1e-2, atol=1e-5)
+
+
+@pytest.mark.parametrize("dtype,precision", [(np.complex128, "fp64"), (np.float64, "fp64"),
+                                             (np.complex64, "fp32"), (np.float32, "fp32")])
+def test_conductivity_tensor_core_gemm_matches_fp64_gemm(oracle, dtype, precision):
+    """gemm_mode 1 (tcgen05 TF32 three-product split of FP32 planes) against gemm_mode 0 (FP64
+    CUDA cores) on the same engine, and against the FP64 oracle: sigma within 2e-5 of max |sigma|.
+    The model is large enough for several 128 x 128 tiles (M = 276 moments) and long slices of
+    I = rows x vectors (3 random vectors of ~5,500 sites)."""
+    m = TM.graphene("magnetic_field" if np.iscomplexobj(np.zeros(1, dtype)) else "const_potential", 12)
+    h = m.hamiltonian.astype(dtype)
+    x, y = m.system.x, m.system.y
+    chem = np.linspace(-2.5, 2.5, 21)
+    cfg = dict(energy_range=(-9.0, 9.0), kernel="jackson", precision=precision)
+    eng = _native.Engine(h, _native.make_config(**cfg))
+    fp64 = eng.calc_conductivity(x, y, chem, 0.08, 0.0, 3, 200, gemm_mode=0)
+    tc = eng.calc_conductivity(x, y, chem, 0.08, 0.0, 3, 200, gemm_mode=1)
+    assert eng.stats().num_moments > 256
+    err = rel_err(tc, fp64)
+    print("%s %s: n=%d M=%d  tensor vs fp64 gemm %.3e" % (np.dtype(dtype).name, precision, h.shape[0],
+                                                       eng.stats().num_moments, err))
+    assert err < 2e-5
+    if precision == "fp64":
+        h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
+        ref = oracle.core_conductivity(h64, x, y, chem, 0.08, 0.0, 3, 200, matrix_format="ELL",
+                                       optimal_size=True, interleaved=True, energy_range=(-9.0, 9.0),
+                                       kernel="jackson")
+        err_o = rel_err(tc, ref)
+        print("  tensor vs oracle %.3e" % err_o)
+        assert err_o < 2e-5
