@@ -186,6 +186,21 @@ int kpm_calc_conductivity(kpm_engine* engine, const float* left_coords, const fl
                           double temperature, int64_t num_random, int64_t num_points, int32_t gemm_mode,
                           double* out);
 
+/* Reverse-mode (adjoint) gradient of the averaged diagonal moments, system 0, real
+ * Hamiltonians. No reference counterpart: pybinding has no gradients; the forward
+ * algorithm differentiated is cpb's diagonal recursion (kpm/calc_moments.hpp:35-58,
+ * kpm/default/collectors.cpp:6-36). For L = sum_n dl_dmu[n] mu_n, mu being what
+ * kpm_moments_diag(engine, num_moments, num_vectors, starters, 0, average = 1, ...) returns
+ * for the same starters ([num_vectors][rows], H's scalar type, site order), it writes
+ * dL/dH for every stored entry of the input CSR (out_grad_values: nnz doubles, CSR order)
+ * and dL/d(onsite energy) per site (out_grad_onsite: rows doubles, nullable; also where H
+ * stores no diagonal). dl_dmu has round_num_moments(num_moments) entries. The scaling
+ * (a, b) is held fixed. checkpoint: forward vectors are kept every `checkpoint` steps and
+ * recomputed segment by segment; 0 = ceil(sqrt(M / 2)); >= M / 2 - 1 recomputes nothing. */
+int kpm_adjoint_diag(kpm_engine* engine, int64_t num_moments, int64_t num_vectors, const void* starters,
+                     const double* dl_dmu, int64_t checkpoint, double* out_grad_values, double* out_grad_onsite,
+                     int64_t* num_moments_out);
+
 /* Stats of the last calculation (kpm/Stats.cpp:31-65; KPMStats, cppmodule/src/kpm.cpp:50-66). */
 int kpm_get_stats(kpm_engine* engine, kpm_stats* out);
 

@@ -6,8 +6,9 @@ computation runs in hand-written CUDA kernels for sm_103a behind a C ABI
 boundary. There is no CPU fallback: calls fail if the CUDA library cannot be
 loaded or no GPU is present.
 """
+from . import adjoint
 from .chebyshev import (KPM, KPMBatch, Series, SpatialLDOS, dirichlet_kernel, jackson_kernel, kpm, kpm_batch,
                         lorentz_kernel)
 
 __all__ = ["KPM", "KPMBatch", "Series", "SpatialLDOS", "kpm", "kpm_batch", "jackson_kernel", "lorentz_kernel",
-           "dirichlet_kernel"]
+           "dirichlet_kernel", "adjoint"]

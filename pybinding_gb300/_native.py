@@ -57,6 +57,7 @@ SIGNATURES = {
     "kpm_calc_greens": (_I32, [_P, _I64, _P, _I64, _P, _I64, _D, _P]),
     "kpm_moments": (_I32, [_P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _P]),
     "kpm_calc_conductivity": (_I32, [_P, _P, _P, _P, _I64, _D, _D, _I64, _I64, _I32, _P]),
+    "kpm_adjoint_diag": (_I32, [_P, _I64, _I64, _P, _P, _I64, _P, _P, _P]),
     "kpm_get_stats": (_I32, [_P, _P]),
     "kpm_report": (_I32, [_P, _I32, _P, _I64]),
     "kpm_optimized_hamiltonian": (_I32, [_P, _P, _I64, _P, _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
@@ -268,6 +269,25 @@ class Engine:
                                           float(temperature), int(num_random), int(num_points), int(gemm_mode),
                                           ptr(out)))
         return out
+
+    def adjoint_diag(self, num_moments, starters, dl_dmu, checkpoint=0):
+        """Gradient of L = sum_n dl_dmu[n] mu_n (mu: averaged diagonal moments of ``starters``
+        [vector][site]) with respect to the stored entries of H (CSR order) and the onsite
+        energies; returns (grad_values, grad_onsite), both float64."""
+        rounded = round_num_moments(num_moments)
+        w = np.ascontiguousarray(dl_dmu, np.float64)
+        if w.size != rounded:
+            raise ValueError("dl_dmu must hold round_num_moments(num_moments) = %d entries" % rounded)
+        keep = np.ascontiguousarray(starters, dtype=self.dtype)
+        if keep.size == 0 or keep.size % self.rows:
+            raise ValueError("starters must hold num_vectors * %d elements" % self.rows)
+        nvec = keep.size // self.rows
+        gv = np.empty(self._nnz, np.float64)
+        go = np.empty(self.rows, np.float64)
+        nout = C.c_int64()
+        check(lib().kpm_adjoint_diag(self._h, num_moments, nvec, ptr(keep), ptr(w), int(checkpoint), ptr(gv), ptr(go),
+                                     C.byref(nout)))
+        return gv, go
 
     def stream(self):
         """The engine's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""

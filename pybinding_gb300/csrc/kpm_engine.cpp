@@ -1773,6 +1773,201 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
     });
 }
 
+// Reverse-mode gradient of the averaged diagonal moments (no reference counterpart).
+// Forward: v0 = r, v1 = S v0 / 2, v_k = S v_{k-1} - v_{k-2} (k <= N = M / 2), with
+// mu_1 = <v1|v0>, mu_{2k} = 2<v_k|v_k> - mu_0, mu_{2k+1} = 2<v_{k+1}|v_k> - mu_1
+// (calc_moments.hpp:35-58, collectors.cpp:6-36). For L = sum_n w_n mean_r mu_n the adjoint
+// vectors lam_k = dL/dv_k obey the same recursion backwards,
+//   lam_N = beta_N v_{N-1},  lam_k = S lam_{k+1} - lam_{k+2} + 2 alpha_k v_k + beta_k v_{k-1} + beta_{k+1} v_{k+1},
+// alpha_k = 2 w_{2k} / R, beta_k = 2 w_{2k-1} / R, and
+//   dL/dS = sum_{k=1}^{N-1} lam_{k+1} v_k^T + (lam_1 + c1 v0) v0^T / 2,  c1 = (w_1 - sum_k w_{2k-1}) / R,
+// on the pattern of S (symmetric, so the kernel accumulates the transposed entry from the
+// gather it already does). dL/dH = (2 / a) dL/dS with a, b frozen. Forward vectors are kept
+// as checkpoint pairs (v_c, v_{c+1}) every `checkpoint` steps and recomputed per segment.
+int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, const void* starters,
+                     const double* dl_dmu, int64_t checkpoint, double* out_grad_values, double* out_grad_onsite,
+                     int64_t* num_moments_out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (!starters || !dl_dmu || !out_grad_values) fail(KPM_ERR_VALUE, "null argument");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "adjoint gradients need a single-system engine");
+        if (kpm::vtype_complex(e->vtype) || e->stype == KPM_C64 || e->stype == KPM_C128)
+            fail(KPM_ERR_VALUE, "adjoint gradients need a real Hamiltonian");
+        if (num_vectors < 1) fail(KPM_ERR_VALUE, "num_vectors must be >= 1");
+        if (checkpoint < 0) fail(KPM_ERR_VALUE, "checkpoint must be >= 0");
+        double const t0 = now_s();
+        int64_t const M = round_moments(num_moments);
+        int64_t const N = M / 2;
+        // segment length: at least 2 (a checkpoint pair is two consecutive vectors)
+        int64_t const seg_len = std::max<int64_t>(
+            2, std::min<int64_t>(checkpoint > 0 ? checkpoint
+                                                : static_cast<int64_t>(std::ceil(std::sqrt(static_cast<double>(N)))),
+                                 N - 1));
+        int64_t const nseg = N >= 2 ? (N - 2) / seg_len + 1 : 0;  // segments cover k = 1 .. N-1
+        e->optimize({0}, {0});
+        auto const sc = e->scale(0);
+        int64_t const n = e->rows;
+        int const vt = e->vtype;
+        int const vb = kpm::vtype_bytes(vt);
+        int const W = e->W;
+        double const R = static_cast<double>(num_vectors);
+        std::vector<double> alpha(N + 2, 0.0), beta(N + 2, 0.0);
+        for (int64_t k = 1; k <= N - 1; ++k) alpha[k] = 2.0 * dl_dmu[2 * k] / R;
+        for (int64_t k = 2; k <= N; ++k) beta[k] = 2.0 * dl_dmu[2 * k - 1] / R;
+        double c1 = M > 1 ? dl_dmu[1] : 0.0;
+        for (int64_t k = 2; k <= N; ++k) c1 -= dl_dmu[2 * k - 1];
+        c1 /= R;
+
+        kpm_engine::Shape sh = e->pick_shape(num_vectors);
+        int64_t const K = sh.K;
+        sh.nbatch = 1;
+        int const ntiles = e->build_tiles(sh, true);
+        size_t const vec = static_cast<size_t>(n) * K * vb;
+        // checkpoint pairs, segment vectors v_{c+2} .. v_{c+seg_len+1}, two adjoint vectors,
+        // two rolling forward vectors
+        DBuf d_ck, d_seg, d_lam, d_roll, d_gt, d_gd;
+        d_ck.ensure(vec * 2 * std::max<int64_t>(nseg, 1));
+        d_seg.ensure(vec * seg_len);
+        d_lam.ensure(vec * 2);
+        d_roll.ensure(vec * 2);
+        d_gt.ensure(sizeof(double) * static_cast<size_t>(n) * W);
+        d_gd.ensure(sizeof(double) * static_cast<size_t>(n));
+        KPM_CUDA(cudaMemsetAsync(d_gt.p, 0, d_gt.bytes, e->stream));
+        KPM_CUDA(cudaMemsetAsync(d_gd.p, 0, d_gd.bytes, e->stream));
+        auto* ck = static_cast<unsigned char*>(d_ck.p);
+        auto* segb = static_cast<unsigned char*>(d_seg.p);
+        auto* lamb = static_cast<unsigned char*>(d_lam.p);
+        auto* roll = static_cast<unsigned char*>(d_roll.p);
+        auto ckA = [&](int64_t j) { return ck + vec * (2 * j); };      // v_{j s}
+        auto ckB = [&](int64_t j) { return ck + vec * (2 * j + 1); };  // v_{j s + 1}
+
+        kpm::AdjStep base{};
+        base.vtype = vt;
+        base.E = sh.E;
+        base.LPR = sh.LPR;
+        base.col = e->d_col.as<int32_t>();
+        base.val = e->d_val.p;
+        base.W = W;
+        base.tiles = e->d_tiles.as<Tile>();
+        base.num_tiles = ntiles;
+        auto step = [&](void const* x, void const* yprev, void* out, bool half) {  // out = S x - yprev
+            kpm::AdjStep a = base;
+            a.x = x;
+            a.yprev = yprev;
+            a.out = out;
+            a.half = half;
+            KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+        };
+
+        size_t const ssize = static_cast<size_t>(scalar_bytes(e->stype));
+        std::vector<unsigned char> stage(static_cast<size_t>(K) * n * ssize);
+        e->d_stage.ensure(stage.size());
+        KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
+        int64_t const nbatch = (num_vectors + K - 1) / K;
+        for (int64_t b = 0; b < nbatch; ++b) {
+            int64_t const v_first = b * K;
+            int64_t const v_count = std::min<int64_t>(K, num_vectors - v_first);
+            KPM_CUDA(cudaStreamSynchronize(e->stream));  // the previous batch's upload has been consumed
+            std::fill(stage.begin(), stage.end(), 0);  // missing vectors of the last batch are zero
+            std::memcpy(stage.data(), static_cast<unsigned char const*>(starters) + static_cast<size_t>(v_first) * n * ssize,
+                        static_cast<size_t>(v_count) * n * ssize);
+            KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, stage.data(), stage.size(), cudaMemcpyHostToDevice, e->stream));
+            KPM_CUDA(cudaMemsetAsync(ckA(0), 0, vec, e->stream));
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, e->d_stage.p, ckA(0), e->d_map.as<int32_t>(),
+                                                  e->d_sysoff.as<int64_t>(), 1, K, static_cast<int>(K), 1, n,
+                                                  e->stream));
+            // forward pass: checkpoints (v_c, v_{c+1}) for c = j * seg_len
+            unsigned char* v0 = ckA(0);
+            unsigned char* v1 = nseg > 0 ? ckB(0) : roll;
+            step(v0, nullptr, v1, true);
+            if (nseg > 1) {
+                int64_t const last = (nseg - 1) * seg_len + 1;  // highest index needed
+                auto fwd_ptr = [&](int64_t k) -> unsigned char* {
+                    if (k % seg_len == 0 && k / seg_len < nseg) return ckA(k / seg_len);
+                    if (k % seg_len == 1 && k / seg_len < nseg) return ckB(k / seg_len);
+                    return roll + vec * (k % 2);
+                };
+                for (int64_t k = 1; k < last; ++k) step(fwd_ptr(k), fwd_ptr(k - 1), fwd_ptr(k + 1), false);
+            }
+            // backward pass, segment by segment from the end
+            unsigned char* lam1 = nullptr;  // lam_{k+1}
+            unsigned char* lam2 = nullptr;  // lam_{k+2} (nullptr = 0)
+            for (int64_t j = nseg - 1; j >= 0; --j) {
+                int64_t const c = j * seg_len;
+                int64_t const kmax = std::min<int64_t>(c + seg_len, N - 1);
+                auto sp = [&](int64_t k) -> unsigned char* {
+                    if (k == c) return ckA(j);
+                    if (k == c + 1) return ckB(j);
+                    return segb + vec * (k - c - 2);
+                };
+                for (int64_t k = c + 1; k <= kmax; ++k) step(sp(k), sp(k - 1), sp(k + 1), false);
+                if (lam1 == nullptr) {  // lam_N = beta_N v_{N-1}
+                    lam1 = lamb;
+                    KPM_CUDA(kpm::launch_axpby(vt, n * K, beta[N], sp(N - 1), 0.0, nullptr, lam1, e->stream));
+                }
+                for (int64_t k = kmax; k > c; --k) {
+                    unsigned char* out = lam2 != nullptr ? lam2 : (lam1 == lamb ? lamb + vec : lamb);
+                    kpm::AdjStep a = base;
+                    a.x = lam1;
+                    a.yprev = lam2;
+                    a.out = out;
+                    a.half = false;
+                    a.v0 = sp(k);
+                    a.a0 = 2.0 * alpha[k];
+                    a.vm = sp(k - 1);
+                    a.am = beta[k];
+                    a.vp = sp(k + 1);
+                    a.ap = beta[k + 1];
+                    a.g = sp(k);
+                    a.gt = d_gt.as<double>();
+                    a.gd = d_gd.as<double>();
+                    KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+                    lam2 = lam1;
+                    lam1 = out;
+                }
+            }
+            // (lam_1 + c1 v0) v0^T / 2
+            unsigned char* u = (lam1 == lamb) ? lamb + vec : lamb;
+            if (lam1 != nullptr)
+                KPM_CUDA(kpm::launch_axpby(vt, n * K, 0.5, lam1, 0.5 * c1, v0, u, e->stream));
+            else
+                KPM_CUDA(kpm::launch_axpby(vt, n * K, 0.5 * c1, v0, 0.0, nullptr, u, e->stream));
+            kpm::AdjStep a = base;
+            a.x = u;
+            a.g = v0;
+            a.gt = d_gt.as<double>();
+            a.gd = d_gd.as<double>();
+            KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+        }
+        KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
+        std::vector<double> gt(static_cast<size_t>(n) * W), gd(static_cast<size_t>(n));
+        std::vector<int32_t> hcol(static_cast<size_t>(n) * W);
+        KPM_CUDA(cudaMemcpyAsync(gt.data(), d_gt.p, sizeof(double) * gt.size(), cudaMemcpyDeviceToHost, e->stream));
+        KPM_CUDA(cudaMemcpyAsync(gd.data(), d_gd.p, sizeof(double) * gd.size(), cudaMemcpyDeviceToHost, e->stream));
+        KPM_CUDA(cudaMemcpyAsync(hcol.data(), e->d_col.p, sizeof(int32_t) * hcol.size(), cudaMemcpyDeviceToHost, e->stream));
+        KPM_CUDA(cudaStreamSynchronize(e->stream));
+        float ms = 0;
+        KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        // gt[p][t] holds G[col(p, t)][p]: entry (i, j) of the input is found in row map[j]
+        double const f = 2.0 / sc.a;
+        for (int64_t i = 0; i < n; ++i)
+            for (int32_t k = e->indptr[i]; k < e->indptr[i + 1]; ++k) {
+                int32_t const ni = e->map[i], nj = e->map[e->indices[k]];
+                int t = 0;
+                while (t < W && hcol[static_cast<size_t>(nj) * W + t] != ni) ++t;
+                if (t == W) fail(KPM_ERR_RUNTIME, "internal: adjoint entry outside the S pattern");
+                out_grad_values[k] = f * (ni == nj ? gd[ni] : gt[static_cast<size_t>(nj) * W + t]);
+            }
+        if (out_grad_onsite)
+            for (int64_t i = 0; i < n; ++i) out_grad_onsite[i] = f * gd[e->map[i]];
+        e->reset_stats(M, true, false, static_cast<double>(num_vectors), 0);
+        e->st.moments_time = ms * 1e-3;
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+        if (num_moments_out) *num_moments_out = M;
+    });
+}
+
 int kpm_get_stats(kpm_engine* e, kpm_stats* out) {
     return guarded([&] {
         if (!e || !out) fail(KPM_ERR_VALUE, "null argument");

@@ -86,6 +86,31 @@ struct DenseStep {
     bool init;
 };
 
+// Adjoint of the diagonal recursion (real types): one launch of
+//   out = S x - yprev (or S x / 2 when half) + a0 v0 + am vm + ap vp
+// plus, when gt is set, gt[r][j] += sum_k x[col[r][j]][k] * g[r][k] (FP64, [rows][W]) and
+// gd[r] += sum_k x[r][k] * g[r][k] (FP64, [rows]).
+struct AdjStep {
+    int vtype;
+    int E, LPR;
+    const int32_t* col;
+    const void* val;
+    int W;
+    const void* x;
+    const void* yprev;        // nullable; may alias out
+    void* out;                // nullable (gradient only)
+    bool half;
+    const void* v0;           // nullable
+    const void* vm;           // nullable
+    const void* vp;           // nullable
+    double a0, am, ap;
+    const void* g;            // row vectors of the gradient term (with gt)
+    double* gt;               // nullable
+    double* gd;               // set with gt
+    const Tile* tiles;
+    int num_tiles;
+};
+
 // Two recursion steps in one launch (steps n and n+1; P = T_{n-2} -> T_n, Q = T_{n-1} -> T_{n+1}).
 // items: [2 * num_tiles] work items (tile * 2 + phase) in dependency order; band: [num_tiles][2]
 // tile range whose phase A must finish before phase B of the tile; flags: [num_tiles] sequence
@@ -139,6 +164,10 @@ cudaError_t launch_kubo_integrate(double const* sum_nm, double const* scaled_sam
                                   double const* scaled_mu, int nmu, double inv_kbt, double coeff, double prefix,
                                   double* out, cudaStream_t s);
 cudaError_t launch_off_step(OffStep const& a, cudaStream_t s);
+cudaError_t launch_adj_step(AdjStep const& a, cudaStream_t s);
+// out = a x + b y over n elements of a real vector type (y nullable)
+cudaError_t launch_axpby(int vtype, int64_t n, double a, void const* x, double b, void const* y, void* out,
+                         cudaStream_t s);
 bool diag_shape_supported(int vtype, int E, int LPR);
 
 // moments from the accumulated sums: out[(s*nbatch*K + v) * M + n] complex double,

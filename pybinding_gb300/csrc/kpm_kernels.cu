@@ -480,6 +480,114 @@ cudaError_t dense_launch(DenseStep const& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ adjoint step (real types)
+// out = S x - yprev (or S x / 2 when half) + a0 v0 + am vm + ap vp   (out and yprev may alias;
+// yprev, v0, vm, vp nullable), and when gt is set, per row r and ELL slot j
+//   gt[r][j] += sum over the K vectors of x[col_j] * g[r]
+// (the gradient of the recursion with respect to the transposed entry S[col_j][r]; the
+// pattern of S is symmetric) and gd[r] += sum_k x[r][k] * g[r][k] (the diagonal, also where
+// S stores none). The row loop is uniform over the block so that the lanes of a row can
+// reduce with warp shuffles.
+template<class V, int E, int LPR>
+__global__ void __launch_bounds__(BLOCK)
+adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x,
+                V const* yprev, V* out, int half, V const* __restrict__ v0, V const* __restrict__ vm,
+                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, double* __restrict__ gt,
+                double* __restrict__ gd, Tile const* __restrict__ tiles) {
+    static_assert(!Tr<V>::C, "the adjoint step is real");
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;
+    constexpr int VS = Tr<V>::VS;
+    using P = Pack<V, E>;
+    Tile const t = tiles[blockIdx.x];
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    for (int rb = t.row_begin; rb < t.row_end; rb += RPP) {
+        int const r = rb + slot;
+        bool const live = r < t.row_end;
+        int const rs = live ? r : t.row_begin;  // dead lanes follow a valid row without storing
+        V sum[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) vzero(sum[e]);
+        P gv;
+        if (gt != nullptr) {
+            gv = ld_ro(reinterpret_cast<P const*>(g + static_cast<int64_t>(rs) * K) + lane);
+            P const xr = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(rs) * K) + lane);
+            V p = V(0);
+#pragma unroll
+            for (int e = 0; e < E; ++e) vfma(p, xr.v[e], gv.v[e]);
+#pragma unroll
+            for (int off = 1; off < LPR; off <<= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
+            if (live && lane == 0) gd[r] += static_cast<double>(p);
+        }
+        int32_t const* cp = col + static_cast<int64_t>(rs) * W;
+        V const* vv = val + static_cast<int64_t>(rs) * W * VS;
+        for (int j = 0; j < W; ++j) {
+            int32_t const c = __ldg(cp + j);
+            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
+#pragma unroll
+            for (int v = 0; v < VS; ++v) {
+                V const a = vv[j * VS + v];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
+            }
+            if (gt != nullptr) {
+                V p = V(0);
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(p, xv.v[e], gv.v[e]);
+#pragma unroll
+                for (int off = 1; off < LPR; off <<= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
+                if (live && lane == 0) gt[static_cast<int64_t>(r) * W + j] += static_cast<double>(p);
+            }
+        }
+        if (live && out != nullptr) {
+            int64_t const off = static_cast<int64_t>(r) * K;
+            P o;
+#pragma unroll
+            for (int e = 0; e < E; ++e) o.v[e] = half ? vhalf(sum[e]) : sum[e];
+            if (yprev != nullptr) {
+                P const yo = reinterpret_cast<P const*>(yprev + off)[lane];
+#pragma unroll
+                for (int e = 0; e < E; ++e) o.v[e] -= yo.v[e];
+            }
+            if (v0 != nullptr) {
+                P const q = ld_ro(reinterpret_cast<P const*>(v0 + off) + lane);
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(o.v[e], a0, q.v[e]);
+            }
+            if (vm != nullptr) {
+                P const q = ld_ro(reinterpret_cast<P const*>(vm + off) + lane);
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(o.v[e], am, q.v[e]);
+            }
+            if (vp != nullptr) {
+                P const q = ld_ro(reinterpret_cast<P const*>(vp + off) + lane);
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(o.v[e], ap, q.v[e]);
+            }
+            reinterpret_cast<P*>(out + off)[lane] = o;
+        }
+    }
+}
+
+template<class V, int E, int LPR>
+cudaError_t adj_launch(AdjStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    adj_step_kernel<V, E, LPR><<<a.num_tiles, BLOCK, 0, s>>>(
+        a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x), static_cast<V const*>(a.yprev),
+        static_cast<V*>(a.out), a.half ? 1 : 0, static_cast<V const*>(a.v0), static_cast<V const*>(a.vm),
+        static_cast<V const*>(a.vp), static_cast<V>(a.a0), static_cast<V>(a.am), static_cast<V>(a.ap),
+        static_cast<V const*>(a.g), a.gt, a.gd, a.tiles);
+    return cudaGetLastError();
+}
+
+template<class V>
+__global__ void axpby_kernel(int64_t n, V a, V const* __restrict__ x, V b, V const* __restrict__ y, V* __restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = a * x[i] + (y != nullptr ? b * y[i] : V(0));
+}
+
 // ------------------------------------------------------------------ FP64 moments-matrix GEMM (split over I)
 __device__ __forceinline__ double2 to_cd(float v) { return make_double2(v, 0.0); }
 __device__ __forceinline__ double2 to_cd(double v) { return make_double2(v, 0.0); }
@@ -1144,6 +1252,29 @@ cudaError_t launch_kubo_integrate(double const* sum_nm, double const* samples, i
                                   double inv_kbt, double coeff, double prefix, double* out, cudaStream_t s) {
     if (nmu == 0) return cudaSuccess;
     kubo_integrate_kernel<<<(nmu + 127) / 128, 128, 0, s>>>(sum_nm, samples, ns, chem, nmu, inv_kbt, coeff, prefix, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_step(AdjStep const& a, cudaStream_t s) {
+#define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return adj_launch<V, e, l>(a, s);
+    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH)
+#undef KPM_DISPATCH
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_axpby(int vtype, int64_t n, double a, void const* x, double b, void const* y, void* out,
+                         cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    unsigned const blocks = static_cast<unsigned>(std::min<int64_t>((n + 255) / 256, 152 * 16));
+    if (vtype == V_F32)
+        axpby_kernel<float><<<blocks, 256, 0, s>>>(n, static_cast<float>(a), static_cast<float const*>(x),
+                                                   static_cast<float>(b), static_cast<float const*>(y),
+                                                   static_cast<float*>(out));
+    else if (vtype == V_F64)
+        axpby_kernel<double><<<blocks, 256, 0, s>>>(n, a, static_cast<double const*>(x), b,
+                                                    static_cast<double const*>(y), static_cast<double*>(out));
+    else
+        return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
