@@ -17,6 +17,15 @@ no explicit L2 flush is needed between steps.
 multithreaded restatement of DefaultCompute: ELL, interleaved recursion,
 8-vector batches, one thread per core) on a bounded sample of the same
 workload, on rank 0.
+
+`--workload` selects one of the other configurations instead (one JSON line
+each, same keys; they are measurements of the other hot-path rows, not the
+headline): `dos_c1` (60k-site complex128 graphene DOS, 8 vectors, 2048
+moments), `conductivity` (1M-site graphene at 20 T, complex128, 16 vectors,
+512 x 512 moments matrix on the tensor cores), `adjoint` (256k-site strained
+graphene, DOS misfit gradient, 32 vectors, 1024 moments, FP32) and
+`anderson3d` (160^3 simple cubic, 256 vectors, 8192 moments, FP32, plus LDOS
+at 4096 sites).
 """
 import argparse
 import json
@@ -51,6 +60,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-error", action="store_true", help="skip the FP64 moment-error check")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of one CPU sample")
+    p.add_argument("--workload", default="dos_batch",
+                   choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d"])
     return p.parse_args()
 
 
@@ -257,6 +268,7 @@ def run_gpu(args, rank, world, local_rank):
     # dominant kernel: the recursion step, timed by the engine's events on its own stream
     rec = float(np.median(rec_times))
     fuse = int(eng.stats().steps_per_launch)
+    lane_map = (int(eng.stats().elems_per_lane), int(eng.stats().lanes_per_row))
     launches = 1 + (M // 2 - 1) // fuse  # init + recursion launches
     avg_launch = rec / launches
     nrows = rows
@@ -333,7 +345,8 @@ def run_gpu(args, rank, world, local_rank):
                "moment_error_vs_fp64": err,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
-                            "kernel": "diag_step_kernel<float,4,16>" if fuse == 1 else "diag_pair_kernel<float,4,16>",
+                            "kernel": "%s<float,%d,%d>" % ("diag_step_kernel" if fuse == 1 else "diag_pair_kernel",
+                                                           lane_map[0], lane_map[1]),
                             "steps_per_launch": fuse, "alg_bytes_per_launch": alg_bytes,
                             "avg_launch_ms": avg_launch * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
                "cpu_baseline": {"value": cpu["value"], "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -346,12 +359,280 @@ def run_gpu(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- other configurations
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def _timed(fn, steps, warmup, stream):
+    """Run fn warmup + steps times; device time of the timed steps (CUDA events on `stream`),
+    the wall time, and the clocks seen meanwhile."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    w0 = time.perf_counter()
+    e0.record(stream)
+    outs = [fn() for _ in range(steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    return e0.elapsed_time(e1) * 1e-3, wall, clocks.stop(), outs
+
+
+def _jackson_broadening(num_moments, a):
+    """Broadening for which calc_* takes exactly num_moments Jackson moments (Kernel.cpp:6-20)."""
+    from pybinding_gb300 import _native
+    lo, hi = 1e-6, 10.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if _native.required_num_moments("jackson", 4.0, mid / a) > num_moments:
+            lo = mid
+        else:
+            hi = mid
+    return hi
+
+
+def _line(args, metric, value, unit, hib, t_step, config, dtype, **extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": hib, "scaling": "weak",
+           "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
+    out.update(extra)
+    print(json.dumps(out), flush=True)
+
+
+def workload_dos_c1(args, stream_of):
+    """60,000-site complex128 graphene flake (t = -2.8 eV, onsite 0), 8 random-phase vectors,
+    2048 moments (2050 after rounding), Jackson, Lanczos bounds, DOS at 1000 energies in [-9, 9]."""
+    from pybinding_gb300 import _native, lattice as L
+    m = L.graphene_flake(60000, is_complex=True, is_double=True)
+    h = m.hamiltonian.astype(np.complex128)
+    eng = _native.Engine(h, _native.make_config())
+    a, b = eng.scaling_factors()
+    broadening = _jackson_broadening(2048, a)
+    energy = np.linspace(-9, 9, 1000)
+    stream = stream_of(eng)
+    t, wall, clk, _ = _timed(lambda: eng.calc_dos(energy, broadening, 8), args.steps, args.warmup, stream)
+    st = eng.stats()
+    M = st.num_moments
+    work = (M / 2) * h.nnz * 8
+    rec = st.moments_time
+    launches = M // 2
+    alg = h.nnz * 20 + 4 * (h.shape[0] + 1) + 3 * h.shape[0] * 8 * 16
+    achieved = alg / (rec / launches) / 1e9
+    cpu = None
+    if args.cpu_seconds > 0:
+        from oracle import oracle as O
+        r = O.optimize(h, [0], [0], a, b)
+        rng = np.random.default_rng(1)
+        st0 = np.exp(2j * np.pi * rng.random((8, h.shape[0])))
+        st0 = O.reorder_vector(st0, r["reorder_map"])
+        Ms = 130
+        _, sec = O.bench_diag(r["h2"], r["slices"], st0, Ms, 8, 1)
+        cpu = {"value": (Ms / 2) * h.nnz * 8 / sec / 1e9, "unit": "Gnnz*vec/s", "cores": 1, "kind": "port",
+               "sample": "the same flake and 8 complex128 vectors, %d moments, 1 thread (the reference's DOS "
+                         "runs one batch of 8 vectors on one thread)" % Ms}
+    _line(args, "KPM DOS (complex128) Gnnz*vec/s", work / (t / args.steps) / 1e9, "Gnnz*vec/s", True,
+          t / args.steps,
+          {"workload": "graphene DOS: 60k sites complex128, 8 random-phase vectors, 2048 moments, 1000 energies",
+           "sites": int(h.shape[0]), "nnz": int(h.nnz), "moments": int(M), "broadening_eV": broadening,
+           "l2": "L2-resident working set (matrix ~4 MB, vectors 8 x 1 MB): latency-bound, no flush"},
+          "c128",
+          roofline={"bound": "l2 (latency)", "achieved": achieved, "unit": "GB/s",
+                    "note": "working set fits in L2; HBM fraction not meaningful",
+                    "avg_launch_us": rec / launches * 1e6, "alg_bytes_per_launch": alg},
+          e2e={"value": work / (wall / args.steps) / 1e9, "unit": "Gnnz*vec/s", "h2d_bytes_per_step": 8000,
+               "d2h_bytes_per_step": 8000},
+          cpu_baseline=cpu, clocks=clk, time_per_dos_ms=t / args.steps * 1e3,
+          gpu_launches=int(args.steps * (launches + 4)))
+
+
+def workload_conductivity(args, stream_of):
+    """Kubo-Bastin sigma_xx: 1M-site graphene under 20 T (Peierls phases, complex128), velocity
+    from bond x-displacements, 16 random-phase vectors, 512 moments, Jackson; mu_mn on the tensor
+    cores (tcgen05 TF32 three-product split of FP32 planes)."""
+    from pybinding_gb300 import _native, lattice as L
+    m = L.graphene_flake(1_000_000, hopping_modifiers=[L.constant_magnetic_field(20.0)], is_complex=True,
+                         is_double=True)
+    h = m.hamiltonian.astype(np.complex128)
+    x = m.system.x
+    eng = _native.Engine(h, _native.make_config(energy_range=(-9.0, 9.0)))
+    a, b = eng.scaling_factors()
+    broadening = _jackson_broadening(512, a)
+    chem = np.linspace(-1.5, 1.5, 31)
+    stream = stream_of(eng)
+    t, wall, clk, outs = _timed(lambda: eng.calc_conductivity(x, x, chem, broadening, 0.0, 16, 1000, gemm_mode=1),
+                                args.steps, args.warmup, stream)
+    st = eng.stats()
+    M = st.num_moments
+    n = h.shape[0]
+    I = n * 16
+    useful = 8.0 * M * M * I
+    tensor = 3 * useful  # hi*hi + hi*lo + lo*hi
+    peaks = _peaks()
+    peak_tf32 = float(peaks.get("bf16_tflops", 1900.0)) / 2
+    gemm = st.gemm_time
+    rec = st.moments_time - gemm
+    rec_work = 2 * M * h.nnz * 16
+    _line(args, "Kubo-Bastin sigma_xx time per call (1M sites, 16 vectors, 512 moments)", t / args.steps, "s",
+          False, t / args.steps,
+          {"workload": "conductivity: 1M-site graphene, 20 T, complex128, 16 vectors, 512 moments, tensor-core mu_mn",
+           "sites": int(n), "nnz": int(h.nnz), "moments": int(M), "vectors": 16, "broadening_eV": broadening,
+           "gemm": "tcgen05 kind::tf32, hi/lo split (3 products), FP32 planes, FP64 slice sums"},
+          "c128 recursion, tf32x3 GEMM",
+          roofline={"bound": "tensor", "achieved": tensor / gemm / 1e12, "peak": peak_tf32, "unit": "TFLOP/s",
+                    "frac": tensor / gemm / 1e12 / peak_tf32, "traffic": None,
+                    "kernel": "mu_gemm_tc_kernel<true>",
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops / 2 (dense TF32 runs at half the BF16 rate)",
+                    "useful_tflops": useful / gemm / 1e12},
+          breakdown={"recursion_s": rec, "recursion_gnnz_vec_per_s": rec_work / rec / 1e9, "gemm_s": gemm,
+                     "reconstruction_and_host_s": t / args.steps - st.moments_time},
+          e2e={"value": wall / args.steps, "unit": "s", "h2d_bytes_per_step": int(8 * n + 8 * 31),
+               "d2h_bytes_per_step": int(16 * 31)},
+          sigma_sample=[float(v.real) for v in outs[-1][:5]], clocks=clk,
+          gpu_launches=int(args.steps * (2 * (M + 2) + 6)))
+
+
+def workload_adjoint(args, stream_of):
+    """DOS-misfit gradient on 256k-site strained graphene (t_ij = -2.8 exp(-3.37 (d/a_cc - 1)),
+    sinusoidal strain 5 %, period 20 nm), 32 Rademacher vectors, 1024 moments, FP32 recursion;
+    target DOS from a 3 % strain. One step = forward moments + adjoint gradient (onsite + bonds)."""
+    from pybinding_gb300 import _native, jackson_kernel, lattice as L
+    from pybinding_gb300.adjoint import DiagonalMoments, moments_weights
+
+    def flake(amp):
+        return L.graphene_flake(256_000, hopping_modifiers=[L.strained_hopping(L.sinusoidal_strain(amp, 20.0))],
+                                is_double=True)
+    m = flake(0.05)
+    h = m.hamiltonian.tocsr()
+    h.sort_indices()
+    n = h.shape[0]
+    rng = np.random.default_rng(3)
+    r0 = np.where(rng.integers(0, 2, (32, n)) == 0, -1.0, 1.0)
+    rng_e = (-9.5, 9.5)
+    op = DiagonalMoments(h, 1024, r0, rng_e, precision="fp32")
+    ht = flake(0.03).hamiltonian.tocsr()
+    ht.sort_indices()
+    tgt = DiagonalMoments(ht, 1024, r0, rng_e, precision="fp32")
+    energy = np.linspace(-8, 8, 400)
+    W = moments_weights(energy, op.scaling, jackson_kernel(), op.num_moments)
+    target = W @ tgt.moments(ht.data)
+    eng_stream = stream_of(op._engine)
+    times = {}
+
+    def step():
+        mu = op.moments(h.data)
+        times["fwd"] = op._engine.stats().moments_time
+        rho = W @ mu
+        dl_dmu = W.T @ (2 * (rho - target))
+        gv, go = op.gradient(h.data, dl_dmu)
+        times["bwd"] = op._engine.stats().moments_time
+        return float(np.sum((rho - target) ** 2)), gv, go
+
+    t, wall, clk, outs = _timed(step, args.steps, args.warmup, eng_stream)
+    M = op.num_moments
+    nnz = h.nnz
+    fwd_work = (M / 2) * nnz * 32
+    # backward (all vectors kept, the automatic choice here): recomputation + adjoint recursion
+    bwd_work = 2 * (M / 2) * nnz * 32
+    # the same with sqrt(M/2) checkpoints: one more forward pass, ~3 sqrt(M/2) vectors of memory
+    op.checkpoint = int(np.ceil(np.sqrt(M // 2)))
+    op.gradient(h.data, np.ones(M))
+    t_sqrt = op._engine.stats().moments_time
+    op.checkpoint = 0
+    _line(args, "adjoint DOS-misfit gradient time per forward+backward (256k sites, 32 vectors, 1024 moments)",
+          t / args.steps, "s", False, t / args.steps,
+          {"workload": "adjoint gradients: 256k-site strained graphene, 32 vectors, 1024 moments, fp32",
+           "sites": int(n), "nnz": int(nnz), "moments": int(M),
+           "checkpoint": "automatic (all vectors: they fit in HBM)"},
+          "f32 recursion, f64 gradient sums",
+          breakdown={"forward_s": times["fwd"], "forward_gnnz_vec_per_s": fwd_work / times["fwd"] / 1e9,
+                     "backward_s": times["bwd"], "backward_gnnz_vec_per_s": bwd_work / times["bwd"] / 1e9,
+                     "backward_over_forward": times["bwd"] / times["fwd"],
+                     "backward_sqrt_checkpoints_s": t_sqrt},
+          loss=outs[-1][0], grad_norm=float(np.linalg.norm(outs[-1][1])),
+          e2e={"value": wall / args.steps, "unit": "s", "h2d_bytes_per_step": int(2 * (8 * nnz + 4 * 32 * n)),
+               "d2h_bytes_per_step": int(8 * (nnz + n) + 8 * M)},
+          clocks=clk)
+
+
+def workload_anderson3d(args, stream_of):
+    """3D Anderson model: simple cubic 160^3 periodic, t = -1, onsite U[-8.25, 8.25], 256 Rademacher
+    vectors, 8192 moments (8194), FP32 vectors / FP64 sums; then LDOS at 4096 sites (1024 moments)."""
+    from pybinding_gb300 import _native, lattice as L
+    Lc = 160
+    rng = np.random.default_rng(5)
+    h = L.simple_cubic_periodic(Lc, onsite=rng.uniform(-8.25, 8.25, Lc ** 3).astype(np.float32)).hamiltonian
+    n = h.shape[0]
+    R = 256
+    eng = _native.Engine(h, _native.make_config())
+    eng.scaling_factors()
+    st = (rng.integers(0, 2, (R, n), dtype=np.int8) * 2 - 1).astype(np.float32)
+    import torch
+    d_st = torch.from_numpy(st.reshape(-1)).cuda()
+    stream = stream_of(eng)
+    t, wall, clk, _ = _timed(lambda: eng.moments_diag(8192, None, average=True, on_device_ptr=d_st.data_ptr(),
+                                                      num_vectors=R), args.steps, args.warmup, stream)
+    s = eng.stats()
+    M = s.num_moments
+    work = (M / 2) * h.nnz * R
+    fuse = int(s.steps_per_launch)
+    launches = 1 + (M // 2 - 1) // fuse
+    vec_bytes = (3 if fuse == 1 else 4) * n * R * 4
+    alg = h.nnz * 12 + 4 * (n + 1) + vec_bytes
+    avg = s.moments_time / launches
+    peak = float(_peaks().get("hbm_gbs", 6800.0))
+    sites = rng.choice(n, 4096, replace=False)
+    a, b = eng.scaling_factors()
+    t0 = time.perf_counter()
+    eng.calc_ldos(sites, np.linspace(-10, 10, 200), _jackson_broadening(1024, a))
+    t_ldos = time.perf_counter() - t0
+    _line(args, "KPM Gnnz*vec/s (3D Anderson, 256 vectors, 8192 moments, FP32)", work / (t / args.steps) / 1e9,
+          "Gnnz*vec/s", True, t / args.steps,
+          {"workload": "3D Anderson: simple cubic 160^3 periodic, W = 16.5, 256 vectors, 8192 moments",
+           "sites": int(n), "nnz": int(h.nnz), "moments": int(M), "vectors": R,
+           "l2": "inputs larger than L2 (no flush)"},
+          "f32",
+          roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",
+                    "frac": alg / avg / 1e9 / peak, "traffic": None, "steps_per_launch": fuse,
+                    "alg_bytes_per_launch": alg, "avg_launch_ms": avg * 1e3,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+          ldos_4096_sites_1024_moments_s=t_ldos, clocks=clk,
+          gpu_launches=int(args.steps * (launches + 3)))
+
+
+def run_workload(args, rank, world, local_rank):
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "workload": args.workload,
+                          "unavailable": "the reference arm is defined for the default workload; the CPU "
+                                         "baseline of this one is in its own line"}), flush=True)
+        return
+    if rank != 0:
+        return
+    import torch
+    torch.cuda.set_device(local_rank)
+
+    def stream_of(eng):
+        return torch.cuda.ExternalStream(eng.stream())
+    {"dos_c1": workload_dos_c1, "conductivity": workload_conductivity, "adjoint": workload_adjoint,
+     "anderson3d": workload_anderson3d}[args.workload](args, stream_of)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.workload != "dos_batch":
+        run_workload(args, rank, world, local_rank)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_gpu(args, rank, world, local_rank)

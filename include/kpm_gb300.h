@@ -65,6 +65,9 @@ typedef struct kpm_config {
     int32_t batch_width;      /* vectors per recursion block (upper bound); 0 = 256-byte rows */
     int32_t tile_rows;        /* rows per thread block tile; 0 = autotuned on the first call */
     int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, or 0 = chosen by timing */
+    int32_t staging;          /* diagonal step operands: 0 = chosen by timing, 1 = register loads,
+                                 2 = TMA bulk copies into shared memory (full-system recursions of
+                                 16-byte-lane shapes; others use register loads) */
 } kpm_config;
 
 /* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */
@@ -84,6 +87,10 @@ typedef struct kpm_stats {
     int32_t lanczos_loops;
     double eps;               /* opt_nnz * multiplier / moments_time */
     int32_t steps_per_launch; /* Chebyshev steps per recursion launch used last (1 or 2) */
+    double gemm_time;         /* seconds: device time of the conductivity's moments GEMM (0 otherwise) */
+    int32_t elems_per_lane;   /* recursion kernel lane mapping used last: vector elements per lane */
+    int32_t lanes_per_row;    /*   and lanes per matrix row (their product = vectors per block) */
+    int32_t staged_rows;      /*   0 = register loads, > 0 = TMA-staged tiles of this many rows */
 } kpm_stats;
 
 typedef struct kpm_engine kpm_engine;
@@ -196,7 +203,9 @@ int kpm_calc_conductivity(kpm_engine* engine, const float* left_coords, const fl
  * and dL/d(onsite energy) per site (out_grad_onsite: rows doubles, nullable; also where H
  * stores no diagonal). dl_dmu has round_num_moments(num_moments) entries. The scaling
  * (a, b) is held fixed. checkpoint: forward vectors are kept every `checkpoint` steps and
- * recomputed segment by segment; 0 = ceil(sqrt(M / 2)); >= M / 2 - 1 recomputes nothing. */
+ * recomputed segment by segment (memory ~ (2 M / checkpoint + checkpoint) vectors);
+ * >= M / 2 - 1 keeps the whole recursion (one forward pass fewer); 0 = the whole recursion
+ * when it fits in half the free device memory, else ceil(sqrt(M / 2)). */
 int kpm_adjoint_diag(kpm_engine* engine, int64_t num_moments, int64_t num_vectors, const void* starters,
                      const double* dl_dmu, int64_t checkpoint, double* out_grad_values, double* out_grad_onsite,
                      int64_t* num_moments_out);

@@ -22,6 +22,7 @@ SCALAR_CODE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1,
                np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
 KERNEL_CODE = {"jackson": 0, "lorentz": 1, "dirichlet": 2}
 PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2}
+STAGING_CODE = {"auto": 0, "registers": 1, "tma": 2}
 
 
 class Config(C.Structure):
@@ -29,7 +30,8 @@ class Config(C.Structure):
     _fields_ = [("min_energy", C.c_double), ("max_energy", C.c_double), ("kernel", C.c_int32),
                 ("kernel_param", C.c_double), ("matrix_format", C.c_int32), ("optimal_size", C.c_int32),
                 ("interleaved", C.c_int32), ("lanczos_precision", C.c_double), ("precision", C.c_int32),
-                ("batch_width", C.c_int32), ("tile_rows", C.c_int32), ("fuse_steps", C.c_int32)]
+                ("batch_width", C.c_int32), ("tile_rows", C.c_int32), ("fuse_steps", C.c_int32),
+                ("staging", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -38,7 +40,8 @@ class Stats(C.Structure):
                 ("opt_nnz", C.c_int64), ("vec", C.c_int64), ("opt_vec", C.c_int64), ("multiplier", C.c_double),
                 ("matrix_memory", C.c_int64), ("vector_memory", C.c_int64), ("hamiltonian_time", C.c_double),
                 ("moments_time", C.c_double), ("bounds_time", C.c_double), ("lanczos_loops", C.c_int32),
-                ("eps", C.c_double), ("steps_per_launch", C.c_int32)]
+                ("eps", C.c_double), ("steps_per_launch", C.c_int32), ("gemm_time", C.c_double),
+                ("elems_per_lane", C.c_int32), ("lanes_per_row", C.c_int32), ("staged_rows", C.c_int32)]
 
 
 # every exported symbol of include/kpm_gb300.h with (restype, argtypes)
@@ -107,7 +110,7 @@ def check(rc):
 
 def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, matrix_format="ELL",
                 optimal_size=True, interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0,
-                tile_rows=0, fuse_steps=0):
+                tile_rows=0, fuse_steps=0, staging="auto"):
     c = Config()
     lib().kpm_config_default(C.byref(c))
     c.min_energy, c.max_energy = float(energy_range[0]), float(energy_range[1])
@@ -121,6 +124,7 @@ def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, mat
     c.batch_width = int(batch_width)
     c.tile_rows = int(tile_rows)
     c.fuse_steps = int(fuse_steps)
+    c.staging = STAGING_CODE[staging]
     return c
 
 

@@ -46,7 +46,8 @@ class DiagonalMoments:
     starters: (num_vectors, rows) real array, site order.
     energy_range: (min, max) that fixes the scaling a, b (``Bounds.hpp:11-24``).
     precision: "fp64" (FP64 recursion) or "fp32" (FP32 vectors, FP64 moment sums).
-    checkpoint: forward vectors kept every ``checkpoint`` steps (0 = sqrt(M/2)).
+    checkpoint: forward vectors kept every ``checkpoint`` steps and recomputed per segment;
+        0 = all of them when they fit in half the free device memory, else sqrt(M/2).
     """
 
     def __init__(self, pattern, num_moments, starters, energy_range, precision="fp64", checkpoint=0):

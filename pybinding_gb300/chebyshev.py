@@ -117,7 +117,7 @@ class GpuImpl:
 
     def __init__(self, model, energy_range=(0, 0), kernel=None, matrix_format="ELL", optimal_size=True,
                  interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0, tile_rows=0,
-                 moments_gemm="fp64", **_):
+                 moments_gemm="fp64", staging="auto", **_):
         if moments_gemm not in ("fp64", "tensor"):
             raise ValueError("moments_gemm must be 'fp64' or 'tensor'")
         self.kernel = kernel if kernel is not None else jackson_kernel()
@@ -126,7 +126,7 @@ class GpuImpl:
                               kernel_param=self.kernel.param, matrix_format=matrix_format,
                               optimal_size=optimal_size, interleaved=interleaved,
                               lanczos_precision=lanczos_precision, precision=precision, batch_width=batch_width,
-                              tile_rows=tile_rows)
+                              tile_rows=tile_rows, staging=staging)
         self._model = model
         self._engine = _native.Engine(model.hamiltonian, _native.make_config(**self._cfg_args))
 
@@ -346,7 +346,7 @@ class KPMBatch:
                     kernel_param=self.kernel.param)
         args.update({k: v for k, v in kwargs.items() if k in ("matrix_format", "optimal_size", "interleaved",
                                                               "lanczos_precision", "precision", "batch_width",
-                                                              "tile_rows", "fuse_steps")})
+                                                              "tile_rows", "fuse_steps", "staging")})
         self.engine = _native.Engine(h, _native.make_config(**args), system_offsets=self.offsets)
 
     def scaling_factors(self):

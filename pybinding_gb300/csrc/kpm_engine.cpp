@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -29,6 +30,7 @@
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 using kpm::Tile;
@@ -254,6 +256,23 @@ std::string pretty_time(double s) {
     return buf;
 }
 
+// Runs f(0 .. count-1) on up to hardware_concurrency threads (host-side setup work).
+template<class F>
+void parallel_for(int64_t count, F&& f) {
+    int64_t const nt = std::max<int64_t>(1, std::min<int64_t>(count, std::thread::hardware_concurrency()));
+    if (nt <= 1) {
+        for (int64_t i = 0; i < count; ++i) f(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> pool;
+    for (int64_t t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+            for (int64_t i = next++; i < count; i = next++) f(i);
+        });
+    for (auto& th : pool) th.join();
+}
+
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -320,7 +339,25 @@ struct kpm_engine {
     double calc_time = 0;
     bool last_bounds_lanczos = false;
 
+    // The single-step recursion of the last diagonal call as a CUDA graph (one node per
+    // step), replayed while every pointer and size it captured is unchanged.
+    struct RecursionGraphKey {
+        void const *x0, *x1, *acc, *tiles, *col, *val;
+        int64_t half, bstride, step_acc;
+        int ntiles, vtype, E, LPR, nbatch, unroll, W, tma_rows;
+        int32_t row_limit;
+        int* error;
+        bool operator==(RecursionGraphKey const& o) const { return std::memcmp(this, &o, sizeof o) == 0; }
+    };
+    RecursionGraphKey graph_key{};
+    cudaGraphExec_t graph_exec = nullptr;
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+    }
+
     ~kpm_engine() {
+        drop_graph();
         if (ev_t0) cudaEventDestroy(ev_t0);
         if (ev_t1) cudaEventDestroy(ev_t1);
         if (ev0) cudaEventDestroy(ev0);
@@ -655,8 +692,9 @@ struct kpm_engine {
                 for (; j < W; ++j) col[r * W + j] = static_cast<int32_t>(r);
             }
             h_col = col;
-            d_col.ensure(col.size() * sizeof(int32_t));
-            d_val.ensure(val.size() * sizeof(Tc));
+            // 64 bytes of tail padding: bulk copies of a tile's entries round their size up to 16 bytes
+            d_col.ensure(col.size() * sizeof(int32_t) + 64);
+            d_val.ensure(val.size() * sizeof(Tc) + 64);
             KPM_CUDA(cudaMemcpyAsync(d_col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
             KPM_CUDA(cudaMemcpyAsync(d_val.p, val.data(), val.size() * sizeof(Tc), cudaMemcpyHostToDevice, stream));
             KPM_CUDA(cudaStreamSynchronize(stream));
@@ -722,45 +760,84 @@ struct kpm_engine {
     struct TuneKey {
         int vtype, E, LPR, nbatch;
         int64_t rows;
+        bool batch_outer;
         bool operator==(TuneKey const& o) const {
-            return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows;
+            return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows &&
+                   batch_outer == o.batch_outer;
         }
     };
-    struct Tuned { int rows_per_tile, unroll; };
+    struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; };
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
     std::vector<std::pair<TuneKey, FuseChoice>> fuse_tuned;
     std::vector<std::pair<TuneKey, Tuned>> tuned;
     std::vector<std::array<double, 3>> last_tuning;  // (rows per tile, unroll, ms) of the last tuning run
 
-    Tuned tune_diag(Shape sh, bool sys0, kpm::DiagStep base) {
-        TuneKey const key{vtype, sh.E, sh.LPR, sh.nbatch, rows};
+    Tuned tune_diag(Shape sh, bool sys0, bool batch_outer, kpm::DiagStep base) {
+        TuneKey const key{vtype, sh.E, sh.LPR, sh.nbatch, rows, batch_outer};
         for (auto const& t : tuned)
             if (t.first == key) return t.second;
-        int const rpp = 256 / sh.LPR;
-        Tuned best{rpp * 16, 1};
-        int64_t const work = rows * sh.K * sh.nbatch;
-        if (work >= (int64_t{1} << 22)) {  // small problems are latency bound: keep the default
+        Tuned best{(256 / sh.LPR) * 16, 1, sh.E, sh.LPR, 0};
+        // lane mappings of this K: the default (16 bytes per lane) and, when the row allows,
+        // half the elements per lane over twice the lanes
+        std::vector<std::pair<int, int>> maps{{sh.E, sh.LPR}};
+        if (sh.E > 1 && kpm::diag_step_supported(vtype, sh.E / 2, sh.LPR * 2)) maps.push_back({sh.E / 2, sh.LPR * 2});
+        {   // small problems (L2-resident, latency bound) want short tiles for parallelism,
+            // large ones taller tiles for fewer flushes: timed either way
             double best_ms = 1e30;
             last_tuning.clear();
-            for (int unroll : {1, 2})
-                for (int rpt : {4, 8, 16, 32, 64}) {
-                    if (rpt < 2 * unroll) continue;
-                    sh.rows_per_tile = rpp * rpt;
-                    base.num_tiles = build_tiles(sh, sys0);
+            for (auto const& mp : maps)
+                for (int unroll : {1, 2})
+                    for (int rpt : {1, 2, 4, 8, 16, 32, 64}) {
+                        if (rpt < 2 * unroll) continue;
+                        Shape t = sh;
+                        t.E = mp.first;
+                        t.LPR = mp.second;
+                        t.rows_per_tile = (256 / t.LPR) * rpt;
+                        base.E = t.E;
+                        base.LPR = t.LPR;
+                        base.num_tiles = build_tiles(t, sys0, batch_outer);
+                        base.tiles = d_tiles.as<Tile>();
+                        base.init = true;
+                        base.unroll = unroll;
+                        KPM_CUDA(kpm::launch_diag_step(base, stream));  // warm
+                        KPM_CUDA(cudaEventRecord(ev0, stream));
+                        for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
+                        KPM_CUDA(cudaEventRecord(ev1, stream));
+                        KPM_CUDA(cudaEventSynchronize(ev1));
+                        float ms = 0;
+                        KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+                        last_tuning.push_back({static_cast<double>(t.rows_per_tile), static_cast<double>(unroll), ms / 3});
+                        if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR, 0}; }
+                    }
+            // the TMA-staged kernel (full rows, 16-byte lanes): tile heights that fit in shared memory
+            if (cfg.staging != 1 && batch_outer && sh.E * kpm::vtype_bytes(vtype) == 16 && sh.LPR > 1 &&
+                base.error != nullptr)
+                for (int tr : {32, 64, 128}) {
+                    Shape t = sh;
+                    t.rows_per_tile = tr;
+                    base.E = sh.E;
+                    base.LPR = sh.LPR;
+                    base.num_tiles = build_tiles(t, sys0, batch_outer);
                     base.tiles = d_tiles.as<Tile>();
                     base.init = true;
-                    base.unroll = unroll;
-                    KPM_CUDA(kpm::launch_diag_step(base, stream));  // warm
+                    base.unroll = 1;
+                    base.tma_rows = tr;
+                    cudaError_t const le = kpm::launch_diag_step(base, stream);
+                    if (le != cudaSuccess) {  // e.g. too much shared memory for this height
+                        cudaGetLastError();
+                        continue;
+                    }
                     KPM_CUDA(cudaEventRecord(ev0, stream));
                     for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
                     KPM_CUDA(cudaEventRecord(ev1, stream));
                     KPM_CUDA(cudaEventSynchronize(ev1));
                     float ms = 0;
                     KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                    last_tuning.push_back({static_cast<double>(sh.rows_per_tile), static_cast<double>(unroll), ms / 3});
-                    if (ms < best_ms) { best_ms = ms; best = Tuned{sh.rows_per_tile, unroll}; }
+                    last_tuning.push_back({static_cast<double>(tr), -1.0, ms / 3});
+                    if (ms < best_ms) { best_ms = ms; best = Tuned{tr, 1, sh.E, sh.LPR, tr}; }
                 }
+            base.tma_rows = 0;
         }
         tuned.push_back({key, best});
         return best;
@@ -853,14 +930,26 @@ struct kpm_engine {
         return ++pair_seq;
     }
 
-    int build_tiles(Shape const& sh, bool sys0_only) {
+    // Tiles of (rows, system, batch). Batch innermost ([tile][batch]) lets a shrinking row
+    // limit cut the list at a tile boundary; batch outermost makes the persistent blocks sweep
+    // one batch at a time, so the gathered x rows that must stay in L2 belong to one batch
+    // (3D lattices: neighbours lie a whole BFS shell away).
+    int build_tiles(Shape const& sh, bool sys0_only, bool batch_outer = false) {
         std::vector<Tile> tiles;
         int const ns = sys0_only ? 1 : nsys;
-        for (int s = 0; s < ns; ++s)
-            for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += sh.rows_per_tile)
-                for (int b = 0; b < sh.nbatch; ++b)
-                    tiles.push_back({static_cast<int32_t>(r),
-                                     static_cast<int32_t>(std::min(sys_off[s + 1], r + sh.rows_per_tile)), s, b});
+        auto add = [&](int s, int64_t r, int b) {
+            tiles.push_back({static_cast<int32_t>(r), static_cast<int32_t>(std::min(sys_off[s + 1], r + sh.rows_per_tile)),
+                             s, b});
+        };
+        if (batch_outer) {
+            for (int b = 0; b < sh.nbatch; ++b)
+                for (int s = 0; s < ns; ++s)
+                    for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += sh.rows_per_tile) add(s, r, b);
+        } else {
+            for (int s = 0; s < ns; ++s)
+                for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += sh.rows_per_tile)
+                    for (int b = 0; b < sh.nbatch; ++b) add(s, r, b);
+        }
         d_tiles.ensure(sizeof(Tile) * tiles.size());
         KPM_CUDA(cudaMemcpyAsync(d_tiles.p, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream));
         return static_cast<int>(tiles.size());
@@ -887,7 +976,8 @@ struct kpm_engine {
         size_t const step_acc = static_cast<size_t>(ns) * sh.nbatch * sh.K * NV;
         d_acc.ensure(sizeof(double) * step_acc * half);
         d_mu.ensure(sizeof(double) * 2 * ns * nvec * M);
-        int ntiles = build_tiles(sh, sys0);
+        bool const batch_outer = !opt_rows;
+        int ntiles = build_tiles(sh, sys0, batch_outer);
 
         KPM_CUDA(cudaMemsetAsync(d_x0.p, 0, vbytes, stream));
         if (units) {
@@ -921,14 +1011,35 @@ struct kpm_engine {
         a.x = d_x0.p;
         a.y = d_x1.p;
         a.acc = d_acc.as<double>();
-        if (cfg.tile_rows > 0) {
+        bool alt_map = false;  // a thinner lane mapping or the TMA-staged kernel: single-step launches only
+        d_pair_error.ensure(sizeof(int));
+        KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
+        a.error = d_pair_error.as<int>();
+        bool const tma_ok = batch_outer && sh.E * vb == 16 && sh.LPR > 1;
+        if (cfg.staging == 2 && tma_ok) {
+            sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 64;
+            a.tma_rows = sh.rows_per_tile;
+            alt_map = true;
+        } else if (cfg.tile_rows > 0) {
             sh.rows_per_tile = cfg.tile_rows;
         } else {
-            Tuned const tu = tune_diag(sh, sys0, a);
+            Tuned const tu = tune_diag(sh, sys0, batch_outer, a);
             sh.rows_per_tile = tu.rows_per_tile;
             a.unroll = tu.unroll;
+            alt_map = tu.E != sh.E || tu.tma_rows > 0;
+            if (alt_map && cfg.fuse_steps == 2 && !opt_rows) {  // two-step launches asked for: default kernel
+                alt_map = false;
+                sh.rows_per_tile = (256 / sh.LPR) * 16;
+                a.unroll = 1;
+            } else {
+                sh.E = tu.E;
+                sh.LPR = tu.LPR;
+                a.tma_rows = tu.tma_rows;
+            }
+            a.E = sh.E;
+            a.LPR = sh.LPR;
         }
-        ntiles = build_tiles(sh, sys0);
+        ntiles = build_tiles(sh, sys0, batch_outer);
         a.tiles = d_tiles.as<Tile>();
         a.num_tiles = ntiles;
         KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
@@ -960,8 +1071,6 @@ struct kpm_engine {
         };
         // two steps per launch: P = r0 (T_{n-2} -> T_n), Q = r1 (T_{n-1} -> T_{n+1}); the
         // roles are unchanged after the pair, so no swap
-        d_pair_error.ensure(sizeof(int));
-        KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
         int64_t const max_pairs = std::max<int64_t>(1, half / 2);
         d_pair_counters.ensure(sizeof(unsigned) * max_pairs);
         KPM_CUDA(cudaMemsetAsync(d_pair_counters.p, 0, sizeof(unsigned) * max_pairs, stream));
@@ -993,9 +1102,9 @@ struct kpm_engine {
             n += 2;
         };
         int const rpp = 256 / sh.LPR;
-        bool const can_pair = !opt_rows && cfg.fuse_steps != 1;
+        bool const can_pair = !opt_rows && cfg.fuse_steps != 1 && !alt_map;
         FuseChoice choice{1, 0};
-        TuneKey const fkey{vtype, sh.E, sh.LPR, sh.nbatch, rows};
+        TuneKey const fkey{vtype, sh.E, sh.LPR, sh.nbatch, rows, batch_outer};
         bool have_choice = false;
         for (auto const& f : fuse_tuned)
             if (f.first == fkey) { choice = f.second; have_choice = true; }
@@ -1031,8 +1140,56 @@ struct kpm_engine {
             PairPlan* pp = pair_plan(sh, choice.rows_per_tile);
             while (n + 1 <= half) pair_step(pp);
         }
+        if (n == 2 && half >= 3 && !opt_rows) {
+            // steady state (no tuning steps ran in this call): replay the captured recursion
+            RecursionGraphKey key{};
+            std::memset(&key, 0, sizeof key);  // padding bytes take part in the comparison
+            key.x0 = d_x0.p;
+            key.x1 = d_x1.p;
+            key.acc = d_acc.p;
+            key.tiles = a.tiles;
+            key.col = a.col;
+            key.val = a.val;
+            key.half = half;
+            key.bstride = bstride;
+            key.step_acc = static_cast<int64_t>(step_acc);
+            key.ntiles = a.num_tiles;
+            key.vtype = vtype;
+            key.E = sh.E;
+            key.LPR = sh.LPR;
+            key.nbatch = sh.nbatch;
+            key.unroll = a.unroll;
+            key.W = W;
+            key.row_limit = a.row_limit;
+            key.tma_rows = a.tma_rows;
+            key.error = a.error;
+            if (graph_exec == nullptr || !(key == graph_key)) {
+                drop_graph();
+                KPM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                cudaGraph_t g = nullptr;
+                try {
+                    while (n <= half) single_step();
+                } catch (...) {
+                    cudaStreamEndCapture(stream, &g);
+                    if (g) cudaGraphDestroy(g);
+                    throw;
+                }
+                KPM_CUDA(cudaStreamEndCapture(stream, &g));
+                cudaError_t const ie = cudaGraphInstantiate(&graph_exec, g, 0);
+                cudaGraphDestroy(g);
+                if (ie != cudaSuccess) {
+                    graph_exec = nullptr;
+                    KPM_CUDA(ie);
+                }
+                std::memcpy(&graph_key, &key, sizeof key);  // padding included
+            } else {
+                n = half + 1;
+            }
+            KPM_CUDA(cudaGraphLaunch(graph_exec, stream));
+        }
         while (n <= half) single_step();
         last_fuse = choice.steps;
+        last_tma_rows = a.tma_rows;
         KPM_CUDA(cudaEventRecord(ev1, stream));
         KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
                                           d_mu.as<double>(), stream));
@@ -1040,20 +1197,22 @@ struct kpm_engine {
         KPM_CUDA(cudaMemcpyAsync(&pair_err, d_pair_error.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         KPM_CUDA(cudaStreamSynchronize(stream));
         if (pair_err)
-            fail(KPM_ERR_TIMEOUT, "a two-step recursion launch gave up waiting for a neighbouring tile; results discarded");
+            fail(KPM_ERR_TIMEOUT, "a recursion launch gave up waiting (a neighbouring tile of a two-step launch, or "
+                                  "a staged copy); results discarded");
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         st.moments_time = ms * 1e-3;
         last_shape = sh;
     }
     Shape last_shape{};
-    double last_gemm_time = 0;
     int last_fuse = 1;
+    int last_tma_rows = 0;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
 
     void reset_stats(int64_t M, bool diagonal, bool opt, double multiplier, int64_t active_rows_nnz_rows) {
         (void)active_rows_nnz_rows;
         st.num_moments = M;
+        st.gemm_time = 0;
         st.multiplier = multiplier;
         int64_t const ell_nnz = rows * W;
         st.uses_full_system = static_cast<int32_t>(static_cast<int64_t>(slices.size()) < M / 2);
@@ -1079,6 +1238,9 @@ struct kpm_engine {
     void finish_stats() {
         st.eps = st.moments_time > 0 ? st.multiplier * st.opt_nnz / st.moments_time : 0.0;
         st.steps_per_launch = last_fuse;
+        st.elems_per_lane = last_shape.E;
+        st.lanes_per_row = last_shape.LPR;
+        st.staged_rows = last_tma_rows;
     }
 
     // ---------------------------------------------------------------- reconstruction
@@ -1132,6 +1294,7 @@ void kpm_config_default(kpm_config* c) {
     c->batch_width = 0;
     c->tile_rows = 0;
     c->fuse_steps = 0;
+    c->staging = 0;
 }
 
 int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const int32_t* indices, const void* values,
@@ -1151,6 +1314,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
+        if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
         *out = e.release();
     });
@@ -1607,29 +1771,33 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
                         if (vs == 2) o[1] = from_cd<Tc>(vrv - to_cd(hi));
                     });
                 }
-            // both starters own a default-seeded generator, so left and right draw the same r
+            // both starters own a default-seeded generator, so left and right draw the same r;
+            // the draws stay in the reference's order (one sequence over vectors, then sites),
+            // the rest (phases, the left velocity product) runs in parallel over vectors
             std::mt19937 gen;
             std::uniform_real_distribution<R> dist;
+            std::vector<R> draws(static_cast<size_t>(num_random) * n);
+            for (auto& d : draws) d = dist(gen);
             auto* sl = reinterpret_cast<T*>(starters_l.data());
             auto* sr = reinterpret_cast<T*>(starters_r.data());
-            std::vector<T> rv(n);
-            for (int64_t v = 0; v < num_random; ++v) {
+            parallel_for(num_random, [&](int64_t v) {
+                T* rv = sr + v * n;
+                R const* dv = draws.data() + static_cast<size_t>(v) * n;
                 for (int64_t i = 0; i < n; ++i) {
                     if constexpr (is_cplx_v<T>) {
                         std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
                         std::complex<R> const kk(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
-                        rv[i] = std::exp(kk * dist(gen));
+                        rv[i] = std::exp(kk * dv[i]);
                     } else {
-                        rv[i] = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
+                        rv[i] = (dv[i] < 0.5f) ? R(-1.f) : R(1.f);
                     }
                 }
                 for (int64_t r = 0; r < n; ++r) {
                     T acc = T(0);
                     for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) acc += vl[k] * rv[e->indices[k]];
                     sl[v * n + r] = acc;
-                    sr[v * n + r] = rv[r];
                 }
-            }
+            });
         });
         // device buffers
         size_t const vec_bytes = static_cast<size_t>(n) * K * vb;
@@ -1768,7 +1936,7 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         e->st.moments_time = rec_time + gemm_time;
         e->reset_stats(M, false, false, static_cast<double>(num_random) * 2, 0);
         e->finish_stats();
-        e->last_gemm_time = gemm_time;
+        e->st.gemm_time = gemm_time;
         e->calc_time = now_s() - t0;
     });
 }
@@ -1798,18 +1966,28 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         double const t0 = now_s();
         int64_t const M = round_moments(num_moments);
         int64_t const N = M / 2;
-        // segment length: at least 2 (a checkpoint pair is two consecutive vectors)
-        int64_t const seg_len = std::max<int64_t>(
-            2, std::min<int64_t>(checkpoint > 0 ? checkpoint
-                                                : static_cast<int64_t>(std::ceil(std::sqrt(static_cast<double>(N)))),
-                                 N - 1));
-        int64_t const nseg = N >= 2 ? (N - 2) / seg_len + 1 : 0;  // segments cover k = 1 .. N-1
         e->optimize({0}, {0});
         auto const sc = e->scale(0);
         int64_t const n = e->rows;
         int const vt = e->vtype;
         int const vb = kpm::vtype_bytes(vt);
         int const W = e->W;
+        kpm_engine::Shape sh = e->pick_shape(num_vectors);
+        int64_t const K = sh.K;
+        size_t const vec = static_cast<size_t>(n) * K * vb;
+        // segment length: at least 2 (a checkpoint pair is two consecutive vectors). Automatic:
+        // the whole recursion when it fits in half the free memory (no checkpoint pass), else
+        // sqrt(M / 2) (memory ~ 3 sqrt(M / 2) vectors, one extra forward pass)
+        int64_t want = checkpoint;
+        if (want == 0) {
+            size_t free_b = 0, total_b = 0;
+            KPM_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            want = static_cast<double>(N + 6) * vec <= 0.5 * static_cast<double>(free_b)
+                       ? N
+                       : static_cast<int64_t>(std::ceil(std::sqrt(static_cast<double>(N))));
+        }
+        int64_t const seg_len = std::max<int64_t>(2, std::min<int64_t>(want, N - 1));
+        int64_t const nseg = N >= 2 ? (N - 2) / seg_len + 1 : 0;  // segments cover k = 1 .. N-1
         double const R = static_cast<double>(num_vectors);
         std::vector<double> alpha(N + 2, 0.0), beta(N + 2, 0.0);
         for (int64_t k = 1; k <= N - 1; ++k) alpha[k] = 2.0 * dl_dmu[2 * k] / R;
@@ -1818,11 +1996,8 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         for (int64_t k = 2; k <= N; ++k) c1 -= dl_dmu[2 * k - 1];
         c1 /= R;
 
-        kpm_engine::Shape sh = e->pick_shape(num_vectors);
-        int64_t const K = sh.K;
         sh.nbatch = 1;
         int const ntiles = e->build_tiles(sh, true);
-        size_t const vec = static_cast<size_t>(n) * K * vb;
         // checkpoint pairs, segment vectors v_{c+2} .. v_{c+seg_len+1}, two adjoint vectors,
         // two rolling forward vectors
         DBuf d_ck, d_seg, d_lam, d_roll, d_gt, d_gd;

@@ -25,6 +25,7 @@
 // of the columns. At the end of the slice the registers go to mu with FP64 atomics.
 // mbarriers: full/converted/empty per stage, done/free per accumulator; every wait is
 // bounded by a clock limit and also ends once any CTA has flagged an error.
+#include "kpm_async.cuh"
 #include "kpm_internal.h"
 
 #include <cuda.h>
@@ -45,59 +46,13 @@ constexpr int THREADS = 320;
 constexpr int CONVERTERS = 256;      // warps 2..9, two per TMEM lane quarter
 constexpr int KB_MAX = 256;          // K blocks per CTA at most (the rest goes to FP64 atomics)
 constexpr uint32_t TILE_BYTES = TM * TK * 4;  // 8 KB, TM == TN
-constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
-__device__ __forceinline__ uint32_t smem_u32(void const* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* err) {
-    uint32_t const a = smem_u32(b);
-    long long const t0 = clock64();
-    for (unsigned spin = 1;; ++spin) {
-        uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return true;
-        if ((spin & 63u) == 0 && *reinterpret_cast<int volatile*>(err) != 0) return false;  // another CTA gave up
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicExch(err, 1);
-            return false;
-        }
-    }
-}
-
-// Wait for asynchronous work of this CTA (copies, MMAs) before it leaves, also after an
-// error elsewhere; still bounded.
-__device__ __forceinline__ void mbar_drain(uint64_t* b, uint32_t parity, int* err) {
-    uint32_t const a = smem_u32(b);
-    long long const t0 = clock64();
-    for (;;) {
-        uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return;
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicExch(err, 2);
-            return;
-        }
-    }
-}
+using async::mbar_arrive;
+using async::mbar_drain;
+using async::mbar_expect_tx;
+using async::mbar_init;
+using async::mbar_wait;
+using async::smem_u32;
 
 __device__ __forceinline__ void tma_load_2d(void* dst, CUtensorMap const* map, uint64_t* bar, int x, int y) {
     asm volatile(
@@ -191,7 +146,7 @@ mu_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_ar, const __grid_const
             mbar_init(gfree + b, CONVERTERS);
         }
         mbar_init(drain, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        async::mbar_init_fence();
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),

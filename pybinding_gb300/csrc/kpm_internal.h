@@ -42,6 +42,9 @@ struct DiagStep {
     double* acc;
     bool init;
     int unroll = 1;           // rows per thread per iteration (1 or 2), chosen by the autotuner
+    int tma_rows = 0;         // > 0: TMA-staged kernel, tiles of at most this many rows (full rows only,
+                              // K * element size a multiple of 16 bytes; col/val padded by 32 bytes)
+    int* error = nullptr;     // TMA-staged kernel: set when a bounded wait gives up
 };
 
 // Off-diagonal step: y <- H~ x - y (or H~ x / 2 when init), optional fused dot
@@ -169,6 +172,8 @@ cudaError_t launch_adj_step(AdjStep const& a, cudaStream_t s);
 cudaError_t launch_axpby(int vtype, int64_t n, double a, void const* x, double b, void const* y, void* out,
                          cudaStream_t s);
 bool diag_shape_supported(int vtype, int E, int LPR);
+// diag_step_kernel instantiations, thinner lane mappings included (what launch_diag_step runs)
+bool diag_step_supported(int vtype, int E, int LPR);
 
 // moments from the accumulated sums: out[(s*nbatch*K + v) * M + n] complex double,
 // or averaged over `nvec` vectors per system into out[s * M + n] when average.

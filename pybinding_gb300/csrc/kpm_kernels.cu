@@ -19,6 +19,7 @@
 // still FP32), and one FP64 atomic add per (block, vector, sum) lands in a
 // per-step FP64 accumulator. Per-element FP64 work is avoided on purpose:
 // GB300's FP64 rate is ~1/300 of its FP32 rate.
+#include "kpm_async.cuh"
 #include "kpm_internal.h"
 
 #include <algorithm>
@@ -308,6 +309,264 @@ diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
         diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
 }
 
+// ------------------------------------------------------------------ diagonal step, TMA-staged
+// The contiguous operands of a tile (its y_old rows, its own x rows for the moment dots,
+// and its ELL indices and values) are prefetched into shared memory by bulk copies, up to
+// TMA_STAGES tiles ahead of the consumers (one producer warp, a ring of stages, full/empty
+// mbarriers). The consumer warps only gather the neighbour x rows from global memory (L2)
+// and stream y_new out. Bulk copies keep far more bytes in flight per SM than register
+// loads, which is what this latency-bound step lacks. Starts of the index and value
+// copies are aligned down to 16 bytes (the consumer skips the lead-in), sizes rounded up
+// (the matrix arrays carry tail padding for that).
+constexpr int TMA_THREADS = 512;
+constexpr int TMA_CONSUMERS = TMA_THREADS - 32;
+constexpr int TMA_STAGES = 3;
+
+struct TmaLayout {
+    uint32_t y, x, col, val, stage;
+};
+__host__ __device__ inline TmaLayout tma_layout(int TR, int K, int vb, int W, int VS) {
+    auto up = [](uint32_t v) { return (v + 127u) & ~127u; };
+    TmaLayout L;
+    L.y = 0;
+    L.x = up(static_cast<uint32_t>(TR * K * vb));
+    L.col = L.x + up(static_cast<uint32_t>(TR * K * vb));
+    L.val = L.col + up(static_cast<uint32_t>(TR * W * 4 + 32));
+    L.stage = L.val + up(static_cast<uint32_t>(TR * W * VS * vb + 32));
+    return L;
+}
+
+template<class V, int E, int LPR>
+size_t diag_tma_smem(int TR, int W) {
+    using R = typename Tr<V>::R;
+    constexpr int NV = Tr<V>::C ? 3 : 2;
+    TmaLayout const L = tma_layout(TR, E * LPR, sizeof(V), W, Tr<V>::VS);
+    return static_cast<size_t>(TMA_STAGES) * L.stage + 2 * TMA_STAGES * sizeof(uint64_t) +
+           sizeof(R) * (TMA_CONSUMERS / 32) * E * LPR * NV + 128;
+}
+
+template<class V, int E, int LPR>
+__device__ __forceinline__ void tma_flush(typename Tr<V>::R (&m2)[E], typename Tr<V>::R (&m3r)[E],
+                                          typename Tr<V>::R (&m3i)[E], typename Tr<V>::R* red, double* a, bool live) {
+    using R = typename Tr<V>::R;
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int NV = CPLX ? 3 : 2;
+    constexpr int CW = TMA_CONSUMERS / 32;
+#pragma unroll
+    for (int off = LPR; off < 32; off <<= 1) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            m2[e] += __shfl_xor_sync(0xffffffffu, m2[e], off);
+            m3r[e] += __shfl_xor_sync(0xffffffffu, m3r[e], off);
+            if (CPLX) m3i[e] += __shfl_xor_sync(0xffffffffu, m3i[e], off);
+        }
+    }
+    int const ct = threadIdx.x - 32;
+    int const cw = ct / 32, wl = ct % 32;
+    asm volatile("bar.sync 1, %0;" ::"n"(TMA_CONSUMERS) : "memory");  // the previous flush has read `red`
+    if (wl < LPR) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            R* rw = red + (cw * K + wl * E + e) * NV;
+            rw[0] = m2[e];
+            rw[1] = m3r[e];
+            if (CPLX) rw[NV - 1] = m3i[e];
+        }
+    }
+    asm volatile("bar.sync 1, %0;" ::"n"(TMA_CONSUMERS) : "memory");
+    if (live)
+        for (int i = ct; i < K * NV; i += TMA_CONSUMERS) {
+            R sum = R(0);
+#pragma unroll
+            for (int w = 0; w < CW; ++w) sum += red[w * K * NV + i];
+            atomicAdd(a + i, static_cast<double>(sum));
+        }
+#pragma unroll
+    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+}
+
+template<class V, int E, int LPR, bool INIT>
+__global__ void __launch_bounds__(TMA_THREADS, 2)
+diag_tma_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x_all,
+                V* __restrict__ y_all, int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles, int nbatch,
+                double* __restrict__ acc, int TR, int* __restrict__ err) {
+    using R = typename Tr<V>::R;
+    using P = Pack<V, E>;
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int VS = Tr<V>::VS;
+    constexpr int NV = CPLX ? 3 : 2;
+    constexpr int RPP = TMA_CONSUMERS / LPR;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t{127});
+    TmaLayout const L = tma_layout(TR, K, sizeof(V), W, VS);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + TMA_STAGES * L.stage);
+    uint64_t* empty = full + TMA_STAGES;
+    R* red = reinterpret_cast<R*>(empty + TMA_STAGES);
+    int const G = gridDim.x;
+    int const my_tiles = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + G - 1) / G : 0;
+    int const warp = threadIdx.x / 32;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TMA_STAGES; ++s) {
+            async::mbar_init(full + s, 1);
+            async::mbar_init(empty + s, TMA_CONSUMERS / 32);
+        }
+        async::mbar_init_fence();
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+        if (threadIdx.x == 0) {  // producer
+            int issued = 0;
+            for (int i = 0; i < my_tiles; ++i) {
+                int const s = i % TMA_STAGES, use = i / TMA_STAGES;
+                if (use > 0 && !async::mbar_wait(empty + s, (use - 1) & 1, err)) break;
+                Tile const t = tiles[blockIdx.x + i * G];
+                int const rows = t.row_end - t.row_begin;
+                unsigned char* st = sm + s * L.stage;
+                uint32_t const vbytes = static_cast<uint32_t>(rows) * K * sizeof(V);
+                auto const* cb = reinterpret_cast<unsigned char const*>(col + static_cast<int64_t>(t.row_begin) * W);
+                auto const* ce = reinterpret_cast<unsigned char const*>(col + static_cast<int64_t>(t.row_end) * W);
+                auto const* c0 = reinterpret_cast<unsigned char const*>(reinterpret_cast<uintptr_t>(cb) & ~uintptr_t{15});
+                uint32_t const cbytes = static_cast<uint32_t>(((ce - c0) + 15) & ~15);
+                auto const* vb = reinterpret_cast<unsigned char const*>(val + static_cast<int64_t>(t.row_begin) * W * VS);
+                auto const* ve = reinterpret_cast<unsigned char const*>(val + static_cast<int64_t>(t.row_end) * W * VS);
+                auto const* v0 = reinterpret_cast<unsigned char const*>(reinterpret_cast<uintptr_t>(vb) & ~uintptr_t{15});
+                uint32_t const valbytes = static_cast<uint32_t>(((ve - v0) + 15) & ~15);
+                int64_t const vo = t.batch * batch_stride + static_cast<int64_t>(t.row_begin) * K;
+                async::mbar_expect_tx(full + s, (INIT ? 0u : vbytes) + vbytes + cbytes + valbytes);
+                if (!INIT) async::bulk_load(st + L.y, y_all + vo, vbytes, full + s);
+                async::bulk_load(st + L.x, x_all + vo, vbytes, full + s);
+                async::bulk_load(st + L.col, c0, cbytes, full + s);
+                async::bulk_load(st + L.val, v0, valbytes, full + s);
+                issued = i + 1;
+            }
+            // copies still in flight land before the block exits (already true without an error)
+            for (int i = issued - TMA_STAGES < 0 ? 0 : issued - TMA_STAGES; i < issued; ++i)
+                async::mbar_drain(full + i % TMA_STAGES, (i / TMA_STAGES) & 1, err);
+        }
+        return;
+    }
+
+    // consumers: every one of them runs the same sequence of flushes (named barriers), also
+    // after an error, in which case the rows are skipped
+    int const ct = threadIdx.x - 32;
+    int const lane = ct % LPR;
+    int const slot = ct / LPR;
+    R m2[E], m3r[E], m3i[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+    int cur_sys = -1, cur_batch = -1;
+    bool ok = true;
+    for (int i = 0; i < my_tiles; ++i) {
+        int const s = i % TMA_STAGES, use = i / TMA_STAGES;
+        Tile const t = tiles[blockIdx.x + i * G];
+        if (t.system != cur_sys || t.batch != cur_batch) {
+            if (cur_sys >= 0)
+                tma_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV, ok);
+            cur_sys = t.system;
+            cur_batch = t.batch;
+        }
+        ok = ok && async::mbar_wait(full + s, use & 1, err);
+        if (ok) {
+            unsigned char const* st = sm + s * L.stage;
+            V const* ys = reinterpret_cast<V const*>(st + L.y);
+            V const* xs = reinterpret_cast<V const*>(st + L.x);
+            uintptr_t const cb = reinterpret_cast<uintptr_t>(col + static_cast<int64_t>(t.row_begin) * W);
+            int32_t const* cs = reinterpret_cast<int32_t const*>(st + L.col + (cb & 15));
+            uintptr_t const vb = reinterpret_cast<uintptr_t>(val + static_cast<int64_t>(t.row_begin) * W * VS);
+            V const* vs = reinterpret_cast<V const*>(st + L.val + (vb & 15));
+            V const* __restrict__ x = x_all + t.batch * batch_stride;
+            V* __restrict__ y = y_all + t.batch * batch_stride;
+            int const rows = t.row_end - t.row_begin;
+            for (int lr = slot; lr < rows; lr += RPP) {
+                P const xr = reinterpret_cast<P const*>(xs + static_cast<int64_t>(lr) * K)[lane];
+                P yo;
+                if (!INIT) yo = reinterpret_cast<P const*>(ys + static_cast<int64_t>(lr) * K)[lane];
+                V sum[E], lo[E];
+#pragma unroll
+                for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(lo[e]); }
+                for (int j0 = 0; j0 < W; j0 += 4) {
+                    int32_t c[4];
+                    P xv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = j0 + q < W ? cs[lr * W + j0 + q] : 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (j0 + q < W) xv[q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[q]) * K) + lane);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (j0 + q >= W) continue;
+                        V const* vp = vs + (lr * W + j0 + q) * VS;
+                        V const a = vp[0];
+#pragma unroll
+                        for (int e = 0; e < E; ++e) vfma(sum[e], a, xv[q].v[e]);
+                        if (VS == 2) {
+                            V const b = vp[1];
+#pragma unroll
+                            for (int e = 0; e < E; ++e) vfma(lo[e], b, xv[q].v[e]);
+                        }
+                    }
+                }
+                P yn;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
+                    yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
+                    m2[e] += vsq(xr.v[e]);
+                    m3r[e] += vdre(yn.v[e], xr.v[e]);
+                    if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
+                }
+                st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(t.row_begin + lr) * K) + lane, yn);
+            }
+        }
+        __syncwarp();
+        if ((ct % 32) == 0) async::mbar_arrive(empty + s);
+    }
+    if (cur_sys >= 0)
+        tma_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV, ok);
+}
+
+template<class V, int E, int LPR>
+cudaError_t diag_tma_launch(DiagStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    if (a.error == nullptr || a.tma_rows < 1 || (E * LPR * sizeof(V)) % 16 != 0) return cudaErrorInvalidValue;
+    size_t const smem = diag_tma_smem<V, E, LPR>(a.tma_rows, a.W);
+    auto fn = a.init ? diag_tma_kernel<V, E, LPR, true> : diag_tma_kernel<V, E, LPR, false>;
+    // one attribute set and occupancy query per (kernel, shared size)
+    static void const* done_fn[32];
+    static size_t done_smem[32];
+    static int done_occ[32];
+    static int ndone = 0;
+    int occ = 0;
+    for (int i = 0; i < ndone; ++i)
+        if (done_fn[i] == reinterpret_cast<void const*>(fn) && done_smem[i] == smem) occ = done_occ[i];
+    if (occ == 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, TMA_THREADS, smem) != cudaSuccess || occ < 1) {
+            cudaGetLastError();
+            return cudaErrorInvalidConfiguration;
+        }
+        if (ndone < 32) {
+            done_fn[ndone] = reinterpret_cast<void const*>(fn);
+            done_smem[ndone] = smem;
+            done_occ[ndone] = occ;
+            ++ndone;
+        }
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int const g = std::max(1, std::min(a.num_tiles, sms * occ));
+    fn<<<g, TMA_THREADS, smem, s>>>(a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x),
+                                    static_cast<V*>(a.y), a.batch_stride, a.tiles, a.num_tiles, a.nbatch, a.acc,
+                                    a.tma_rows, a.error);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ off-diagonal step
 template<class V, int E, int LPR, bool INIT>
 __global__ void __launch_bounds__(BLOCK)
@@ -393,71 +652,95 @@ off_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 }
 
 // ------------------------------------------------------------------ dense collection step
+int persistent_grid(void const* fn, int num_tiles);
+
+// One row of y <- H~ x - y (or H~ x / 2) for this lane's E vectors and the collected vector
+// of the row: x[r] (left side) or V x at row r (right side, V = val2 on the pattern of H~).
+// The row's entries go in chunks of 4 with all index loads, then all gathers, issued before
+// the first use (as in the diagonal step), so a row costs two dependent round trips.
 template<class V, int E, int LPR, bool INIT>
-__global__ void __launch_bounds__(BLOCK)
-dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V const* __restrict__ val2, int W,
-                  V const* __restrict__ x, V* __restrict__ y, V* __restrict__ zx, V* __restrict__ zv,
-                  float* __restrict__ zre, float* __restrict__ zim, Tile const* __restrict__ tiles) {
+__device__ __forceinline__ void dense_row(int32_t const* __restrict__ col, V const* __restrict__ val,
+                                          V const* __restrict__ val2, int W, V const* __restrict__ x,
+                                          V* __restrict__ y, int r, int lane, Pack<V, E>& z) {
     constexpr int K = E * LPR;
-    constexpr int RPP = BLOCK / LPR;
+    constexpr int VS = Tr<V>::VS;
     using P = Pack<V, E>;
-    Tile const t = tiles[blockIdx.x];
-    int const lane = threadIdx.x % LPR;
-    int const slot = threadIdx.x / LPR;
-    for (int r = t.row_begin + slot; r < t.row_end; r += RPP) {
-        V sum[E], sv[E];
+    P const* xr_p = reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane;
+    P yo;
+    if (!INIT) yo = ld_stream(reinterpret_cast<P const*>(y + static_cast<int64_t>(r) * K) + lane);
+    if (val2 == nullptr) z = ld_ro(xr_p);
+    V sum[E], lo[E], sv[E], svl[E];
 #pragma unroll
-        for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(sv[e]); }
-        constexpr int VS = Tr<V>::VS;
-        int32_t const* cp = col + static_cast<int64_t>(r) * W;
-        V const* vp = val + static_cast<int64_t>(r) * W * VS;
-        for (int j = 0; j < W; ++j) {
-            int32_t const c = __ldg(cp + j);
-            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
+    for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(lo[e]); vzero(sv[e]); vzero(svl[e]); }
+    for (int j0 = 0; j0 < W; j0 += 4) {
+        int32_t c[4];
+        P xv[4];
 #pragma unroll
-            for (int v = 0; v < VS; ++v) {
-                V const a = vp[j * VS + v];
+        for (int q = 0; q < 4; ++q) c[q] = j0 + q < W ? __ldg(col + static_cast<int64_t>(r) * W + j0 + q) : 0;
 #pragma unroll
-                for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
-                if (val2 != nullptr) {
-                    V const b = val2[(static_cast<int64_t>(r) * W + j) * VS + v];
+        for (int q = 0; q < 4; ++q)
+            if (j0 + q < W) xv[q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[q]) * K) + lane);
 #pragma unroll
-                    for (int e = 0; e < E; ++e) vfma(sv[e], b, xv.v[e]);
+        for (int q = 0; q < 4; ++q) {
+            if (j0 + q >= W) continue;
+            int64_t const vi = (static_cast<int64_t>(r) * W + j0 + q) * VS;
+            V const a = val[vi];
+#pragma unroll
+            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv[q].v[e]);
+            if (VS == 2) {
+                V const b = val[vi + 1];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(lo[e], b, xv[q].v[e]);
+            }
+            if (val2 != nullptr) {
+                V const a2 = val2[vi];
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sv[e], a2, xv[q].v[e]);
+                if (VS == 2) {
+                    V const b2 = val2[vi + 1];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) vfma(svl[e], b2, xv[q].v[e]);
                 }
             }
         }
-        int64_t const off = static_cast<int64_t>(r) * K;
-        P* yp = reinterpret_cast<P*>(y + off) + lane;
-        P yn;
-        if (INIT) {
+    }
+    P yn;
 #pragma unroll
-            for (int e = 0; e < E; ++e) yn.v[e] = vhalf(sum[e]);
-        } else {
-            P const yo = *yp;
+    for (int e = 0; e < E; ++e) {
+        V const s = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
+        yn.v[e] = INIT ? vhalf(s) : vsub(s, yo.v[e]);
+        if (val2 != nullptr) z.v[e] = (VS == 2) ? vadd(sv[e], svl[e]) : sv[e];
+    }
+    st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
+}
+
+// Dense-collection step, persistent over interleaved tiles. The collected vector goes to z
+// (vector type, [rows][K]) or, for the tensor-core moments GEMM, to FP32 planes zre / zim.
+template<class V, int E, int LPR, bool INIT>
+__global__ void __launch_bounds__(BLOCK)
+dense_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, V const* __restrict__ val2, int W,
+                  V const* __restrict__ x, V* __restrict__ y, V* __restrict__ z, float* __restrict__ zre,
+                  float* __restrict__ zim, Tile const* __restrict__ tiles, int num_tiles) {
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;
+    using P = Pack<V, E>;
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    for (int ti = blockIdx.x; ti < num_tiles; ti += gridDim.x) {
+        Tile const t = tiles[ti];
+        for (int r = t.row_begin + slot; r < t.row_end; r += RPP) {
+            P zv;
+            dense_row<V, E, LPR, INIT>(col, val, val2, W, x, y, r, lane, zv);
+            int64_t const off = static_cast<int64_t>(r) * K;
+            if (zre != nullptr) {
 #pragma unroll
-            for (int e = 0; e < E; ++e) yn.v[e] = vsub(sum[e], yo.v[e]);
-        }
-        *yp = yn;
-        if (zre != nullptr) {  // FP32 planes for the tensor-core moments GEMM: V r (right) or r (left)
-            P o;
-            if (val2 != nullptr) {
-#pragma unroll
-                for (int e = 0; e < E; ++e) o.v[e] = sv[e];
+                for (int e = 0; e < E; ++e) {
+                    __stcs(zre + off + lane * E + e, re32(zv.v[e]));
+                    if constexpr (Tr<V>::C) __stcs(zim + off + lane * E + e, im32(zv.v[e]));
+                }
             } else {
-                o = reinterpret_cast<P const*>(x + off)[lane];
+                st_stream(reinterpret_cast<P*>(z + off) + lane, zv);
             }
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                zre[off + lane * E + e] = re32(o.v[e]);
-                if constexpr (Tr<V>::C) zim[off + lane * E + e] = im32(o.v[e]);
-            }
-        }
-        if (zx != nullptr) reinterpret_cast<P*>(zx + off)[lane] = reinterpret_cast<P const*>(x + off)[lane];
-        if (zv != nullptr) {
-            P o;
-#pragma unroll
-            for (int e = 0; e < E; ++e) o.v[e] = sv[e];
-            reinterpret_cast<P*>(zv + off)[lane] = o;
         }
     }
 }
@@ -469,14 +752,12 @@ cudaError_t dense_launch(DenseStep const& a, cudaStream_t s) {
     auto const* val2 = static_cast<V const*>(a.val2);
     auto const* x = static_cast<V const*>(a.x);
     auto* y = static_cast<V*>(a.y);
-    auto* zx = static_cast<V*>(a.zx);
-    auto* zv = static_cast<V*>(a.zv);
-    if (a.init)
-        dense_step_kernel<V, E, LPR, true><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.zre,
-                                                                         a.zim, a.tiles);
-    else
-        dense_step_kernel<V, E, LPR, false><<<a.num_tiles, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, zx, zv, a.zre,
-                                                                          a.zim, a.tiles);
+    auto* z = static_cast<V*>(a.zv != nullptr ? a.zv : a.zx);
+    if (a.zre == nullptr && z == nullptr) return cudaErrorInvalidValue;
+    if ((a.zv != nullptr) != (a.val2 != nullptr) && a.zre == nullptr) return cudaErrorInvalidValue;
+    auto fn = a.init ? dense_step_kernel<V, E, LPR, true> : dense_step_kernel<V, E, LPR, false>;
+    int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
+    fn<<<g, BLOCK, 0, s>>>(a.col, val, val2, a.W, x, y, z, a.zre, a.zim, a.tiles, a.num_tiles);
     return cudaGetLastError();
 }
 
@@ -493,79 +774,89 @@ __global__ void __launch_bounds__(BLOCK)
 adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x,
                 V const* yprev, V* out, int half, V const* __restrict__ v0, V const* __restrict__ vm,
                 V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, double* __restrict__ gt,
-                double* __restrict__ gd, Tile const* __restrict__ tiles) {
+                double* __restrict__ gd, Tile const* __restrict__ tiles, int num_tiles) {
     static_assert(!Tr<V>::C, "the adjoint step is real");
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;
     constexpr int VS = Tr<V>::VS;
     using P = Pack<V, E>;
-    Tile const t = tiles[blockIdx.x];
     int const lane = threadIdx.x % LPR;
     int const slot = threadIdx.x / LPR;
-    for (int rb = t.row_begin; rb < t.row_end; rb += RPP) {
-        int const r = rb + slot;
-        bool const live = r < t.row_end;
-        int const rs = live ? r : t.row_begin;  // dead lanes follow a valid row without storing
-        V sum[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) vzero(sum[e]);
-        P gv;
-        if (gt != nullptr) {
-            gv = ld_ro(reinterpret_cast<P const*>(g + static_cast<int64_t>(rs) * K) + lane);
-            P const xr = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(rs) * K) + lane);
-            V p = V(0);
-#pragma unroll
-            for (int e = 0; e < E; ++e) vfma(p, xr.v[e], gv.v[e]);
-#pragma unroll
-            for (int off = 1; off < LPR; off <<= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
-            if (live && lane == 0) gd[r] += static_cast<double>(p);
-        }
-        int32_t const* cp = col + static_cast<int64_t>(rs) * W;
-        V const* vv = val + static_cast<int64_t>(rs) * W * VS;
-        for (int j = 0; j < W; ++j) {
-            int32_t const c = __ldg(cp + j);
-            P const xv = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c) * K) + lane);
-#pragma unroll
-            for (int v = 0; v < VS; ++v) {
-                V const a = vv[j * VS + v];
-#pragma unroll
-                for (int e = 0; e < E; ++e) vfma(sum[e], a, xv.v[e]);
-            }
-            if (gt != nullptr) {
+    bool const grad = gt != nullptr;
+    for (int ti = blockIdx.x; ti < num_tiles; ti += gridDim.x) {  // uniform over the block
+        Tile const t = tiles[ti];
+        for (int rb = t.row_begin; rb < t.row_end; rb += RPP) {
+            int const r = rb + slot;
+            bool const live = r < t.row_end;
+            int const rs = live ? r : t.row_begin;  // dead lanes follow a valid row without storing
+            int64_t const off = static_cast<int64_t>(rs) * K;
+            P gv, yo, q0;
+            if (grad) gv = ld_ro(reinterpret_cast<P const*>(g + off) + lane);
+            if (out != nullptr && yprev != nullptr) yo = reinterpret_cast<P const*>(yprev + off)[lane];
+            if (out != nullptr && v0 != nullptr) q0 = (grad && v0 == g) ? gv : ld_ro(reinterpret_cast<P const*>(v0 + off) + lane);
+            if (grad) {
+                P const xr = ld_ro(reinterpret_cast<P const*>(x + off) + lane);
                 V p = V(0);
 #pragma unroll
-                for (int e = 0; e < E; ++e) vfma(p, xv.v[e], gv.v[e]);
+                for (int e = 0; e < E; ++e) vfma(p, xr.v[e], gv.v[e]);
 #pragma unroll
-                for (int off = 1; off < LPR; off <<= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
-                if (live && lane == 0) gt[static_cast<int64_t>(r) * W + j] += static_cast<double>(p);
+                for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+                if (live && lane == 0) gd[r] += static_cast<double>(p);
             }
-        }
-        if (live && out != nullptr) {
-            int64_t const off = static_cast<int64_t>(r) * K;
-            P o;
+            V sum[E], lo[E];
 #pragma unroll
-            for (int e = 0; e < E; ++e) o.v[e] = half ? vhalf(sum[e]) : sum[e];
-            if (yprev != nullptr) {
-                P const yo = reinterpret_cast<P const*>(yprev + off)[lane];
+            for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(lo[e]); }
+            for (int j0 = 0; j0 < W; j0 += 4) {
+                int32_t c[4];
+                P xv[4];
 #pragma unroll
-                for (int e = 0; e < E; ++e) o.v[e] -= yo.v[e];
+                for (int q = 0; q < 4; ++q) c[q] = j0 + q < W ? __ldg(col + static_cast<int64_t>(rs) * W + j0 + q) : 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (j0 + q < W) xv[q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[q]) * K) + lane);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (j0 + q >= W) continue;
+                    int64_t const vi = (static_cast<int64_t>(rs) * W + j0 + q) * VS;
+                    V const a = val[vi];
+#pragma unroll
+                    for (int e = 0; e < E; ++e) vfma(sum[e], a, xv[q].v[e]);
+                    if (VS == 2) {
+                        V const b = val[vi + 1];
+#pragma unroll
+                        for (int e = 0; e < E; ++e) vfma(lo[e], b, xv[q].v[e]);
+                    }
+                    if (grad) {
+                        V p = V(0);
+#pragma unroll
+                        for (int e = 0; e < E; ++e) vfma(p, xv[q].v[e], gv.v[e]);
+#pragma unroll
+                        for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+                        if (live && lane == 0) gt[static_cast<int64_t>(r) * W + j0 + q] += static_cast<double>(p);
+                    }
+                }
             }
-            if (v0 != nullptr) {
-                P const q = ld_ro(reinterpret_cast<P const*>(v0 + off) + lane);
+            if (live && out != nullptr) {
+                P o;
 #pragma unroll
-                for (int e = 0; e < E; ++e) vfma(o.v[e], a0, q.v[e]);
-            }
-            if (vm != nullptr) {
-                P const q = ld_ro(reinterpret_cast<P const*>(vm + off) + lane);
+                for (int e = 0; e < E; ++e) {
+                    V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
+                    o.v[e] = half ? vhalf(sv) : sv;
+                    if (yprev != nullptr) o.v[e] -= yo.v[e];
+                    if (v0 != nullptr) vfma(o.v[e], a0, q0.v[e]);
+                }
+                if (vm != nullptr) {
+                    P const q = ld_ro(reinterpret_cast<P const*>(vm + off) + lane);
 #pragma unroll
-                for (int e = 0; e < E; ++e) vfma(o.v[e], am, q.v[e]);
-            }
-            if (vp != nullptr) {
-                P const q = ld_ro(reinterpret_cast<P const*>(vp + off) + lane);
+                    for (int e = 0; e < E; ++e) vfma(o.v[e], am, q.v[e]);
+                }
+                if (vp != nullptr) {
+                    P const q = ld_ro(reinterpret_cast<P const*>(vp + off) + lane);
 #pragma unroll
-                for (int e = 0; e < E; ++e) vfma(o.v[e], ap, q.v[e]);
+                    for (int e = 0; e < E; ++e) vfma(o.v[e], ap, q.v[e]);
+                }
+                reinterpret_cast<P*>(out + off)[lane] = o;
             }
-            reinterpret_cast<P*>(out + off)[lane] = o;
         }
     }
 }
@@ -573,11 +864,13 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 template<class V, int E, int LPR>
 cudaError_t adj_launch(AdjStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
-    adj_step_kernel<V, E, LPR><<<a.num_tiles, BLOCK, 0, s>>>(
-        a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x), static_cast<V const*>(a.yprev),
-        static_cast<V*>(a.out), a.half ? 1 : 0, static_cast<V const*>(a.v0), static_cast<V const*>(a.vm),
-        static_cast<V const*>(a.vp), static_cast<V>(a.a0), static_cast<V>(a.am), static_cast<V>(a.ap),
-        static_cast<V const*>(a.g), a.gt, a.gd, a.tiles);
+    auto fn = adj_step_kernel<V, E, LPR>;
+    int const grid = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
+    fn<<<grid, BLOCK, 0, s>>>(a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x),
+                              static_cast<V const*>(a.yprev), static_cast<V*>(a.out), a.half ? 1 : 0,
+                              static_cast<V const*>(a.v0), static_cast<V const*>(a.vm), static_cast<V const*>(a.vp),
+                              static_cast<V>(a.a0), static_cast<V>(a.am), static_cast<V>(a.ap),
+                              static_cast<V const*>(a.g), a.gt, a.gd, a.tiles, a.num_tiles);
     return cudaGetLastError();
 }
 
@@ -906,6 +1199,12 @@ cudaError_t pair_launch(DiagPair const& a, cudaStream_t s) {
 template<class V, int E, int LPR>
 cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
+    if (a.tma_rows > 0) {
+        if constexpr (E * sizeof(V) == 16 && LPR > 1)  // multi-vector rows of 16-byte lanes
+            return diag_tma_launch<V, E, LPR>(a, s);
+        else
+            return cudaErrorInvalidValue;
+    }
     if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2>(a, s);
     return diag_launch_u<V, E, LPR, 1>(a, s);
 }
@@ -931,6 +1230,12 @@ cudaError_t off_launch(OffStep const& a, cudaStream_t s) {
 #define KPM_SHAPES_F64(X) X(double, 1, 1) X(double, 2, 2) X(double, 2, 4) X(double, 2, 8) X(double, 2, 16) X(double, 2, 32)
 #define KPM_SHAPES_C64(X) X(float2, 1, 1) X(float2, 2, 2) X(float2, 2, 4) X(float2, 2, 8) X(float2, 2, 16) X(float2, 2, 32)
 #define KPM_SHAPES_C128(X) X(double2, 1, 1) X(double2, 1, 2) X(double2, 1, 4) X(double2, 1, 8) X(double2, 1, 16) X(double2, 1, 32)
+
+// thinner lane mappings of the same K (half the bytes per lane, twice the lanes per row) for
+// the diagonal step: fewer registers per thread, more rows in flight; the autotuner picks
+#define KPM_DIAG_ALT_F32(X) X(float, 2, 32) X(float, 2, 16) X(float, 2, 8)
+#define KPM_DIAG_ALT_F64(X) X(double, 1, 32) X(double, 1, 16) X(double, 1, 8)
+#define KPM_DIAG_ALT_C64(X) X(float2, 1, 32) X(float2, 1, 16) X(float2, 1, 8)
 
 template<class V> constexpr int vcode();
 template<> constexpr int vcode<float>() { return V_F32; }
@@ -1197,6 +1502,14 @@ bool diag_shape_supported(int vtype, int E, int LPR) {
     return false;
 }
 
+bool diag_step_supported(int vtype, int E, int LPR) {
+#define KPM_CHECK(V, e, l) if (vtype == vcode<V>() && E == e && LPR == l) return true;
+    KPM_SHAPES_F32(KPM_CHECK) KPM_SHAPES_F64(KPM_CHECK) KPM_SHAPES_C64(KPM_CHECK) KPM_SHAPES_C128(KPM_CHECK)
+    KPM_DIAG_ALT_F32(KPM_CHECK) KPM_DIAG_ALT_F64(KPM_CHECK) KPM_DIAG_ALT_C64(KPM_CHECK)
+#undef KPM_CHECK
+    return false;
+}
+
 cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s) {
 #define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return pair_launch<V, e, l>(a, s);
     KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
@@ -1207,6 +1520,7 @@ cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s) {
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s) {
 #define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return diag_launch<V, e, l>(a, s);
     KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
+    KPM_DIAG_ALT_F32(KPM_DISPATCH) KPM_DIAG_ALT_F64(KPM_DISPATCH) KPM_DIAG_ALT_C64(KPM_DISPATCH)
 #undef KPM_DISPATCH
     return cudaErrorInvalidValue;
 }

@@ -322,3 +322,67 @@ def test_conductivity_tensor_core_gemm_matches_fp64_gemm(oracle, dtype, precisio
         err_o = rel_err(tc, ref)
         print("  tensor vs oracle %.3e" % err_o)
         assert err_o < 2e-5
+
+
+@pytest.mark.parametrize("dtype,nvec", [(np.float64, 8), (np.float32, 64), (np.complex128, 1)])
+def test_repeated_calls_replay_the_recursion_graph(dtype, nvec):
+    """From the second call on, an engine replays its captured recursion (a CUDA graph). New
+    starters, and new values after set_hamiltonian (same sizes, same device buffers), must give
+    what a fresh engine gives."""
+    h1, h2 = (_disordered_flake(20000, s, np.float64).astype(dtype) for s in (3, 4))
+    cfg = dict(energy_range=(-9.5, 9.5))
+    rng = np.random.default_rng(0)
+    M = 258
+    eng = _native.Engine(h1, _native.make_config(**cfg))
+
+    def starters():
+        st = np.where(rng.integers(0, 2, (nvec, h1.shape[0])) == 0, -1.0, 1.0)
+        return st.astype(dtype)[None]
+
+    def fresh(h, st):
+        e = _native.Engine(h, _native.make_config(**cfg))
+        out = e.moments_diag(M, st)
+        e.close()
+        return out
+
+    tol = 1e-12 if np.dtype(dtype) in (np.dtype(np.float64), np.dtype(np.complex128)) else 1e-5
+    for _ in range(3):
+        st = starters()
+        assert rel_err(eng.moments_diag(M, st), fresh(h1, st)) < tol
+    eng.set_hamiltonian(h2)
+    for _ in range(2):
+        st = starters()
+        assert rel_err(eng.moments_diag(M, st), fresh(h2, st)) < tol
+
+
+@pytest.mark.parametrize("dtype,nvec,tol", [(np.float32, 64, 1e-5), (np.float64, 16, 1e-10),
+                                            (np.complex64, 32, 1e-5), (np.complex128, 8, 1e-10)])
+def test_tma_staged_step_matches_register_step_and_oracle(oracle, dtype, nvec, tol):
+    """The TMA-staged diagonal step (bulk copies of y_old, own x rows and the ELL entries into
+    shared memory) against the register-load step and the FP64 oracle, on a ragged batch of
+    three flakes whose row offsets are not multiples of 4 (unaligned index and value copies)."""
+    hs = [_disordered_flake(n, s, np.float64) for n, s in ((9001, 1), (4003, 2), (12007, 3))]
+    if np.iscomplexobj(np.zeros(1, dtype)):
+        hs = [(h + 1j * sp.triu(h, 1) * 0.1 - 1j * sp.tril(h, -1) * 0.1).tocsr() for h in hs]
+    hs = [h.astype(dtype) for h in hs]
+    rng = (-9.5, 9.5)
+    M = 130
+    a, b = oracle.scale(*rng)
+    starters = [oracle.random_starters(h.shape[0], nvec, dtype) for h in hs]
+    flat = np.concatenate([st.ravel() for st in starters])
+    out = {}
+    for staging in ("tma", "registers"):
+        batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, staging=staging)
+        out[staging] = batch.engine.moments_diag(M, flat)
+        st = batch.engine.stats()
+        assert (st.staged_rows > 0) == (staging == "tma"), st.staged_rows
+        out[staging + "2"] = batch.engine.moments_diag(M, flat)  # replayed recursion graph
+    for s, h in enumerate(hs):
+        h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
+        r = oracle.optimize(h64, [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(h64.dtype), r["reorder_map"]), M,
+                                  slices=r["slices"])
+        for k in ("tma", "tma2", "registers", "registers2"):
+            err = rel_err(out[k][s], ref)
+            print("%s %s system %d: %.3e" % (np.dtype(dtype).name, k, s, err))
+            assert err <= tol
