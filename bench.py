@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-error", action="store_true", help="skip the FP64 moment-error check")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of one CPU sample")
+    p.add_argument("--cond-sites", type=int, default=1_000_000, help="sites of the conductivity workload")
     p.add_argument("--workload", default="dos_batch",
                    choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d"])
     return p.parse_args()
@@ -459,7 +460,7 @@ def workload_conductivity(args, stream_of):
     from bond x-displacements, 16 random-phase vectors, 512 moments, Jackson; mu_mn on the tensor
     cores (tcgen05 TF32 three-product split of FP32 planes)."""
     from pybinding_gb300 import _native, lattice as L
-    m = L.graphene_flake(1_000_000, hopping_modifiers=[L.constant_magnetic_field(20.0)], is_complex=True,
+    m = L.graphene_flake(args.cond_sites, hopping_modifiers=[L.constant_magnetic_field(20.0)], is_complex=True,
                          is_double=True)
     h = m.hamiltonian.astype(np.complex128)
     x = m.system.x
@@ -481,9 +482,10 @@ def workload_conductivity(args, stream_of):
     gemm = st.gemm_time
     rec = st.moments_time - gemm
     rec_work = 2 * M * h.nnz * 16
-    _line(args, "Kubo-Bastin sigma_xx time per call (1M sites, 16 vectors, 512 moments)", t / args.steps, "s",
+    _line(args, "Kubo-Bastin sigma_xx time per call (%d sites, 16 vectors, 512 moments)" % n, t / args.steps, "s",
           False, t / args.steps,
-          {"workload": "conductivity: 1M-site graphene, 20 T, complex128, 16 vectors, 512 moments, tensor-core mu_mn",
+          {"workload": "conductivity: %d-site graphene, 20 T, complex128, 16 vectors, 512 moments, tensor-core mu_mn"
+                       % n,
            "sites": int(n), "nnz": int(h.nnz), "moments": int(M), "vectors": 16, "broadening_eV": broadening,
            "gemm": "tcgen05 kind::tf32, hi/lo split (3 products), FP32 planes, FP64 slice sums"},
           "c128 recursion, tf32x3 GEMM",

@@ -53,6 +53,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* err
     }
 }
 
+// Warp-wide wait: lane 0 polls (bounded), then every lane checks the completed phase once
+// for its own acquire. Polling with all 32 lanes issues 32 shared-memory barrier operations
+// per poll, which serialise like same-address atomics and steal shared-memory bandwidth.
+// The phase cannot advance again before this warp arrives, so the parity stays valid.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* b, uint32_t parity, int* err) {
+    bool ok = true;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(b, parity, err);
+    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    if (ok) {
+        uint32_t const a = smem_u32(b);
+        long long const t0 = clock64();
+        while (!mbar_try(a, parity))
+            if (clock64() - t0 > kWaitCycles) {  // not expected: the phase is complete
+                atomicExch(err, 3);
+                ok = false;
+                break;
+            }
+    }
+    return __all_sync(0xffffffffu, ok);
+}
+
 // Wait for this block's own asynchronous work (copies, MMAs) before it exits, also after
 // an error elsewhere; still bounded.
 __device__ __forceinline__ void mbar_drain(uint64_t* b, uint32_t parity, int* err) {

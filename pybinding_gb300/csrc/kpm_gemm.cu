@@ -237,8 +237,7 @@ mu_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_ar, const __grid_const
         bool ok = true;
         auto fold = [&](int g) {
             int const b = g & 1;
-            if (!mbar_wait(gdone + b, (g >> 1) & 1, err)) { ok = false; return; }
-            __syncwarp();
+            if (!async::mbar_wait_warp(gdone + b, (g >> 1) & 1, err)) { ok = false; return; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
             for (int q = 0; q < HCOL / 32; ++q) {
@@ -252,7 +251,7 @@ mu_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_ar, const __grid_const
         };
         for (int kb = 0; kb < nkb && ok; ++kb) {
             int const s = kb % STAGES, use = kb / STAGES;
-            if (!mbar_wait(full + s, use & 1, err)) { ok = false; break; }
+            if (!async::mbar_wait_warp(full + s, use & 1, err)) { ok = false; break; }
 #pragma unroll
             for (int p = 0; p < PLANES; ++p) {
                 float4* hi = reinterpret_cast<float4*>(tile(s, p, 0));

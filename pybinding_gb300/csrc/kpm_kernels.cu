@@ -469,7 +469,7 @@ diag_tma_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
             cur_sys = t.system;
             cur_batch = t.batch;
         }
-        ok = ok && async::mbar_wait(full + s, use & 1, err);
+        ok = ok && async::mbar_wait_warp(full + s, use & 1, err);
         if (ok) {
             unsigned char const* st = sm + s * L.stage;
             V const* ys = reinterpret_cast<V const*>(st + L.y);
