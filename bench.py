@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--no-error", action="store_true", help="skip the FP64 moment-error check")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of one CPU sample")
     p.add_argument("--cond-sites", type=int, default=1_000_000, help="sites of the conductivity workload")
+    p.add_argument("--adj-sites", type=int, default=256_000, help="sites of the adjoint workload")
+    p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
                    choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d"])
     return p.parse_args()
@@ -510,7 +512,7 @@ def workload_adjoint(args, stream_of):
     from pybinding_gb300.adjoint import DiagonalMoments, moments_weights
 
     def flake(amp):
-        return L.graphene_flake(256_000, hopping_modifiers=[L.strained_hopping(L.sinusoidal_strain(amp, 20.0))],
+        return L.graphene_flake(args.adj_sites, hopping_modifiers=[L.strained_hopping(L.sinusoidal_strain(amp, 20.0))],
                                 is_double=True)
     m = flake(0.05)
     h = m.hamiltonian.tocsr()
@@ -519,10 +521,10 @@ def workload_adjoint(args, stream_of):
     rng = np.random.default_rng(3)
     r0 = np.where(rng.integers(0, 2, (32, n)) == 0, -1.0, 1.0)
     rng_e = (-9.5, 9.5)
-    op = DiagonalMoments(h, 1024, r0, rng_e, precision="fp32")
+    op = DiagonalMoments(h, args.adj_moments, r0, rng_e, precision="fp32")
     ht = flake(0.03).hamiltonian.tocsr()
     ht.sort_indices()
-    tgt = DiagonalMoments(ht, 1024, r0, rng_e, precision="fp32")
+    tgt = DiagonalMoments(ht, args.adj_moments, r0, rng_e, precision="fp32")
     energy = np.linspace(-8, 8, 400)
     W = moments_weights(energy, op.scaling, jackson_kernel(), op.num_moments)
     target = W @ tgt.moments(ht.data)
@@ -549,12 +551,12 @@ def workload_adjoint(args, stream_of):
     op.gradient(h.data, np.ones(M))
     t_sqrt = op._engine.stats().moments_time
     op.checkpoint = 0
-    _line(args, "adjoint DOS-misfit gradient time per forward+backward (256k sites, 32 vectors, 1024 moments)",
+    _line(args, "adjoint DOS-misfit gradient time per forward+backward (%d sites, 32 vectors, %d moments)" % (n, M),
           t / args.steps, "s", False, t / args.steps,
-          {"workload": "adjoint gradients: 256k-site strained graphene, 32 vectors, 1024 moments, fp32",
+          {"workload": "adjoint gradients: %d-site strained graphene, 32 vectors, %d moments, fp32" % (n, M),
            "sites": int(n), "nnz": int(nnz), "moments": int(M),
            "checkpoint": "automatic (all vectors: they fit in HBM)"},
-          "f32 recursion, f64 gradient sums",
+          "f32 recursion and gradient sums",
           breakdown={"forward_s": times["fwd"], "forward_gnnz_vec_per_s": fwd_work / times["fwd"] / 1e9,
                      "backward_s": times["bwd"], "backward_gnnz_vec_per_s": bwd_work / times["bwd"] / 1e9,
                      "backward_over_forward": times["bwd"] / times["fwd"],

@@ -2005,8 +2005,8 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         d_seg.ensure(vec * seg_len);
         d_lam.ensure(vec * 2);
         d_roll.ensure(vec * 2);
-        d_gt.ensure(sizeof(double) * static_cast<size_t>(n) * W);
-        d_gd.ensure(sizeof(double) * static_cast<size_t>(n));
+        d_gt.ensure(static_cast<size_t>(vb) * n * W);  // gradient sums in the vectors' precision
+        d_gd.ensure(static_cast<size_t>(vb) * n);
         KPM_CUDA(cudaMemsetAsync(d_gt.p, 0, d_gt.bytes, e->stream));
         KPM_CUDA(cudaMemsetAsync(d_gd.p, 0, d_gd.bytes, e->stream));
         auto* ck = static_cast<unsigned char*>(d_ck.p);
@@ -2094,8 +2094,8 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
                     a.vp = sp(k + 1);
                     a.ap = beta[k + 1];
                     a.g = sp(k);
-                    a.gt = d_gt.as<double>();
-                    a.gd = d_gd.as<double>();
+                    a.gt = d_gt.p;
+                    a.gd = d_gd.p;
                     KPM_CUDA(kpm::launch_adj_step(a, e->stream));
                     lam2 = lam1;
                     lam1 = out;
@@ -2110,19 +2110,24 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
             kpm::AdjStep a = base;
             a.x = u;
             a.g = v0;
-            a.gt = d_gt.as<double>();
-            a.gd = d_gd.as<double>();
+            a.gt = d_gt.p;
+            a.gd = d_gd.p;
             KPM_CUDA(kpm::launch_adj_step(a, e->stream));
         }
         KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
-        std::vector<double> gt(static_cast<size_t>(n) * W), gd(static_cast<size_t>(n));
+        std::vector<unsigned char> gt_raw(d_gt.bytes), gd_raw(d_gd.bytes);
         std::vector<int32_t> hcol(static_cast<size_t>(n) * W);
-        KPM_CUDA(cudaMemcpyAsync(gt.data(), d_gt.p, sizeof(double) * gt.size(), cudaMemcpyDeviceToHost, e->stream));
-        KPM_CUDA(cudaMemcpyAsync(gd.data(), d_gd.p, sizeof(double) * gd.size(), cudaMemcpyDeviceToHost, e->stream));
+        KPM_CUDA(cudaMemcpyAsync(gt_raw.data(), d_gt.p, gt_raw.size(), cudaMemcpyDeviceToHost, e->stream));
+        KPM_CUDA(cudaMemcpyAsync(gd_raw.data(), d_gd.p, gd_raw.size(), cudaMemcpyDeviceToHost, e->stream));
         KPM_CUDA(cudaMemcpyAsync(hcol.data(), e->d_col.p, sizeof(int32_t) * hcol.size(), cudaMemcpyDeviceToHost, e->stream));
         KPM_CUDA(cudaStreamSynchronize(e->stream));
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        std::vector<double> gt(static_cast<size_t>(n) * W), gd(static_cast<size_t>(n));
+        for (size_t i = 0; i < gt.size(); ++i)
+            gt[i] = vb == 4 ? reinterpret_cast<float const*>(gt_raw.data())[i] : reinterpret_cast<double const*>(gt_raw.data())[i];
+        for (size_t i = 0; i < gd.size(); ++i)
+            gd[i] = vb == 4 ? reinterpret_cast<float const*>(gd_raw.data())[i] : reinterpret_cast<double const*>(gd_raw.data())[i];
         // gt[p][t] holds G[col(p, t)][p]: entry (i, j) of the input is found in row map[j]
         double const f = 2.0 / sc.a;
         for (int64_t i = 0; i < n; ++i)

@@ -91,8 +91,8 @@ struct DenseStep {
 
 // Adjoint of the diagonal recursion (real types): one launch of
 //   out = S x - yprev (or S x / 2 when half) + a0 v0 + am vm + ap vp
-// plus, when gt is set, gt[r][j] += sum_k x[col[r][j]][k] * g[r][k] (FP64, [rows][W]) and
-// gd[r] += sum_k x[r][k] * g[r][k] (FP64, [rows]).
+// plus, when gt is set, gt[r][j] += sum_k x[col[r][j]][k] * g[r][k] ([rows][W]) and
+// gd[r] += sum_k x[r][k] * g[r][k] ([rows]), both in the vector type's precision.
 struct AdjStep {
     int vtype;
     int E, LPR;
@@ -108,8 +108,8 @@ struct AdjStep {
     const void* vp;           // nullable
     double a0, am, ap;
     const void* g;            // row vectors of the gradient term (with gt)
-    double* gt;               // nullable
-    double* gd;               // set with gt
+    void* gt;                 // nullable
+    void* gd;                 // set with gt
     const Tile* tiles;
     int num_tiles;
 };

@@ -773,8 +773,8 @@ template<class V, int E, int LPR>
 __global__ void __launch_bounds__(BLOCK)
 adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x,
                 V const* yprev, V* out, int half, V const* __restrict__ v0, V const* __restrict__ vm,
-                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, double* __restrict__ gt,
-                double* __restrict__ gd, Tile const* __restrict__ tiles, int num_tiles) {
+                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, V* __restrict__ gt,
+                V* __restrict__ gd, Tile const* __restrict__ tiles, int num_tiles) {
     static_assert(!Tr<V>::C, "the adjoint step is real");
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;
@@ -783,6 +783,10 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
     int const lane = threadIdx.x % LPR;
     int const slot = threadIdx.x / LPR;
     bool const grad = gt != nullptr;
+    // gradient sums (the recursion's precision): with fewer entries per row than lanes, lane j
+    // owns slot j and lane W the diagonal; their old values are loaded with the row's other
+    // loads, so no dependent read-modify-write ends the row
+    bool const spread = grad && W < LPR;
     for (int ti = blockIdx.x; ti < num_tiles; ti += gridDim.x) {  // uniform over the block
         Tile const t = tiles[ti];
         for (int rb = t.row_begin; rb < t.row_end; rb += RPP) {
@@ -791,6 +795,11 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
             int const rs = live ? r : t.row_begin;  // dead lanes follow a valid row without storing
             int64_t const off = static_cast<int64_t>(rs) * K;
             P gv, yo, q0;
+            V gpre = V(0), gsum = V(0);
+            if (spread && live) {
+                if (lane < W) gpre = gt[static_cast<int64_t>(r) * W + lane];
+                else if (lane == W) gpre = gd[r];
+            }
             if (grad) gv = ld_ro(reinterpret_cast<P const*>(g + off) + lane);
             if (out != nullptr && yprev != nullptr) yo = reinterpret_cast<P const*>(yprev + off)[lane];
             if (out != nullptr && v0 != nullptr) q0 = (grad && v0 == g) ? gv : ld_ro(reinterpret_cast<P const*>(v0 + off) + lane);
@@ -801,7 +810,11 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
                 for (int e = 0; e < E; ++e) vfma(p, xr.v[e], gv.v[e]);
 #pragma unroll
                 for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-                if (live && lane == 0) gd[r] += static_cast<double>(p);
+                if (spread) {
+                    if (lane == W) gsum += p;
+                } else if (live && lane == 0) {
+                    gd[r] += p;
+                }
             }
             V sum[E], lo[E];
 #pragma unroll
@@ -832,9 +845,17 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
                         for (int e = 0; e < E; ++e) vfma(p, xv[q].v[e], gv.v[e]);
 #pragma unroll
                         for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-                        if (live && lane == 0) gt[static_cast<int64_t>(r) * W + j0 + q] += static_cast<double>(p);
+                        if (spread) {
+                            if (lane == j0 + q) gsum += p;
+                        } else if (live && lane == 0) {
+                            gt[static_cast<int64_t>(r) * W + j0 + q] += p;
+                        }
                     }
                 }
+            }
+            if (spread && live) {
+                if (lane < W) gt[static_cast<int64_t>(r) * W + lane] = gpre + gsum;
+                else if (lane == W) gd[r] = gpre + gsum;
             }
             if (live && out != nullptr) {
                 P o;
@@ -870,7 +891,8 @@ cudaError_t adj_launch(AdjStep const& a, cudaStream_t s) {
                               static_cast<V const*>(a.yprev), static_cast<V*>(a.out), a.half ? 1 : 0,
                               static_cast<V const*>(a.v0), static_cast<V const*>(a.vm), static_cast<V const*>(a.vp),
                               static_cast<V>(a.a0), static_cast<V>(a.am), static_cast<V>(a.ap),
-                              static_cast<V const*>(a.g), a.gt, a.gd, a.tiles, a.num_tiles);
+                              static_cast<V const*>(a.g), static_cast<V*>(a.gt), static_cast<V*>(a.gd), a.tiles,
+                              a.num_tiles);
     return cudaGetLastError();
 }
 

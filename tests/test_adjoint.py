@@ -190,7 +190,7 @@ def test_gpu_adjoint_matches_dense_eigh_gradient():
 
 @pytest.mark.gpu
 def test_gpu_adjoint_fp32_close_to_fp64():
-    """FP32 recursion (FP32 vectors, FP64 gradient sums) against the FP64 one on a 64k-site
+    """FP32 recursion (FP32 vectors and gradient sums) against the FP64 one on a 64k-site
     strained flake, 1026 moments, 32 Rademacher vectors: within 5e-4 of the largest entry
     (measured 1.8e-4; each entry's gradient is a local sum over 513 steps, so it keeps less of
     the FP32 cancellation than the global moments, which agree to ~2e-6)."""
