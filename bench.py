@@ -272,6 +272,8 @@ def run_gpu(args, rank, world, local_rank):
     rec = float(np.median(rec_times))
     fuse = int(eng.stats().steps_per_launch)
     lane_map = (int(eng.stats().elems_per_lane), int(eng.stats().lanes_per_row))
+    tiling = {"tile_rows": int(eng.stats().tile_rows), "unroll": int(eng.stats().unroll),
+              "staged_rows": int(eng.stats().staged_rows)}
     launches = 1 + (M // 2 - 1) // fuse  # init + recursion launches
     avg_launch = rec / launches
     nrows = rows
@@ -350,7 +352,7 @@ def run_gpu(args, rank, world, local_rank):
                             "frac": achieved / peak, "traffic": traffic,
                             "kernel": "%s<float,%d,%d>" % ("diag_step_kernel" if fuse == 1 else "diag_pair_kernel",
                                                            lane_map[0], lane_map[1]),
-                            "steps_per_launch": fuse, "alg_bytes_per_launch": alg_bytes,
+                            "steps_per_launch": fuse, "tiling": tiling, "alg_bytes_per_launch": alg_bytes,
                             "avg_launch_ms": avg_launch * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
                "cpu_baseline": {"value": cpu["value"], "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": cpu["sample"]},

@@ -91,6 +91,8 @@ typedef struct kpm_stats {
     int32_t elems_per_lane;   /* recursion kernel lane mapping used last: vector elements per lane */
     int32_t lanes_per_row;    /*   and lanes per matrix row (their product = vectors per block) */
     int32_t staged_rows;      /*   0 = register loads, > 0 = TMA-staged tiles of this many rows */
+    int32_t tile_rows;        /*   rows per tile */
+    int32_t unroll;           /*   rows per thread per iteration */
 } kpm_stats;
 
 typedef struct kpm_engine kpm_engine;

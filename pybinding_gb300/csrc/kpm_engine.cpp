@@ -31,6 +31,7 @@
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 using kpm::Tile;
@@ -309,6 +310,8 @@ struct kpm_engine {
     int W = 0;
     int64_t opt_nnz = 0;                     // reordered CSR non-zeros (all systems)
     DBuf d_col, d_val, d_map, d_sysoff;
+    DBuf d_val_real;          // real-valued copy of a complex H~ whose values are all real
+    bool real_values = false;
 
     // Lanczos device state
     bool lz_uploaded = false;
@@ -347,6 +350,7 @@ struct kpm_engine {
         int ntiles, vtype, E, LPR, nbatch, unroll, W, tma_rows;
         int32_t row_limit;
         int* error;
+        bool real_matrix;
         bool operator==(RecursionGraphKey const& o) const { return std::memcmp(this, &o, sizeof o) == 0; }
     };
     RecursionGraphKey graph_key{};
@@ -699,6 +703,35 @@ struct kpm_engine {
             KPM_CUDA(cudaMemcpyAsync(d_val.p, val.data(), val.size() * sizeof(Tc), cudaMemcpyHostToDevice, stream));
             KPM_CUDA(cudaStreamSynchronize(stream));
         });
+        // A complex H~ whose values are all real (e.g. a real lattice stored as complex so that
+        // random-phase starters apply): the diagonal step can multiply by real values, two FMAs
+        // per entry instead of four (same results: the imaginary parts are exact zeros)
+        real_values = false;
+        if (cpx) {
+            real_values = std::all_of(oval_c.begin(), oval_c.end(), [](cd const& h) { return h.imag() == 0.0; });
+            if (real_values) {
+                auto upload = [&](auto zr) {
+                    using Tr_ = decltype(zr);
+                    int const rvs = std::is_same_v<Tr_, float> ? 2 : 1;  // FP32: (hi, lo) pairs
+                    std::vector<Tr_> rv(static_cast<size_t>(rows) * W * rvs, Tr_(0));
+                    for (int64_t r = 0; r < rows; ++r) {
+                        int j = 0;
+                        for (int32_t k = oip[r]; k < oip[r + 1]; ++k, ++j) {
+                            double const h = oval_c[k].real();
+                            Tr_ const hi = static_cast<Tr_>(h);
+                            rv[(r * W + j) * rvs] = hi;
+                            if (rvs == 2) rv[(r * W + j) * rvs + 1] = static_cast<Tr_>(h - static_cast<double>(hi));
+                        }
+                    }
+                    d_val_real.ensure(rv.size() * sizeof(Tr_) + 64);
+                    KPM_CUDA(cudaMemcpyAsync(d_val_real.p, rv.data(), rv.size() * sizeof(Tr_), cudaMemcpyHostToDevice,
+                                             stream));
+                    KPM_CUDA(cudaStreamSynchronize(stream));
+                };
+                if (vtype == kpm::V_C64) upload(float{});
+                else upload(double{});
+            }
+        }
         opt_nnz = oip.back();
         d_map.ensure(sizeof(int32_t) * rows);
         KPM_CUDA(cudaMemcpy(d_map.p, map.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice));
@@ -812,7 +845,7 @@ struct kpm_engine {
                     }
             // the TMA-staged kernel (full rows, 16-byte lanes): tile heights that fit in shared memory
             if (cfg.staging != 1 && batch_outer && sh.E * kpm::vtype_bytes(vtype) == 16 && sh.LPR > 1 &&
-                base.error != nullptr)
+                base.error != nullptr && !base.real_matrix)
                 for (int tr : {32, 64, 128}) {
                     Shape t = sh;
                     t.rows_per_tile = tr;
@@ -1001,7 +1034,8 @@ struct kpm_engine {
         a.E = sh.E;
         a.LPR = sh.LPR;
         a.col = d_col.as<int32_t>();
-        a.val = d_val.p;
+        a.val = real_values ? d_val_real.p : d_val.p;
+        a.real_matrix = real_values;
         a.W = W;
         a.batch_stride = bstride;
         a.tiles = d_tiles.as<Tile>();
@@ -1015,7 +1049,7 @@ struct kpm_engine {
         d_pair_error.ensure(sizeof(int));
         KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
         a.error = d_pair_error.as<int>();
-        bool const tma_ok = batch_outer && sh.E * vb == 16 && sh.LPR > 1;
+        bool const tma_ok = batch_outer && sh.E * vb == 16 && sh.LPR > 1 && !real_values;
         if (cfg.staging == 2 && tma_ok) {
             sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 64;
             a.tma_rows = sh.rows_per_tile;
@@ -1162,6 +1196,7 @@ struct kpm_engine {
             key.W = W;
             key.row_limit = a.row_limit;
             key.tma_rows = a.tma_rows;
+            key.real_matrix = a.real_matrix;
             key.error = a.error;
             if (graph_exec == nullptr || !(key == graph_key)) {
                 drop_graph();
@@ -1190,6 +1225,7 @@ struct kpm_engine {
         while (n <= half) single_step();
         last_fuse = choice.steps;
         last_tma_rows = a.tma_rows;
+        last_unroll = a.unroll;
         KPM_CUDA(cudaEventRecord(ev1, stream));
         KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
                                           d_mu.as<double>(), stream));
@@ -1207,6 +1243,7 @@ struct kpm_engine {
     Shape last_shape{};
     int last_fuse = 1;
     int last_tma_rows = 0;
+    int last_unroll = 1;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
 
     void reset_stats(int64_t M, bool diagonal, bool opt, double multiplier, int64_t active_rows_nnz_rows) {
@@ -1241,6 +1278,8 @@ struct kpm_engine {
         st.elems_per_lane = last_shape.E;
         st.lanes_per_row = last_shape.LPR;
         st.staged_rows = last_tma_rows;
+        st.tile_rows = last_shape.rows_per_tile;
+        st.unroll = last_unroll;
     }
 
     // ---------------------------------------------------------------- reconstruction

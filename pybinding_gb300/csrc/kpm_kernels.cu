@@ -70,6 +70,15 @@ __device__ __forceinline__ void vfma(double2& acc, double2 a, double2 x) {
     acc.y = fma(a.x, x.y, acc.y);
     acc.y = fma(a.y, x.x, acc.y);
 }
+// real matrix value times complex vector element (two FMAs)
+__device__ __forceinline__ void vfma(float2& acc, float a, float2 x) {
+    acc.x = fmaf(a, x.x, acc.x);
+    acc.y = fmaf(a, x.y, acc.y);
+}
+__device__ __forceinline__ void vfma(double2& acc, double a, double2 x) {
+    acc.x = fma(a, x.x, acc.x);
+    acc.y = fma(a, x.y, acc.y);
+}
 __device__ __forceinline__ float vadd(float a, float b) { return a + b; }
 __device__ __forceinline__ double vadd(double a, double b) { return a + b; }
 __device__ __forceinline__ float2 vadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -144,14 +153,14 @@ __device__ __forceinline__ void st_stream(P* p, P const& v) {
 // in chunks of 4 with every load of a chunk issued before its first use, so a row
 // costs two dependent memory round trips (indices, then gathers) rather than one
 // per entry; x[r] and y_old[r] are issued ahead of the index loads.
-template<class V, int E, int LPR, bool INIT, int U, bool XCOH = false>
-__device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
+template<class V, int E, int LPR, bool INIT, int U, bool XCOH = false, class MV = V>
+__device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
                                           V const* __restrict__ x, V* __restrict__ y, int const (&rr)[U],
                                           bool const (&live)[U], int lane, typename Tr<V>::R (&m2)[E],
                                           typename Tr<V>::R (&m3r)[E], typename Tr<V>::R (&m3i)[E]) {
     constexpr bool CPLX = Tr<V>::C;
     constexpr int K = E * LPR;
-    constexpr int VS = Tr<V>::VS;
+    constexpr int VS = Tr<MV>::VS;
     using P = Pack<V, E>;
     P xr[U], yo[U];
     V sum[U][E], lo[U][E];
@@ -185,12 +194,12 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, V con
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (!(live[u] && j0 + q < W)) continue;
-                V const* vp = val + (static_cast<int64_t>(rr[u]) * W + j0 + q) * VS;
-                V const a = vp[0];
+                MV const* vp = val + (static_cast<int64_t>(rr[u]) * W + j0 + q) * VS;
+                MV const a = vp[0];
 #pragma unroll
                 for (int e = 0; e < E; ++e) vfma(sum[u][e], a, xv[u][q].v[e]);
                 if (VS == 2) {
-                    V const b = vp[1];
+                    MV const b = vp[1];
 #pragma unroll
                     for (int e = 0; e < E; ++e) vfma(lo[u][e], b, xv[u][q].v[e]);
                 }
@@ -260,9 +269,9 @@ __device__ __forceinline__ void diag_flush(typename Tr<V>::R (&m2)[E], typename 
     for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
 }
 
-template<class V, int E, int LPR, bool INIT, int U>
+template<class V, int E, int LPR, bool INIT, int U, class MV = V>
 __global__ void __launch_bounds__(BLOCK)
-diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W,
+diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
                  V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
                  Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
                  double* __restrict__ acc) {
@@ -302,7 +311,7 @@ diag_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
                 rr[u] = r + u * RPP;
                 live[u] = rr[u] < row_end;
             }
-            diag_rows<V, E, LPR, INIT, U>(col, val, W, x, y, rr, live, lane, m2, m3r, m3i);
+            diag_rows<V, E, LPR, INIT, U, false, MV>(col, val, W, x, y, rr, live, lane, m2, m3r, m3i);
         }
     }
     if (cur_sys >= 0)
@@ -1071,18 +1080,18 @@ int persistent_grid(void const* fn, int num_tiles) {
     return std::max(1, std::min(num_tiles, sms * per_sm));
 }
 
-template<class V, int E, int LPR, int U>
+template<class V, int E, int LPR, int U, class MV = V>
 cudaError_t diag_launch_u(DiagStep const& a, cudaStream_t s) {
-    auto const* val = static_cast<V const*>(a.val);
+    auto const* val = static_cast<MV const*>(a.val);
     auto const* x = static_cast<V const*>(a.x);
     auto* y = static_cast<V*>(a.y);
     if (a.init) {
-        auto fn = diag_step_kernel<V, E, LPR, true, U>;
+        auto fn = diag_step_kernel<V, E, LPR, true, U, MV>;
         int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
         fn<<<g, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit, a.nbatch,
                                a.acc);
     } else {
-        auto fn = diag_step_kernel<V, E, LPR, false, U>;
+        auto fn = diag_step_kernel<V, E, LPR, false, U, MV>;
         int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
         fn<<<g, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit, a.nbatch,
                                a.acc);
@@ -1222,10 +1231,20 @@ template<class V, int E, int LPR>
 cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
     if (a.tma_rows > 0) {
+        if (a.real_matrix) return cudaErrorInvalidValue;
         if constexpr (E * sizeof(V) == 16 && LPR > 1)  // multi-vector rows of 16-byte lanes
             return diag_tma_launch<V, E, LPR>(a, s);
         else
             return cudaErrorInvalidValue;
+    }
+    if (a.real_matrix) {  // complex vectors, real H~ values: two FMAs per entry instead of four
+        if constexpr (Tr<V>::C) {
+            using MR = typename Tr<V>::R;
+            if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2, MR>(a, s);
+            return diag_launch_u<V, E, LPR, 1, MR>(a, s);
+        } else {
+            return cudaErrorInvalidValue;
+        }
     }
     if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2>(a, s);
     return diag_launch_u<V, E, LPR, 1>(a, s);

@@ -386,3 +386,28 @@ def test_tma_staged_step_matches_register_step_and_oracle(oracle, dtype, nvec, t
             err = rel_err(out[k][s], ref)
             print("%s %s system %d: %.3e" % (np.dtype(dtype).name, k, s, err))
             assert err <= tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_complex_vectors_with_real_valued_hamiltonian(oracle, dtype, tol):
+    """A real lattice stored as complex (so that random-phase starters apply, as the 60k-site
+    FP64 DOS configuration does): the diagonal step then multiplies by the real values only.
+    Moments against the FP64 oracle on the same complex H and starters; a field breaks the
+    real-valuedness and takes the complex-value path, checked the same way."""
+    for field in (None, 50.0):
+        mods = [L.constant_magnetic_field(field)] if field else []
+        m = L.graphene_flake(8000, hopping_modifiers=mods, onsite_modifiers=[L.anderson_disorder(0.5, 4)],
+                             is_complex=True)
+        h = m.hamiltonian.astype(dtype)
+        assert (np.abs(h.data.imag).max() == 0) == (field is None)
+        rng = (-9.5, 9.5)
+        a, b = oracle.scale(*rng)
+        M = 258
+        starters = oracle.random_starters(h.shape[0], 8, dtype)
+        got = _native.Engine(h, _native.make_config(energy_range=rng)).moments_diag(M, starters[None])[0]
+        r = oracle.optimize(h.astype(np.complex128), [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters.astype(np.complex128), r["reorder_map"]), M,
+                                  slices=r["slices"])
+        err = rel_err(got, ref)
+        print("%s field=%s: %.3e" % (np.dtype(dtype).name, field, err))
+        assert err <= tol
