@@ -83,6 +83,19 @@ def build_workload(args, rank):
     return hs, h, offsets
 
 
+def job_rate(work, seconds, dist=None, device="cpu"):
+    """Whole-job throughput of replicas: the units every rank processed over the slowest rank's
+    time (ranks run different seeds, so their work differs). Returns (units/s, max seconds)."""
+    if dist is None:
+        return work / seconds, seconds
+    import torch
+    w = torch.tensor([float(work)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(w.item()) / float(t.item()), float(t.item())
+
+
 def rademacher(rng, n):
     return np.where(rng.integers(0, 2, size=n, dtype=np.int8) == 0, -1.0, 1.0).astype(np.float32)
 
@@ -262,11 +275,8 @@ def run_gpu(args, rank, world, local_rank):
     barrier()
     clk = clocks.stop()
     t = e0.elapsed_time(e1) * 1e-3
-    if dist is not None:
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = world * work * args.steps / t / 1e9
+    rate, t = job_rate(work * args.steps, t, dist, "cuda")
+    value = rate / 1e9
 
     # dominant kernel: the recursion step, timed by the engine's events on its own stream
     rec = float(np.median(rec_times))
@@ -316,11 +326,8 @@ def run_gpu(args, rank, world, local_rank):
         torch.cuda.synchronize()
         barrier()
         te = max(f0.elapsed_time(f1) * 1e-3, time.perf_counter() - w0)
-        if dist is not None:
-            tt = torch.tensor([te], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
-        e2e = {"value": world * work * args.steps / te / 1e9, "unit": UNIT,
+        rate_e, te = job_rate(work * args.steps, te, dist, "cuda")
+        e2e = {"value": rate_e / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(starters.nbytes), "d2h_bytes_per_step": int(nsys * M * 16)}
 
     err = None
