@@ -93,6 +93,8 @@ typedef struct kpm_stats {
     int32_t staged_rows;      /*   0 = register loads, > 0 = TMA-staged tiles of this many rows */
     int32_t tile_rows;        /*   rows per tile */
     int32_t unroll;           /*   rows per thread per iteration */
+    double upload_time;       /* seconds (device): starter upload and scatter of the last diagonal call */
+    double call_time;         /* seconds (host wall clock) of the last call, entry to return */
 } kpm_stats;
 
 typedef struct kpm_engine kpm_engine;

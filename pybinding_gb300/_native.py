@@ -42,7 +42,8 @@ class Stats(C.Structure):
                 ("moments_time", C.c_double), ("bounds_time", C.c_double), ("lanczos_loops", C.c_int32),
                 ("eps", C.c_double), ("steps_per_launch", C.c_int32), ("gemm_time", C.c_double),
                 ("elems_per_lane", C.c_int32), ("lanes_per_row", C.c_int32), ("staged_rows", C.c_int32),
-                ("tile_rows", C.c_int32), ("unroll", C.c_int32)]
+                ("tile_rows", C.c_int32), ("unroll", C.c_int32), ("upload_time", C.c_double),
+                ("call_time", C.c_double)]
 
 
 # every exported symbol of include/kpm_gb300.h with (restype, argtypes)

@@ -355,6 +355,20 @@ struct kpm_engine {
     };
     RecursionGraphKey graph_key{};
     cudaGraphExec_t graph_exec = nullptr;
+    // The GPU can dereference pageable host memory through the host's page tables (address
+    // translation services on Grace): kernels then read caller-provided host buffers in place.
+    int host_direct = -1;
+    bool host_reads_direct() {
+        if (host_direct < 0) {
+            int dev = 0, pageable = 0, host_tables = 0;
+            KPM_CUDA(cudaGetDevice(&dev));
+            KPM_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+            KPM_CUDA(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+            host_direct = (pageable && host_tables) ? 1 : 0;
+        }
+        return host_direct == 1;
+    }
+
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
@@ -364,6 +378,8 @@ struct kpm_engine {
         drop_graph();
         if (ev_t0) cudaEventDestroy(ev_t0);
         if (ev_t1) cudaEventDestroy(ev_t1);
+        if (ev_u0) cudaEventDestroy(ev_u0);
+        if (ev_u1) cudaEventDestroy(ev_u1);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -386,6 +402,8 @@ struct kpm_engine {
         KPM_CUDA(cudaEventCreate(&ev1));
         KPM_CUDA(cudaEventCreate(&ev_t0));
         KPM_CUDA(cudaEventCreate(&ev_t1));
+        KPM_CUDA(cudaEventCreate(&ev_u0));
+        KPM_CUDA(cudaEventCreate(&ev_u1));
     }
 
     void set_h(int st_, int64_t n, int32_t const* ip, int32_t const* ix, void const* v, int ns, int64_t const* offs) {
@@ -1012,16 +1030,19 @@ struct kpm_engine {
         bool const batch_outer = !opt_rows;
         int ntiles = build_tiles(sh, sys0, batch_outer);
 
+        KPM_CUDA(cudaEventRecord(ev_u0, stream));
         KPM_CUDA(cudaMemsetAsync(d_x0.p, 0, vbytes, stream));
         if (units) {
             d_pos.ensure(sizeof(int32_t) * units->size());
             KPM_CUDA(cudaMemcpyAsync(d_pos.p, units->data(), sizeof(int32_t) * units->size(), cudaMemcpyHostToDevice, stream));
             KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, sh.K, rows, stream));
         } else {
-            // starters are in the Hamiltonian's scalar type; the scatter converts them
+            // starters are in the Hamiltonian's scalar type; the scatter converts them. Host starters:
+            // where the GPU reads host memory through the host page tables (Grace), the scatter
+            // kernel reads them in place; elsewhere they are staged in device memory first
             size_t const in_bytes = static_cast<size_t>(nvec) * rows * scalar_bytes(stype);
             void const* src = starters;
-            if (!on_device) {
+            if (!on_device && !host_reads_direct()) {
                 d_stage.ensure(in_bytes);
                 KPM_CUDA(cudaMemcpyAsync(d_stage.p, starters, in_bytes, cudaMemcpyHostToDevice, stream));
                 src = d_stage.p;
@@ -1029,6 +1050,7 @@ struct kpm_engine {
             KPM_CUDA(kpm::launch_scatter_starters(stype, vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(),
                                                   nsys, nvec, sh.K, sh.nbatch, rows, stream));
         }
+        KPM_CUDA(cudaEventRecord(ev_u1, stream));
         kpm::DiagStep a{};
         a.vtype = vtype;
         a.E = sh.E;
@@ -1238,13 +1260,18 @@ struct kpm_engine {
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         st.moments_time = ms * 1e-3;
+        float ums = 0;
+        KPM_CUDA(cudaEventElapsedTime(&ums, ev_u0, ev_u1));
+        last_upload_time = ums * 1e-3;
         last_shape = sh;
     }
     Shape last_shape{};
     int last_fuse = 1;
     int last_tma_rows = 0;
     int last_unroll = 1;
+    double last_upload_time = 0;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+    cudaEvent_t ev_u0 = nullptr, ev_u1 = nullptr;  // starter upload + scatter of the last diagonal call
 
     void reset_stats(int64_t M, bool diagonal, bool opt, double multiplier, int64_t active_rows_nnz_rows) {
         (void)active_rows_nnz_rows;
@@ -1280,6 +1307,7 @@ struct kpm_engine {
         st.staged_rows = last_tma_rows;
         st.tile_rows = last_shape.rows_per_tile;
         st.unroll = last_unroll;
+        st.upload_time = last_upload_time;
     }
 
     // ---------------------------------------------------------------- reconstruction
@@ -2191,6 +2219,7 @@ int kpm_get_stats(kpm_engine* e, kpm_stats* out) {
     return guarded([&] {
         if (!e || !out) fail(KPM_ERR_VALUE, "null argument");
         *out = e->st;
+        out->call_time = e->calc_time;
     });
 }
 
