@@ -369,6 +369,18 @@ struct kpm_engine {
         return host_direct == 1;
     }
 
+    // A device-readable view of a host buffer for a kernel on `stream`: the buffer itself where
+    // the GPU reads host memory in place, else a copy in d_stage. The host buffer must stay
+    // unchanged until the stream has consumed it.
+    void const* device_view(void const* host, size_t bytes) {
+        if (host_reads_direct()) return host;
+        d_stage.ensure(bytes);
+        KPM_CUDA(cudaMemcpyAsync(d_stage.p, host, bytes, cudaMemcpyHostToDevice, stream));
+        return d_stage.p;
+    }
+
+    std::vector<unsigned char> h_starters, h_starters_right;  // host starters the engine generates
+
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
@@ -1042,11 +1054,7 @@ struct kpm_engine {
             // kernel reads them in place; elsewhere they are staged in device memory first
             size_t const in_bytes = static_cast<size_t>(nvec) * rows * scalar_bytes(stype);
             void const* src = starters;
-            if (!on_device && !host_reads_direct()) {
-                d_stage.ensure(in_bytes);
-                KPM_CUDA(cudaMemcpyAsync(d_stage.p, starters, in_bytes, cudaMemcpyHostToDevice, stream));
-                src = d_stage.p;
-            }
+            if (!on_device) src = device_view(starters, in_bytes);
             KPM_CUDA(kpm::launch_scatter_starters(stype, vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(),
                                                   nsys, nvec, sh.K, sh.nbatch, rows, stream));
         }
@@ -1467,7 +1475,10 @@ int kpm_calc_dos(kpm_engine* e, const double* energy, int64_t ne, double broaden
         e->optimize({0}, {0});
         // the reference's random starters: one default-seeded mt19937 per system (Starter.cpp:48-84),
         // in the Hamiltonian's scalar type
-        std::vector<unsigned char> st(static_cast<size_t>(num_random) * e->rows * scalar_bytes(e->stype));
+        // kept by the engine between calls: the GPU reads it in place, and pages it has seen
+        // before are cheaper to read again
+        std::vector<unsigned char>& st = e->h_starters;
+        st.resize(static_cast<size_t>(num_random) * e->rows * scalar_bytes(e->stype));
         with_scalar(e->stype, [&](auto zi) {
             using Tin = decltype(zi);
             using R = real_of<Tin>;
@@ -1713,10 +1724,9 @@ int kpm_moments(kpm_engine* e, int64_t num_moments, const double* alpha, int64_t
             size_t const vbytes = static_cast<size_t>(n) * vb;
             e->d_x0.ensure(vbytes);
             e->d_x1.ensure(vbytes);
-            e->d_stage.ensure(st.size());
-            KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, st.data(), st.size(), cudaMemcpyHostToDevice, e->stream));
+            void const* src = e->device_view(st.data(), st.size());
             KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, vbytes, e->stream));
-            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, e->d_stage.p, e->d_x0.p, e->d_map.as<int32_t>(),
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, src, e->d_x0.p, e->d_map.as<int32_t>(),
                                                   e->d_sysoff.as<int64_t>(), 1, 1, 1, 1, n, e->stream));
             kpm_engine::Shape sh{1, 1, 1, 1, 4096};
             int const ntiles = e->build_tiles(sh, true);
@@ -1795,7 +1805,8 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         KPM_CUDA(cudaMemcpy(hcol.data(), e->d_col.p, hcol.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
         int const vs = kpm::vtype_vs(vt);
         std::vector<unsigned char> vr_ell(static_cast<size_t>(n) * W * vs * vb, 0);
-        std::vector<unsigned char> starters_l, starters_r;
+        std::vector<unsigned char>& starters_l = e->h_starters;  // reused between calls (read in place)
+        std::vector<unsigned char>& starters_r = e->h_starters_right;
         int64_t K = 1;
         // tensor-core GEMM: the collected vectors are kept as FP32 planes (re [, im])
         int const planes = kpm::vtype_complex(vt) ? 2 : 1;
@@ -1885,16 +1896,14 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         }
         e->d_x0.ensure(vec_bytes);
         e->d_x1.ensure(vec_bytes);
-        e->d_stage.ensure(static_cast<size_t>(K) * n * ssize);
         d_mu_acc.ensure(sizeof(double) * 2 * M * M);
         KPM_CUDA(cudaMemsetAsync(d_mu_acc.p, 0, sizeof(double) * 2 * M * M, e->stream));
         int const ntiles = e->build_tiles(sh, true);
         double rec_time = 0;
         auto recursion = [&](unsigned char const* host_starters, bool right_side) {
-            KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, host_starters, static_cast<size_t>(K) * n * ssize,
-                                     cudaMemcpyHostToDevice, e->stream));
+            void const* src = e->device_view(host_starters, static_cast<size_t>(K) * n * ssize);
             KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, vec_bytes, e->stream));
-            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, e->d_stage.p, e->d_x0.p, e->d_map.as<int32_t>(),
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, src, e->d_x0.p, e->d_map.as<int32_t>(),
                                                   e->d_sysoff.as<int64_t>(), 1, K, static_cast<int>(K), 1, n, e->stream));
             kpm::DenseStep a{};
             a.vtype = vt;
@@ -2103,7 +2112,6 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
 
         size_t const ssize = static_cast<size_t>(scalar_bytes(e->stype));
         std::vector<unsigned char> stage(static_cast<size_t>(K) * n * ssize);
-        e->d_stage.ensure(stage.size());
         KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
         int64_t const nbatch = (num_vectors + K - 1) / K;
         for (int64_t b = 0; b < nbatch; ++b) {
@@ -2113,9 +2121,9 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
             std::fill(stage.begin(), stage.end(), 0);  // missing vectors of the last batch are zero
             std::memcpy(stage.data(), static_cast<unsigned char const*>(starters) + static_cast<size_t>(v_first) * n * ssize,
                         static_cast<size_t>(v_count) * n * ssize);
-            KPM_CUDA(cudaMemcpyAsync(e->d_stage.p, stage.data(), stage.size(), cudaMemcpyHostToDevice, e->stream));
+            void const* src = e->device_view(stage.data(), stage.size());
             KPM_CUDA(cudaMemsetAsync(ckA(0), 0, vec, e->stream));
-            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, e->d_stage.p, ckA(0), e->d_map.as<int32_t>(),
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, src, ckA(0), e->d_map.as<int32_t>(),
                                                   e->d_sysoff.as<int64_t>(), 1, K, static_cast<int>(K), 1, n,
                                                   e->stream));
             // forward pass: checkpoints (v_c, v_{c+1}) for c = j * seg_len
