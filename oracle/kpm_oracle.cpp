@@ -454,8 +454,16 @@ Optimized<T> create_reordered(CSR<T> const& h, Indices const& idx, Scale s) {
     h2.rows = h2.cols = n;
     h2.indptr.assign(n + 1, 0);
     Vec<std::pair<int32_t, T>> row_buf;
+    int32_t next_unvisited = 0;
     for (int64_t h2_row = 0; h2_row < n; ++h2_row) {
         bool diagonal_inserted = false;
+        if (h2_row == static_cast<int64_t>(queue.size())) {
+            // disconnected graph: the reference reads past its queue here (it assumes a connected
+            // system); continue from the first row not reached yet, as the engine does
+            while (oh.reorder_map[next_unvisited] >= 0) ++next_unvisited;
+            oh.reorder_map[next_unvisited] = static_cast<int32_t>(queue.size());
+            queue.push_back(next_unvisited);
+        }
         auto const row = queue[h2_row];
         row_buf.clear();
         for (auto k = h.indptr[row]; k < h.indptr[row + 1]; ++k) {

@@ -637,7 +637,16 @@ struct kpm_engine {
             for (int64_t i = 0; i < n; ++i) { order.push_back(static_cast<int32_t>(i)); local[i] = static_cast<int32_t>(i); }
         }
         std::vector<std::pair<int32_t, Tc>> row_buf;
+        int32_t next_unvisited = 0;
         for (int64_t nr = 0; nr < n; ++nr) {
+            if (nr == static_cast<int64_t>(order.size())) {
+                // the breadth-first search has exhausted the target's connected component (the
+                // reference assumes a connected graph and would read past its queue here): continue
+                // from the first row not reached yet, as a new component
+                while (local[next_unvisited] >= 0) ++next_unvisited;
+                local[next_unvisited] = static_cast<int32_t>(order.size());
+                order.push_back(next_unvisited);
+            }
             int32_t const orow = order[nr];
             row_buf.clear();
             bool diag = false;

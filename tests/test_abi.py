@@ -138,3 +138,30 @@ def test_optimized_hamiltonian_bit_exact(oracle):
                 assert np.array_equal(got["src"], ref["src"]) and np.array_equal(got["dest"], ref["dest"])
                 assert (got["src_offset"], got["dest_offset"]) == (ref["src_offset"], ref["dest_offset"])
         eng.close()
+
+
+def test_optimized_hamiltonian_disconnected_bit_exact(oracle):
+    """A system of two flakes without a shared bond plus a site with no entries: the reorder
+    continues from the first unreached row when the target's component is exhausted (the
+    reference assumes a connected graph); engine and oracle agree bit for bit, and every row
+    appears exactly once."""
+    import scipy.sparse as sp
+    from pybinding_gb300 import lattice as L
+    h1 = L.graphene_flake(300).hamiltonian
+    h2 = L.graphene_flake(200).hamiltonian
+    h = sp.block_diag([h1, sp.csr_matrix((1, 1), dtype=h1.dtype), h2], format="csr")
+    h.sort_indices()
+    n = h.shape[0]
+    for rng in ((-9.0, 9.0), (-8.0, 9.5)):
+        eng = _native.Engine(h, _native.make_config(energy_range=rng))
+        a, b = oracle.scale(*rng)
+        for src in ([0], [h1.shape[0] + 5], [h1.shape[0]]):
+            got = eng.optimized_hamiltonian(src, src)
+            ref = oracle.optimize(h, src, src, a, b)
+            assert np.array_equal(np.sort(got["reorder_map"]), np.arange(n))
+            assert np.array_equal(got["reorder_map"], ref["reorder_map"])
+            assert np.array_equal(got["h2"].indptr, ref["h2"].indptr)
+            assert np.array_equal(got["h2"].indices, ref["h2"].indices)
+            assert np.array_equal(got["h2"].data.view(np.uint8), ref["h2"].data.view(np.uint8))
+            assert np.array_equal(got["slices"], ref["slices"])
+        eng.close()

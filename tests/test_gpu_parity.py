@@ -411,3 +411,41 @@ def test_complex_vectors_with_real_valued_hamiltonian(oracle, dtype, tol):
         err = rel_err(got, ref)
         print("%s field=%s: %.3e" % (np.dtype(dtype).name, field, err))
         assert err <= tol
+
+
+def test_disconnected_system(oracle):
+    """One system made of two flakes that share no bond plus a site with no entries at all: the
+    breadth-first reorder must cover every component (the reference assumes a connected graph).
+    Moments against a plain FP64 NumPy recursion on the unreordered matrix; LDOS of a site in the
+    second flake equals the LDOS of that flake alone; bit-exact against the oracle's reorder."""
+    h1 = _disordered_flake(3000, 1, np.float64)
+    h2 = _disordered_flake(2000, 2, np.float64)
+    h = sp.block_diag([h1, sp.csr_matrix((1, 1)), h2], format="csr")
+    h.sort_indices()
+    n = h.shape[0]
+    rng = (-9.5, 9.5)
+    a, b = oracle.scale(*rng)
+    M = 66
+    rs = np.random.default_rng(3)
+    st = np.where(rs.integers(0, 2, (4, n)) == 0, -1.0, 1.0)
+    eng = _native.Engine(h, _native.make_config(energy_range=rng))
+    got = eng.moments_diag(M, st[None])[0]
+    ht = ((h - b * sp.identity(n)) / a).tocsr()
+    ref = np.zeros((4, M))
+    for v in range(4):
+        r0 = st[v]
+        r1 = ht @ r0
+        ref[v, 0], ref[v, 1] = r0 @ r0, r1 @ r0
+        for k in range(2, M):
+            r0, r1 = r1, 2 * (ht @ r1) - r0
+            ref[v, k] = r1 @ st[v]
+    ref[:, 0] *= 0.5  # the collectors store mu_0 halved
+    assert rel_err(got.real, ref) < 1e-12
+    energy = np.linspace(-3, 3, 21)
+    site = h1.shape[0] + 1 + 100  # in the second flake
+    ldos = eng.calc_ldos([site], energy, 0.2)[:, 0]
+    alone = _native.Engine(h2, _native.make_config(energy_range=rng)).calc_ldos([100], energy, 0.2)[:, 0]
+    np.testing.assert_allclose(ldos, alone, rtol=1e-10, atol=1e-12)
+    r = oracle.optimize(h, [site], [site], a, b)
+    opt = eng.optimized_hamiltonian([site], [site])
+    assert np.array_equal(opt["reorder_map"], r["reorder_map"])
