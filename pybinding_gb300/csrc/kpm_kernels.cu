@@ -1131,18 +1131,34 @@ diag_pair_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
     constexpr int RPP = BLOCK / LPR;
     constexpr int NV = CPLX ? 3 : 2;
     __shared__ R red[WARPS * K * NV];
+    // per-thread moment partials of both phases live in shared memory (own slot, no sync); only
+    // the current item's partials are in registers, which keeps the kernel within 64 registers
+    __shared__ R part[2][NV][E][BLOCK];
     __shared__ int s_item[2];
     __shared__ int s_ok;
 
     int const lane = threadIdx.x % LPR;
     int const slot = threadIdx.x / LPR;
     int const total = 2 * num_tiles;
-    R aA2[E], aA3r[E], aA3i[E], aB2[E], aB3r[E], aB3i[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        aA2[e] = R(0); aA3r[e] = R(0); aA3i[e] = R(0);
-        aB2[e] = R(0); aB3r[e] = R(0); aB3i[e] = R(0);
-    }
+    for (int ph = 0; ph < 2; ++ph)
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+#pragma unroll
+            for (int e = 0; e < E; ++e) part[ph][v][e][threadIdx.x] = R(0);
+    // flush the partials of one phase into its FP64 accumulator slot (block-wide)
+    auto flush = [&](int ph, double* a) {
+        R f2[E], f3r[E], f3i[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            f2[e] = part[ph][0][e][threadIdx.x];
+            f3r[e] = part[ph][1][e][threadIdx.x];
+            f3i[e] = CPLX ? part[ph][NV - 1][e][threadIdx.x] : R(0);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) part[ph][v][e][threadIdx.x] = R(0);
+        }
+        diag_flush<V, E, LPR>(f2, f3r, f3i, red, a);
+    };
     int curA_sys = -1, curA_b = -1, curB_sys = -1, curB_b = -1;
     for (int iter = 0;; ++iter) {
         int const buf = iter & 1;
@@ -1156,28 +1172,11 @@ diag_pair_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
         int const item = s_item[buf];
         if (item < 0) break;
         int const t = item >> 1;
+        int const ph = item & 1;
         Tile const tl = tiles[t];
         V* P = P_all + tl.batch * batch_stride;
         V* Q = Q_all + tl.batch * batch_stride;
-        if ((item & 1) == 0) {  // phase A
-            if (tl.system != curA_sys || tl.batch != curA_b) {
-                if (curA_sys >= 0)
-                    diag_flush<V, E, LPR>(aA2, aA3r, aA3i, red,
-                                          accA + static_cast<int64_t>(curA_sys * nbatch + curA_b) * K * NV);
-                curA_sys = tl.system;
-                curA_b = tl.batch;
-            }
-            for (int r = tl.row_begin + slot; r < tl.row_end; r += RPP) {
-                int rr[1] = {r};
-                bool live[1] = {true};
-                diag_rows<V, E, LPR, false, 1, false>(col, val, W, Q, P, rr, live, lane, aA2, aA3r, aA3i);
-            }
-            __syncthreads();  // every row of the tile is stored
-            if (threadIdx.x == 0) {
-                __threadfence();
-                st_release(flags + t, seq);
-            }
-        } else {  // phase B
+        if (ph == 1) {  // phase B waits for phase A of its band
             if (threadIdx.x < 32) {
                 int const lo = band[2 * t], hi = band[2 * t + 1];
                 bool ok = true;
@@ -1196,24 +1195,46 @@ diag_pair_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
                 if (threadIdx.x == 0) atomicExch(error, 1);
                 continue;
             }
-            if (tl.system != curB_sys || tl.batch != curB_b) {
-                if (curB_sys >= 0)
-                    diag_flush<V, E, LPR>(aB2, aB3r, aB3i, red,
-                                          accB + static_cast<int64_t>(curB_sys * nbatch + curB_b) * K * NV);
-                curB_sys = tl.system;
-                curB_b = tl.batch;
-            }
+        }
+        int& cs = ph == 0 ? curA_sys : curB_sys;
+        int& cb = ph == 0 ? curA_b : curB_b;
+        if (tl.system != cs || tl.batch != cb) {
+            if (cs >= 0) flush(ph, (ph == 0 ? accA : accB) + static_cast<int64_t>(cs * nbatch + cb) * K * NV);
+            cs = tl.system;
+            cb = tl.batch;
+        }
+        R m2[E], m3r[E], m3i[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+        if (ph == 0) {  // T_n from Q = T_{n-1} into P = T_{n-2}
             for (int r = tl.row_begin + slot; r < tl.row_end; r += RPP) {
                 int rr[1] = {r};
                 bool live[1] = {true};
-                diag_rows<V, E, LPR, false, 1, true>(col, val, W, P, Q, rr, live, lane, aB2, aB3r, aB3i);
+                diag_rows<V, E, LPR, false, 1, false>(col, val, W, Q, P, rr, live, lane, m2, m3r, m3i);
+            }
+        } else {        // T_{n+1} from P = T_n into Q = T_{n-1}
+            for (int r = tl.row_begin + slot; r < tl.row_end; r += RPP) {
+                int rr[1] = {r};
+                bool live[1] = {true};
+                diag_rows<V, E, LPR, false, 1, true>(col, val, W, P, Q, rr, live, lane, m2, m3r, m3i);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            part[ph][0][e][threadIdx.x] += m2[e];
+            part[ph][1][e][threadIdx.x] += m3r[e];
+            if (CPLX) part[ph][NV - 1][e][threadIdx.x] += m3i[e];
+        }
+        if (ph == 0) {
+            __syncthreads();  // every row of the tile is stored
+            if (threadIdx.x == 0) {
+                __threadfence();
+                st_release(flags + t, seq);
             }
         }
     }
-    if (curA_sys >= 0)
-        diag_flush<V, E, LPR>(aA2, aA3r, aA3i, red, accA + static_cast<int64_t>(curA_sys * nbatch + curA_b) * K * NV);
-    if (curB_sys >= 0)
-        diag_flush<V, E, LPR>(aB2, aB3r, aB3i, red, accB + static_cast<int64_t>(curB_sys * nbatch + curB_b) * K * NV);
+    if (curA_sys >= 0) flush(0, accA + static_cast<int64_t>(curA_sys * nbatch + curA_b) * K * NV);
+    if (curB_sys >= 0) flush(1, accB + static_cast<int64_t>(curB_sys * nbatch + curB_b) * K * NV);
 }
 
 template<class V, int E, int LPR>
