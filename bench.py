@@ -62,6 +62,13 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of one CPU sample")
     p.add_argument("--cond-sites", type=int, default=1_000_000, help="sites of the conductivity workload")
     p.add_argument("--adj-sites", type=int, default=256_000, help="sites of the adjoint workload")
+    p.add_argument("--cube", type=int, default=160, help="edge of the 3D Anderson cube")
+    p.add_argument("--cube-vectors", type=int, default=256, help="vectors of the 3D Anderson workload")
+    p.add_argument("--cube-moments", type=int, default=8192, help="moments of the 3D Anderson workload")
+    p.add_argument("--ldos-sites", type=int, default=4096, help="LDOS sites of the 3D Anderson workload (0: none)")
+    p.add_argument("--staging", default="auto", choices=["auto", "registers", "tma"],
+                   help="recursion kernel operands (auto = chosen by timing; pin it under a profiler)")
+    p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2], help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
                    choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d"])
@@ -243,7 +250,8 @@ def run_gpu(args, rank, world, local_rank):
         for _ in range(R):
             starters[pos:pos + n] = rademacher(rng, n)
             pos += n
-    cfg = _native.make_config()  # Lanczos bounds, Jackson, auto precision (fp32 vectors for an f32 H)
+    # Lanczos bounds, Jackson, auto precision (fp32 vectors for an f32 H)
+    cfg = _native.make_config(staging=args.staging, fuse_steps=args.fuse)
     eng = _native.Engine(h, cfg, system_offsets=offsets)
     for s in range(nsys):
         eng.scaling_factors(s)
@@ -580,18 +588,18 @@ def workload_anderson3d(args, stream_of):
     """3D Anderson model: simple cubic 160^3 periodic, t = -1, onsite U[-8.25, 8.25], 256 Rademacher
     vectors, 8192 moments (8194), FP32 vectors / FP64 sums; then LDOS at 4096 sites (1024 moments)."""
     from pybinding_gb300 import _native, lattice as L
-    Lc = 160
+    Lc = args.cube
     rng = np.random.default_rng(5)
     h = L.simple_cubic_periodic(Lc, onsite=rng.uniform(-8.25, 8.25, Lc ** 3).astype(np.float32)).hamiltonian
     n = h.shape[0]
-    R = 256
-    eng = _native.Engine(h, _native.make_config())
+    R = args.cube_vectors
+    eng = _native.Engine(h, _native.make_config(staging=args.staging, fuse_steps=args.fuse))
     eng.scaling_factors()
     st = (rng.integers(0, 2, (R, n), dtype=np.int8) * 2 - 1).astype(np.float32)
     import torch
     d_st = torch.from_numpy(st.reshape(-1)).cuda()
     stream = stream_of(eng)
-    t, wall, clk, _ = _timed(lambda: eng.moments_diag(8192, None, average=True, on_device_ptr=d_st.data_ptr(),
+    t, wall, clk, _ = _timed(lambda: eng.moments_diag(args.cube_moments, None, average=True, on_device_ptr=d_st.data_ptr(),
                                                       num_vectors=R), args.steps, args.warmup, stream)
     s = eng.stats()
     M = s.num_moments
@@ -602,22 +610,27 @@ def workload_anderson3d(args, stream_of):
     alg = h.nnz * 12 + 4 * (n + 1) + vec_bytes
     avg = s.moments_time / launches
     peak = float(_peaks().get("hbm_gbs", 6800.0))
-    sites = rng.choice(n, 4096, replace=False)
-    a, b = eng.scaling_factors()
-    t0 = time.perf_counter()
-    eng.calc_ldos(sites, np.linspace(-10, 10, 200), _jackson_broadening(1024, a))
-    t_ldos = time.perf_counter() - t0
-    _line(args, "KPM Gnnz*vec/s (3D Anderson, 256 vectors, 8192 moments, FP32)", work / (t / args.steps) / 1e9,
+    t_ldos = None
+    if args.ldos_sites > 0:
+        sites = rng.choice(n, args.ldos_sites, replace=False)
+        a, b = eng.scaling_factors()
+        t0 = time.perf_counter()
+        eng.calc_ldos(sites, np.linspace(-10, 10, 200), _jackson_broadening(1024, a))
+        t_ldos = time.perf_counter() - t0
+    _line(args, "KPM Gnnz*vec/s (3D Anderson, %d vectors, %d moments, FP32)" % (R, M), work / (t / args.steps) / 1e9,
           "Gnnz*vec/s", True, t / args.steps,
-          {"workload": "3D Anderson: simple cubic 160^3 periodic, W = 16.5, 256 vectors, 8192 moments",
+          {"workload": "3D Anderson: simple cubic %d^3 periodic, W = 16.5, %d vectors, %d moments" % (Lc, R, M),
            "sites": int(n), "nnz": int(h.nnz), "moments": int(M), "vectors": R,
            "l2": "inputs larger than L2 (no flush)"},
           "f32",
           roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",
                     "frac": alg / avg / 1e9 / peak, "traffic": None, "steps_per_launch": fuse,
+                    "kernel": ("diag_tma_kernel" if s.staged_rows else "diag_step_kernel") if fuse == 1 else "diag_pair_kernel",
+                    "lane_map": [int(s.elems_per_lane), int(s.lanes_per_row)], "tile_rows": int(s.tile_rows),
+                    "unroll": int(s.unroll),
                     "alg_bytes_per_launch": alg, "avg_launch_ms": avg * 1e3,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-          ldos_4096_sites_1024_moments_s=t_ldos, clocks=clk,
+          ldos_sites=args.ldos_sites, ldos_1024_moments_s=t_ldos, clocks=clk,
           gpu_launches=int(args.steps * (launches + 3)))
 
 

@@ -825,10 +825,11 @@ struct kpm_engine {
         return sh;
     }
 
-    // Autotuner: the tile height (rows per block) of a launch shape is picked by timing
-    // the diagonal kernel on this engine's matrix. It runs the INIT form (x0 -> x1, a
-    // pure function of x0), so the recursion that follows is unaffected; the
-    // accumulator slot it touches is cleared again by the caller. Cached per shape.
+    // Autotuner: the launch options of a shape are picked by timing the diagonal kernel on
+    // this engine's matrix, in its regular form (x1 <- H~ x0 - x1, the register footprint of
+    // the recursion; the INIT form needs fewer registers and times differently). Only x1 and
+    // the first accumulator slot change; the init step that follows overwrites x1 and the
+    // caller clears the accumulators again. Cached per shape.
     struct TuneKey {
         int vtype, E, LPR, nbatch;
         int64_t rows;
@@ -870,7 +871,7 @@ struct kpm_engine {
                         base.LPR = t.LPR;
                         base.num_tiles = build_tiles(t, sys0, batch_outer);
                         base.tiles = d_tiles.as<Tile>();
-                        base.init = true;
+                        base.init = false;
                         base.unroll = unroll;
                         KPM_CUDA(kpm::launch_diag_step(base, stream));  // warm
                         KPM_CUDA(cudaEventRecord(ev0, stream));
@@ -892,7 +893,7 @@ struct kpm_engine {
                     base.LPR = sh.LPR;
                     base.num_tiles = build_tiles(t, sys0, batch_outer);
                     base.tiles = d_tiles.as<Tile>();
-                    base.init = true;
+                    base.init = false;
                     base.unroll = 1;
                     base.tma_rows = tr;
                     cudaError_t const le = kpm::launch_diag_step(base, stream);
