@@ -288,13 +288,14 @@ def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
 
 
 def _csr_sorted(rows, cols, vals, n, dtype):
-    order = np.lexsort((cols, rows))
-    rows, cols, vals = rows[order], cols[order], vals[order]
-    indptr = np.zeros(n + 1, np.int32)
-    np.add.at(indptr, rows + 1, 1)
-    indptr = np.cumsum(indptr).astype(np.int32)
-    m = sp.csr_matrix((vals.astype(dtype), cols.astype(np.int32), indptr), shape=(n, n))
-    m.has_sorted_indices = True
+    """CSR with sorted column indices per row from (row, col, value) triples without
+    duplicates: a counting sort by row (COO -> CSR, O(nnz)) and a per-row sort of the few
+    columns of each row, instead of a global lexicographic sort."""
+    m = sp.coo_matrix((np.asarray(vals).astype(dtype), (rows.astype(np.int32), cols.astype(np.int32))),
+                      shape=(n, n)).tocsr()
+    m.sort_indices()
+    m.indptr = m.indptr.astype(np.int32, copy=False)
+    m.indices = m.indices.astype(np.int32, copy=False)
     return m
 
 
