@@ -708,14 +708,32 @@ struct kpm_engine {
         bool const cpx = kpm::vtype_complex(vtype);
         std::vector<cd> oval_c;
         std::vector<double> oval_r;
+        // systems are independent: reorder them in parallel into their own buffers, then join
+        std::vector<ScaleAB> scs(nsys);  // bounds (Lanczos on the GPU) before the threads start
+        for (int s = 0; s < nsys; ++s) scs[s] = scale(s);
+        std::vector<std::vector<int32_t>> sip(nsys), six(nsys);
+        std::vector<std::vector<cd>> svc(cpx ? nsys : 0);
+        std::vector<std::vector<double>> svr(cpx ? 0 : nsys);
         with_scalar(stype, [&](auto zi) {
             using Tin = decltype(zi);
-            for (int s = 0; s < nsys; ++s) {
+            parallel_for(nsys, [&](int64_t s) {
                 std::vector<int32_t> sl = (s == 0) ? src : std::vector<int32_t>{0};
-                if (cpx) reorder_system<cd, Tin>(s, sl, scale(s), reorders(), oip, oix, oval_c, s == 0 ? &slices : nullptr);
-                else reorder_system<double, Tin>(s, sl, scale(s), reorders(), oip, oix, oval_r, s == 0 ? &slices : nullptr);
-            }
+                if (cpx)
+                    reorder_system<cd, Tin>(static_cast<int>(s), sl, scs[s], reorders(), sip[s], six[s], svc[s],
+                                            s == 0 ? &slices : nullptr);
+                else
+                    reorder_system<double, Tin>(static_cast<int>(s), sl, scs[s], reorders(), sip[s], six[s], svr[s],
+                                                s == 0 ? &slices : nullptr);
+            });
         });
+        for (int s = 0; s < nsys; ++s) {
+            int32_t const base = static_cast<int32_t>(oix.size());
+            for (int32_t e : sip[s]) oip.push_back(base + e);
+            oix.insert(oix.end(), six[s].begin(), six[s].end());
+            if (cpx) oval_c.insert(oval_c.end(), svc[s].begin(), svc[s].end());
+            else oval_r.insert(oval_r.end(), svr[s].begin(), svr[s].end());
+            std::vector<int32_t>().swap(six[s]);
+        }
         for (int64_t r = 0; r < rows; ++r) W = std::max(W, oip[r + 1] - oip[r]);
         W = std::max(W, 1);
         int const vs = kpm::vtype_vs(vtype);
