@@ -66,8 +66,9 @@ typedef struct kpm_config {
     int32_t tile_rows;        /* rows per thread block tile; 0 = autotuned on the first call */
     int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, or 0 = chosen by timing */
     int32_t staging;          /* diagonal step operands: 0 = chosen by timing, 1 = register loads,
-                                 2 = TMA bulk copies into shared memory (full-system recursions of
-                                 16-byte-lane shapes; others use register loads) */
+                                 2 = TMA bulk copies into shared memory, 3 = per-thread cp.async
+                                 pipeline (2 and 3: full-system recursions of 16-byte-lane shapes,
+                                 3 also rows of <= 4 entries; others use register loads) */
 } kpm_config;
 
 /* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */
@@ -90,7 +91,8 @@ typedef struct kpm_stats {
     double gemm_time;         /* seconds: device time of the conductivity's moments GEMM (0 otherwise) */
     int32_t elems_per_lane;   /* recursion kernel lane mapping used last: vector elements per lane */
     int32_t lanes_per_row;    /*   and lanes per matrix row (their product = vectors per block) */
-    int32_t staged_rows;      /*   0 = register loads, > 0 = TMA-staged tiles of this many rows */
+    int32_t staged_rows;      /*   0 = register loads, > 0 = TMA-staged tiles of this many rows,
+                                   < 0 = cp.async-pipelined tiles of -staged_rows rows */
     int32_t tile_rows;        /*   rows per tile */
     int32_t unroll;           /*   rows per thread per iteration */
     double upload_time;       /* seconds (device): starter upload and scatter of the last diagonal call */

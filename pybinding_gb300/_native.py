@@ -22,7 +22,7 @@ SCALAR_CODE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1,
                np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
 KERNEL_CODE = {"jackson": 0, "lorentz": 1, "dirichlet": 2}
 PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2}
-STAGING_CODE = {"auto": 0, "registers": 1, "tma": 2}
+STAGING_CODE = {"auto": 0, "registers": 1, "tma": 2, "async": 3}
 
 
 class Config(C.Structure):

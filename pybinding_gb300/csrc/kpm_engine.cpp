@@ -351,6 +351,7 @@ struct kpm_engine {
         int32_t row_limit;
         int* error;
         bool real_matrix;
+        bool async_copy;
         bool operator==(RecursionGraphKey const& o) const { return std::memcmp(this, &o, sizeof o) == 0; }
     };
     RecursionGraphKey graph_key{};
@@ -857,7 +858,7 @@ struct kpm_engine {
                    batch_outer == o.batch_outer;
         }
     };
-    struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; };
+    struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; bool async_copy; };
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
     std::vector<std::pair<TuneKey, FuseChoice>> fuse_tuned;
@@ -868,7 +869,7 @@ struct kpm_engine {
         TuneKey const key{vtype, sh.E, sh.LPR, sh.nbatch, rows, batch_outer};
         for (auto const& t : tuned)
             if (t.first == key) return t.second;
-        Tuned best{(256 / sh.LPR) * 16, 1, sh.E, sh.LPR, 0};
+        Tuned best{(256 / sh.LPR) * 16, 1, sh.E, sh.LPR, 0, false};
         // lane mappings of this K: the default (16 bytes per lane) and, when the row allows,
         // half the elements per lane over twice the lanes
         std::vector<std::pair<int, int>> maps{{sh.E, sh.LPR}};
@@ -899,7 +900,7 @@ struct kpm_engine {
                         float ms = 0;
                         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
                         last_tuning.push_back({static_cast<double>(t.rows_per_tile), static_cast<double>(unroll), ms / 3});
-                        if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR, 0}; }
+                        if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR, 0, false}; }
                     }
             // the TMA-staged kernel (full rows, 16-byte lanes): tile heights that fit in shared memory
             if (cfg.staging != 1 && batch_outer && sh.E * kpm::vtype_bytes(vtype) == 16 && sh.LPR > 1 &&
@@ -926,9 +927,37 @@ struct kpm_engine {
                     float ms = 0;
                     KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
                     last_tuning.push_back({static_cast<double>(tr), -1.0, ms / 3});
-                    if (ms < best_ms) { best_ms = ms; best = Tuned{tr, 1, sh.E, sh.LPR, tr}; }
+                    if (ms < best_ms) { best_ms = ms; best = Tuned{tr, 1, sh.E, sh.LPR, tr, false}; }
                 }
             base.tma_rows = 0;
+            // the cp.async pipeline kernel (rows of at most 4 entries, 16-byte lanes)
+            if (cfg.staging != 1 && batch_outer && W <= 4 && sh.E * kpm::vtype_bytes(vtype) == 16 && !base.real_matrix)
+                for (int rpt : {8, 16, 32}) {
+                    Shape t = sh;
+                    t.rows_per_tile = (256 / sh.LPR) * rpt;
+                    base.E = sh.E;
+                    base.LPR = sh.LPR;
+                    base.num_tiles = build_tiles(t, sys0, batch_outer);
+                    base.tiles = d_tiles.as<Tile>();
+                    base.init = false;
+                    base.unroll = 1;
+                    base.async_copy = true;
+                    cudaError_t const le = kpm::launch_diag_step(base, stream);
+                    if (le != cudaSuccess) {
+                        cudaGetLastError();
+                        base.async_copy = false;
+                        break;
+                    }
+                    KPM_CUDA(cudaEventRecord(ev0, stream));
+                    for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
+                    KPM_CUDA(cudaEventRecord(ev1, stream));
+                    KPM_CUDA(cudaEventSynchronize(ev1));
+                    float ms = 0;
+                    KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+                    last_tuning.push_back({static_cast<double>(t.rows_per_tile), -2.0, ms / 3});
+                    if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, 1, sh.E, sh.LPR, 0, true}; }
+                }
+            base.async_copy = false;
         }
         tuned.push_back({key, best});
         return best;
@@ -1108,9 +1137,14 @@ struct kpm_engine {
         KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
         a.error = d_pair_error.as<int>();
         bool const tma_ok = batch_outer && sh.E * vb == 16 && sh.LPR > 1 && !real_values;
+        bool const async_ok = batch_outer && sh.E * vb == 16 && W <= 4 && !real_values;
         if (cfg.staging == 2 && tma_ok) {
             sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 64;
             a.tma_rows = sh.rows_per_tile;
+            alt_map = true;
+        } else if (cfg.staging == 3 && async_ok) {
+            sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : (256 / sh.LPR) * 16;
+            a.async_copy = true;
             alt_map = true;
         } else if (cfg.tile_rows > 0) {
             sh.rows_per_tile = cfg.tile_rows;
@@ -1118,7 +1152,7 @@ struct kpm_engine {
             Tuned const tu = tune_diag(sh, sys0, batch_outer, a);
             sh.rows_per_tile = tu.rows_per_tile;
             a.unroll = tu.unroll;
-            alt_map = tu.E != sh.E || tu.tma_rows > 0;
+            alt_map = tu.E != sh.E || tu.tma_rows > 0 || tu.async_copy;
             if (alt_map && cfg.fuse_steps == 2 && !opt_rows) {  // two-step launches asked for: default kernel
                 alt_map = false;
                 sh.rows_per_tile = (256 / sh.LPR) * 16;
@@ -1127,6 +1161,7 @@ struct kpm_engine {
                 sh.E = tu.E;
                 sh.LPR = tu.LPR;
                 a.tma_rows = tu.tma_rows;
+                a.async_copy = tu.async_copy;
             }
             a.E = sh.E;
             a.LPR = sh.LPR;
@@ -1255,6 +1290,7 @@ struct kpm_engine {
             key.row_limit = a.row_limit;
             key.tma_rows = a.tma_rows;
             key.real_matrix = a.real_matrix;
+            key.async_copy = a.async_copy;
             key.error = a.error;
             if (graph_exec == nullptr || !(key == graph_key)) {
                 drop_graph();
@@ -1282,7 +1318,7 @@ struct kpm_engine {
         }
         while (n <= half) single_step();
         last_fuse = choice.steps;
-        last_tma_rows = a.tma_rows;
+        last_tma_rows = a.async_copy ? -sh.rows_per_tile : a.tma_rows;
         last_unroll = a.unroll;
         KPM_CUDA(cudaEventRecord(ev1, stream));
         KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
@@ -1417,7 +1453,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
-        if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
+        if (e->cfg.staging < 0 || e->cfg.staging > 3) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2 or 3");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
         *out = e.release();
     });

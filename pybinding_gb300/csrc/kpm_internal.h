@@ -45,6 +45,7 @@ struct DiagStep {
     int tma_rows = 0;         // > 0: TMA-staged kernel, tiles of at most this many rows (full rows only,
                               // K * element size a multiple of 16 bytes; col/val padded by 32 bytes)
     int* error = nullptr;     // TMA-staged kernel: set when a bounded wait gives up
+    bool async_copy = false;  // cp.async pipeline kernel (rows of <= 4 entries, 16-byte lanes; full rows)
     bool real_matrix = false; // complex vectors with real H~ values: val holds [rows][W][vs] of the
                               // real type (vs of that type: hi/lo pairs for FP32)
 };

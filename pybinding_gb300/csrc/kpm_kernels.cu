@@ -318,6 +318,187 @@ diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, in
         diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
 }
 
+// ------------------------------------------------------------------ diagonal step, cp.async pipeline
+// Per-thread asynchronous copies (cp.async, global -> shared) of the next row's x[r], y_old[r]
+// and gathered x[col] while the current row is computed from shared memory: each thread keeps
+// two rows in flight without holding their data in registers. The next row's column indices
+// and matrix values are prefetched into registers one row further ahead. Rows of at most 4
+// entries, 16-byte lanes.
+__device__ __forceinline__ void cp_async16_ca(void* smem, void const* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16_cg(void* smem, void const* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+constexpr int ASYNC_ITEMS = 6;  // x[r], y_old[r], 4 gathers
+
+template<class V, int E, int LPR>
+size_t diag_async_smem() {
+    using R = typename Tr<V>::R;
+    constexpr int NV = Tr<V>::C ? 3 : 2;
+    return static_cast<size_t>(2) * BLOCK * ASYNC_ITEMS * 16 + sizeof(R) * WARPS * E * LPR * NV;
+}
+
+template<class V, int E, int LPR, bool INIT>
+__global__ void __launch_bounds__(BLOCK)
+diag_async_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x_all,
+                  V* __restrict__ y_all, int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles,
+                  int nbatch, double* __restrict__ acc) {
+    using R = typename Tr<V>::R;
+    using P = Pack<V, E>;
+    static_assert(sizeof(P) == 16, "16-byte lanes");
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int VS = Tr<V>::VS;
+    constexpr int RPP = BLOCK / LPR;
+    constexpr int NV = CPLX ? 3 : 2;
+    extern __shared__ __align__(16) unsigned char async_smem[];
+    P* stage = reinterpret_cast<P*>(async_smem);  // [2][BLOCK][ASYNC_ITEMS]
+    R* red = reinterpret_cast<R*>(async_smem + static_cast<size_t>(2) * BLOCK * ASYNC_ITEMS * 16);
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    int const G = gridDim.x;
+    R m2[E], m3r[E], m3i[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+    int cur_sys = -1, cur_batch = -1;
+    auto slot_of = [&](int st, int item) -> P* { return stage + (st * BLOCK + threadIdx.x) * ASYNC_ITEMS + item; };
+
+    for (int ti = blockIdx.x; ti < num_tiles; ti += G) {
+        Tile const t = tiles[ti];
+        if (t.system != cur_sys || t.batch != cur_batch) {
+            if (cur_sys >= 0)
+                diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+            cur_sys = t.system;
+            cur_batch = t.batch;
+        }
+        V const* __restrict__ x = x_all + t.batch * batch_stride;
+        V* __restrict__ y = y_all + t.batch * batch_stride;
+        int const row_end = t.row_end;
+        // prefetched indices and values of the next row to issue
+        int32_t cn[4];
+        V vn[4 * VS];
+        auto fetch_meta = [&](int r) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                cn[q] = q < W ? __ldg(col + static_cast<int64_t>(r) * W + q) : 0;
+#pragma unroll
+                for (int v = 0; v < VS; ++v) {
+                    vzero(vn[q * VS + v]);
+                    if (q < W) vn[q * VS + v] = val[(static_cast<int64_t>(r) * W + q) * VS + v];
+                }
+            }
+        };
+        auto issue = [&](int r, int st) {
+            P const* xr = reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane;
+            cp_async16_ca(slot_of(st, 0), xr);
+            if (!INIT) cp_async16_cg(slot_of(st, 1), reinterpret_cast<P const*>(y + static_cast<int64_t>(r) * K) + lane);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (q < W) cp_async16_ca(slot_of(st, 2 + q), reinterpret_cast<P const*>(x + static_cast<int64_t>(cn[q]) * K) + lane);
+        };
+        int r = t.row_begin + slot;
+        int32_t cc[4];
+        V vc[4 * VS];
+        if (r < row_end) {
+            fetch_meta(r);
+            issue(r, 0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cc[q] = cn[q];
+#pragma unroll
+            for (int i = 0; i < 4 * VS; ++i) vc[i] = vn[i];
+        }
+        cp_async_commit();
+        if (r + RPP < row_end) fetch_meta(r + RPP);
+        for (int k = 0; r < row_end; ++k, r += RPP) {
+            int const st = k & 1;
+            int const rn = r + RPP;
+            int32_t cnn[4];
+            V vnn[4 * VS];
+            if (rn < row_end) {
+                issue(rn, st ^ 1);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cnn[q] = cn[q];
+#pragma unroll
+                for (int i = 0; i < 4 * VS; ++i) vnn[i] = vn[i];
+            }
+            cp_async_commit();
+            if (rn + RPP < row_end) fetch_meta(rn + RPP);
+            cp_async_wait1();  // this row's copies have landed (only the newest group may be pending)
+            P const xr = *slot_of(st, 0);
+            P yo;
+            if (!INIT) yo = *slot_of(st, 1);
+            V sum[E], lo[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(lo[e]); }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q >= W) continue;
+                P const xv = *slot_of(st, 2 + q);
+#pragma unroll
+                for (int e = 0; e < E; ++e) vfma(sum[e], vc[q * VS], xv.v[e]);
+                if (VS == 2) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) vfma(lo[e], vc[q * VS + 1], xv.v[e]);
+                }
+            }
+            P yn;
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
+                yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
+                m2[e] += vsq(xr.v[e]);
+                m3r[e] += vdre(yn.v[e], xr.v[e]);
+                if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
+            }
+            st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cc[q] = cnn[q];
+#pragma unroll
+            for (int i = 0; i < 4 * VS; ++i) vc[i] = vnn[i];
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    }
+    if (cur_sys >= 0)
+        diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+}
+
+template<class V, int E, int LPR>
+cudaError_t diag_async_launch(DiagStep const& a, cudaStream_t s) {
+    if (a.num_tiles == 0) return cudaSuccess;
+    if (a.W > 4) return cudaErrorInvalidValue;
+    size_t const smem = diag_async_smem<V, E, LPR>();
+    auto fn = a.init ? diag_async_kernel<V, E, LPR, true> : diag_async_kernel<V, E, LPR, false>;
+    static void const* done[16];
+    static int ndone = 0;
+    bool set = false;
+    for (int i = 0; i < ndone; ++i) set = set || done[i] == reinterpret_cast<void const*>(fn);
+    if (!set) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        if (ndone < 16) done[ndone++] = reinterpret_cast<void const*>(fn);
+    }
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, BLOCK, smem) != cudaSuccess || occ < 1) {
+        cudaGetLastError();
+        return cudaErrorInvalidConfiguration;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int const g = std::max(1, std::min(a.num_tiles, sms * occ));
+    fn<<<g, BLOCK, smem, s>>>(a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x), static_cast<V*>(a.y),
+                              a.batch_stride, a.tiles, a.num_tiles, a.nbatch, a.acc);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ diagonal step, TMA-staged
 // The contiguous operands of a tile (its y_old rows, its own x rows for the moment dots,
 // and its ELL indices and values) are prefetched into shared memory by bulk copies, up to
@@ -1251,6 +1432,13 @@ cudaError_t pair_launch(DiagPair const& a, cudaStream_t s) {
 template<class V, int E, int LPR>
 cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
+    if (a.async_copy) {
+        if (a.real_matrix || a.W > 4) return cudaErrorInvalidValue;
+        if constexpr (E * sizeof(V) == 16)
+            return diag_async_launch<V, E, LPR>(a, s);
+        else
+            return cudaErrorInvalidValue;
+    }
     if (a.tma_rows > 0) {
         if (a.real_matrix) return cudaErrorInvalidValue;
         if constexpr (E * sizeof(V) == 16 && LPR > 1)  // multi-vector rows of 16-byte lanes

@@ -359,8 +359,9 @@ def test_repeated_calls_replay_the_recursion_graph(dtype, nvec):
                                             (np.complex64, 32, 1e-5), (np.complex128, 8, 1e-10)])
 def test_tma_staged_step_matches_register_step_and_oracle(oracle, dtype, nvec, tol):
     """The TMA-staged diagonal step (bulk copies of y_old, own x rows and the ELL entries into
-    shared memory) against the register-load step and the FP64 oracle, on a ragged batch of
-    three flakes whose row offsets are not multiples of 4 (unaligned index and value copies)."""
+    shared memory) and the cp.async-pipelined step against the register-load step and the FP64
+    oracle, on a ragged batch of three flakes whose row offsets are not multiples of 4
+    (unaligned index and value copies)."""
     hs = [_disordered_flake(n, s, np.float64) for n, s in ((9001, 1), (4003, 2), (12007, 3))]
     if np.iscomplexobj(np.zeros(1, dtype)):
         hs = [(h + 1j * sp.triu(h, 1) * 0.1 - 1j * sp.tril(h, -1) * 0.1).tocsr() for h in hs]
@@ -371,18 +372,19 @@ def test_tma_staged_step_matches_register_step_and_oracle(oracle, dtype, nvec, t
     starters = [oracle.random_starters(h.shape[0], nvec, dtype) for h in hs]
     flat = np.concatenate([st.ravel() for st in starters])
     out = {}
-    for staging in ("tma", "registers"):
+    for staging in ("tma", "async", "registers"):
         batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, staging=staging)
         out[staging] = batch.engine.moments_diag(M, flat)
         st = batch.engine.stats()
         assert (st.staged_rows > 0) == (staging == "tma"), st.staged_rows
+        assert (st.staged_rows < 0) == (staging == "async"), st.staged_rows
         out[staging + "2"] = batch.engine.moments_diag(M, flat)  # replayed recursion graph
     for s, h in enumerate(hs):
         h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
         r = oracle.optimize(h64, [0], [0], a, b)
         ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(h64.dtype), r["reorder_map"]), M,
                                   slices=r["slices"])
-        for k in ("tma", "tma2", "registers", "registers2"):
+        for k in ("tma", "tma2", "async", "async2", "registers", "registers2"):
             err = rel_err(out[k][s], ref)
             print("%s %s system %d: %.3e" % (np.dtype(dtype).name, k, s, err))
             assert err <= tol
