@@ -27,6 +27,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -849,26 +850,52 @@ struct kpm_engine {
     // the recursion; the INIT form needs fewer registers and times differently). Only x1 and
     // the first accumulator slot change; the init step that follows overwrites x1 and the
     // caller clears the accumulators again. Cached per shape.
+    // Choices are kept process-wide: a new engine on a matrix of the same size, width and
+    // non-zero count (e.g. another disorder realisation) reuses them instead of timing again.
     struct TuneKey {
         int vtype, E, LPR, nbatch;
-        int64_t rows;
-        bool batch_outer;
+        int64_t rows, nnz;
+        int W, staging, device;
+        bool batch_outer, real;
         bool operator==(TuneKey const& o) const {
             return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows &&
-                   batch_outer == o.batch_outer;
+                   nnz == o.nnz && W == o.W && staging == o.staging && device == o.device &&
+                   batch_outer == o.batch_outer && real == o.real;
         }
     };
+    TuneKey tune_key(Shape const& sh, bool batch_outer) const {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, batch_outer, real_values};
+    }
     struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; bool async_copy; };
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
-    std::vector<std::pair<TuneKey, FuseChoice>> fuse_tuned;
-    std::vector<std::pair<TuneKey, Tuned>> tuned;
+    template<class T>
+    struct SharedCache {
+        std::mutex m;
+        std::vector<std::pair<TuneKey, T>> v;
+        bool find(TuneKey const& k, T& out) {
+            std::lock_guard<std::mutex> lock(m);
+            for (auto const& e : v)
+                if (e.first == k) { out = e.second; return true; }
+            return false;
+        }
+        void put(TuneKey const& k, T const& t) {
+            std::lock_guard<std::mutex> lock(m);
+            v.push_back({k, t});
+        }
+    };
+    static SharedCache<Tuned>& tuned() { static SharedCache<Tuned> c; return c; }
+    static SharedCache<FuseChoice>& fuse_tuned() { static SharedCache<FuseChoice> c; return c; }
     std::vector<std::array<double, 3>> last_tuning;  // (rows per tile, unroll, ms) of the last tuning run
 
     Tuned tune_diag(Shape sh, bool sys0, bool batch_outer, kpm::DiagStep base) {
-        TuneKey const key{vtype, sh.E, sh.LPR, sh.nbatch, rows, batch_outer};
-        for (auto const& t : tuned)
-            if (t.first == key) return t.second;
+        TuneKey const key = tune_key(sh, batch_outer);
+        {
+            Tuned hit{};
+            if (tuned().find(key, hit)) return hit;
+        }
         Tuned best{(256 / sh.LPR) * 16, 1, sh.E, sh.LPR, 0, false};
         // lane mappings of this K: the default (16 bytes per lane) and, when the row allows,
         // half the elements per lane over twice the lanes
@@ -959,7 +986,7 @@ struct kpm_engine {
                 }
             base.async_copy = false;
         }
-        tuned.push_back({key, best});
+        tuned().put(key, best);
         return best;
     }
 
@@ -1231,10 +1258,8 @@ struct kpm_engine {
         int const rpp = 256 / sh.LPR;
         bool const can_pair = !opt_rows && cfg.fuse_steps != 1 && !alt_map;
         FuseChoice choice{1, 0};
-        TuneKey const fkey{vtype, sh.E, sh.LPR, sh.nbatch, rows, batch_outer};
-        bool have_choice = false;
-        for (auto const& f : fuse_tuned)
-            if (f.first == fkey) { choice = f.second; have_choice = true; }
+        TuneKey const fkey = tune_key(sh, batch_outer);
+        bool have_choice = fuse_tuned().find(fkey, choice);
         if (can_pair && cfg.fuse_steps == 2 && !have_choice) {
             choice = FuseChoice{2, cfg.tile_rows > 0 ? cfg.tile_rows : rpp * 8};
             have_choice = true;
@@ -1256,7 +1281,7 @@ struct kpm_engine {
                     KPM_CUDA(cudaEventElapsedTime(&ms, ev_t0, ev_t1));
                     if (ms < best) { best = ms; choice = c; }
                 }
-                fuse_tuned.push_back({fkey, choice});
+                fuse_tuned().put(fkey, choice);
             } else {
                 choice = FuseChoice{1, 0};
             }
