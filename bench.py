@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--no-error", action="store_true", help="skip the FP64 moment-error check")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of one CPU sample")
     p.add_argument("--cond-sites", type=int, default=1_000_000, help="sites of the conductivity workload")
+    p.add_argument("--cond-precision", default="auto", choices=["auto", "fp32"],
+                   help="conductivity recursion: auto (complex128 for the complex128 H) or fp32 (complex64 "
+                        "vectors; the line then also reports sigma's deviation from an FP64 run)")
     p.add_argument("--adj-sites", type=int, default=256_000, help="sites of the adjoint workload")
     p.add_argument("--cube", type=int, default=160, help="edge of the 3D Anderson cube")
     p.add_argument("--cube-vectors", type=int, default=256, help="vectors of the 3D Anderson workload")
@@ -485,13 +488,20 @@ def workload_conductivity(args, stream_of):
                          is_double=True)
     h = m.hamiltonian.astype(np.complex128)
     x = m.system.x
-    eng = _native.Engine(h, _native.make_config(energy_range=(-9.0, 9.0)))
+    eng = _native.Engine(h, _native.make_config(energy_range=(-9.0, 9.0), precision=args.cond_precision))
     a, b = eng.scaling_factors()
     broadening = _jackson_broadening(512, a)
     chem = np.linspace(-1.5, 1.5, 31)
     stream = stream_of(eng)
     t, wall, clk, outs = _timed(lambda: eng.calc_conductivity(x, x, chem, broadening, 0.0, 16, 1000, gemm_mode=1),
                                 args.steps, args.warmup, stream)
+    deviation = None
+    if args.cond_precision == "fp32":  # sigma against the complex128 recursion (same tensor-core GEMM)
+        e64 = _native.Engine(h, _native.make_config(energy_range=(-9.0, 9.0), precision="fp64"))
+        s64 = e64.calc_conductivity(x, x, chem, broadening, 0.0, 16, 1000, gemm_mode=1).real
+        e64.close()
+        deviation = float(np.max(np.abs(outs[-1].real - s64)) / np.max(np.abs(s64)))
+        eng.calc_conductivity(x, x, chem, broadening, 0.0, 16, 1000, gemm_mode=1)  # stats of this engine again
     st = eng.stats()
     M = st.num_moments
     n = h.shape[0]
@@ -509,7 +519,7 @@ def workload_conductivity(args, stream_of):
                        % n,
            "sites": int(n), "nnz": int(h.nnz), "moments": int(M), "vectors": 16, "broadening_eV": broadening,
            "gemm": "tcgen05 kind::tf32, hi/lo split (3 products), FP32 planes, FP64 slice sums"},
-          "c128 recursion, tf32x3 GEMM",
+          ("c64" if args.cond_precision == "fp32" else "c128") + " recursion, tf32x3 GEMM",
           roofline={"bound": "tensor", "achieved": tensor / gemm / 1e12, "peak": peak_tf32, "unit": "TFLOP/s",
                     "frac": tensor / gemm / 1e12 / peak_tf32, "traffic": None,
                     "kernel": "mu_gemm_tc_kernel<true>",
@@ -519,7 +529,7 @@ def workload_conductivity(args, stream_of):
                      "reconstruction_and_host_s": t / args.steps - st.moments_time},
           e2e={"value": wall / args.steps, "unit": "s", "h2d_bytes_per_step": int(8 * n + 8 * 31),
                "d2h_bytes_per_step": int(16 * 31)},
-          sigma_sample=[float(v.real) for v in outs[-1][:5]], clocks=clk,
+          sigma_sample=[float(v.real) for v in outs[-1][:5]], sigma_rel_deviation_vs_fp64=deviation, clocks=clk,
           gpu_launches=int(args.steps * (2 * (M + 2) + 6)))
 
 

@@ -1227,7 +1227,10 @@ __global__ void kubo_integrate_kernel(double const* __restrict__ sum_nm, double 
     double const mu = chem[j];
     double tr = 0.0, ti = 0.0;
     for (int e = 0; e < ns; ++e) {
-        double const fd = 1.0 / (1.0 + exp((samples[e] - mu) * inv_kbt));
+        // Fermi-Dirac; at T = 0 (inv_kbt infinite) the step function, 1/2 on the edge, where the
+        // reference's formula (reconstruct.hpp:126-128) evaluates 0 * inf and returns NaN
+        double const fd = isinf(inv_kbt) ? (samples[e] < mu ? 1.0 : (samples[e] > mu ? 0.0 : 0.5))
+                                         : 1.0 / (1.0 + exp((samples[e] - mu) * inv_kbt));
         double const w = (e == 0 || e == ns - 1) ? 1.0 : 2.0;
         tr += w * fd * sum_nm[2 * e];
         ti += w * fd * sum_nm[2 * e + 1];

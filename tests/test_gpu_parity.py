@@ -451,3 +451,24 @@ def test_disconnected_system(oracle):
     r = oracle.optimize(h, [site], [site], a, b)
     opt = eng.optimized_hamiltonian([site], [site])
     assert np.array_equal(opt["reorder_map"], r["reorder_map"])
+
+
+def test_conductivity_zero_temperature_on_a_sample_energy(oracle):
+    """At T = 0 a chemical potential that coincides with an energy sample (here mu = -1.0 and
+    linspace(-9, 9, 1000) holds -1.0 exactly) makes the reference's Fermi factor 0 * inf = NaN;
+    the engine uses the step function with 1/2 on the edge: finite, and equal to the oracle
+    everywhere else."""
+    m = TM.graphene("magnetic_field", 6)
+    h = m.hamiltonian.astype(np.complex128)
+    x = m.system.x
+    cfg = dict(energy_range=(-9.0, 9.0), kernel="jackson")
+    eng = _native.Engine(h, _native.make_config(**cfg))
+    chem = np.array([-1.0, -0.987, 0.5])
+    got = eng.calc_conductivity(x, x, chem, 0.6, 0.0, 2, 1000)
+    assert np.all(np.isfinite(got))
+    ref = oracle.core_conductivity(h, x, x, chem, 0.6, 0.0, 2, 1000, matrix_format="ELL", optimal_size=False,
+                                   interleaved=False, **cfg)
+    assert np.isnan(ref[0])  # the reference's behaviour at this point
+    assert rel_err(got[1:], ref[1:]) < 1e-9
+    near = eng.calc_conductivity(x, x, np.array([-1.0 - 1e-9, -1.0 + 1e-9]), 0.6, 0.0, 2, 1000)
+    assert min(near.real) - 1e-9 * abs(near.real).max() <= got[0].real <= max(near.real) + 1e-9 * abs(near.real).max()
