@@ -199,6 +199,21 @@ int kpm_calc_conductivity(kpm_engine* engine, const float* left_coords, const fl
                           double temperature, int64_t num_random, int64_t num_points, int32_t gemm_mode,
                           double* out);
 
+/* The two halves of kpm_calc_conductivity, for callers that keep or combine moments.
+ * kpm_conductivity_moments: the Kubo-Bastin moments matrix of system 0 as Core::conductivity
+ * builds it before damping (Core.cpp:119-145: DenseMatrixMoments of both sides,
+ * MomentMultiplication::matrix_mul_add and normalize, Moments.cpp:92-126):
+ * mu[m][n] = sum_r L_m conj(R_n) / num_random, row and column 0 halved; num_moments as given
+ * (no rounding); out: num_moments^2 complex, column n at out + 2 n num_moments; gemm_mode
+ * as for kpm_calc_conductivity.
+ * kpm_kubo_bastin: reconstruct<KuboBastin> (reconstruct.hpp:90-143) of a DAMPED moments
+ * matrix (multiply by g_m g_n, kpm_damping_coefficients) over num_points energy samples of
+ * the engine's bounds and its scaling; out: num_mu complex. */
+int kpm_conductivity_moments(kpm_engine* engine, const float* left_coords, const float* right_coords,
+                             int64_t num_moments, int64_t num_random, int32_t gemm_mode, double* out);
+int kpm_kubo_bastin(kpm_engine* engine, const double* moments, int64_t num_moments, const double* chemical_potential,
+                    int64_t num_mu, double temperature, int64_t num_points, double* out);
+
 /* Reverse-mode (adjoint) gradient of the averaged diagonal moments, system 0, real
  * Hamiltonians. No reference counterpart: pybinding has no gradients; the forward
  * algorithm differentiated is cpb's diagonal recursion (kpm/calc_moments.hpp:35-58,

@@ -63,6 +63,8 @@ SIGNATURES = {
     "kpm_moments": (_I32, [_P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _P]),
     "kpm_calc_conductivity": (_I32, [_P, _P, _P, _P, _I64, _D, _D, _I64, _I64, _I32, _P]),
     "kpm_adjoint_diag": (_I32, [_P, _I64, _I64, _P, _P, _I64, _P, _P, _P]),
+    "kpm_conductivity_moments": (_I32, [_P, _P, _P, _I64, _I64, _I32, _P]),
+    "kpm_kubo_bastin": (_I32, [_P, _P, _I64, _P, _I64, _D, _I64, _P]),
     "kpm_get_stats": (_I32, [_P, _P]),
     "kpm_report": (_I32, [_P, _I32, _P, _I64]),
     "kpm_optimized_hamiltonian": (_I32, [_P, _P, _I64, _P, _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
@@ -274,6 +276,26 @@ class Engine:
         check(lib().kpm_calc_conductivity(self._h, ptr(l_), ptr(r_), ptr(mu), mu.size, float(broadening),
                                           float(temperature), int(num_random), int(num_points), int(gemm_mode),
                                           ptr(out)))
+        return out
+
+    def conductivity_moments(self, left, right, num_moments, num_random, gemm_mode=0):
+        """Undamped Kubo-Bastin moments matrix (num_moments, num_moments) complex: mu[m, n]."""
+        l_ = np.ascontiguousarray(left, np.float32)
+        r_ = np.ascontiguousarray(right, np.float32)
+        M = int(num_moments)
+        out = np.empty((M, M), np.complex128)  # row n = column n of mu
+        check(lib().kpm_conductivity_moments(self._h, ptr(l_), ptr(r_), M, int(num_random), int(gemm_mode), ptr(out)))
+        return out.T.copy()
+
+    def kubo_bastin(self, moments, chemical_potential, temperature, num_points):
+        """Kubo-Bastin conductivity (complex) from a damped moments matrix mu[m, n]."""
+        m = np.asarray(moments, np.complex128)
+        M = m.shape[0]
+        col_major = np.ascontiguousarray(m.T)  # column n contiguous
+        mu = np.ascontiguousarray(np.atleast_1d(chemical_potential), np.float64)
+        out = np.empty(mu.size, np.complex128)
+        check(lib().kpm_kubo_bastin(self._h, ptr(col_major), M, ptr(mu), mu.size, float(temperature), int(num_points),
+                                    ptr(out)))
         return out
 
     def adjoint_diag(self, num_moments, starters, dl_dmu, checkpoint=0):

@@ -1869,19 +1869,21 @@ int kpm_moments(kpm_engine* e, int64_t num_moments, const double* alpha, int64_t
     });
 }
 
-int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, const double* chem, int64_t nmu,
-                          double broadening, double temperature, int64_t num_random, int64_t num_points,
-                          int32_t gemm_mode, double* out) {
-    return guarded([&] {
-        if (!e) fail(KPM_ERR_VALUE, "null engine");
+namespace {
+
+// The Kubo-Bastin moments matrix of system 0 (Core.cpp:119-145 up to normalize):
+// mu[m][n] = sum_r L_m conj(R_n) / num_random with L_n = T_n(H~) V_l r and R_n = V_r T_n(H~) r
+// (kpm/Moments.cpp:92-126), row and column 0 halved as the collectors store T_0 / 2,
+// undamped; complex double, column n of M entries at mu + 2 n M. Returns the recursion and
+// GEMM device times.
+void conductivity_mu(kpm_engine* e, const float* left, const float* right, int64_t M, int64_t num_random,
+                     int32_t gemm_mode, std::vector<double>& mu, double& rec_time, double& gemm_time) {
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "conductivity needs a single-system engine");
-        if (!left || !right || (nmu > 0 && (!chem || !out))) fail(KPM_ERR_VALUE, "null argument");
-        if (num_random < 1 || num_points < 2) fail(KPM_ERR_VALUE, "num_random >= 1 and num_points >= 2 required");
+        if (!left || !right) fail(KPM_ERR_VALUE, "null argument");
+        if (num_random < 1) fail(KPM_ERR_VALUE, "num_random must be >= 1");
+        if (M < 2) fail(KPM_ERR_VALUE, "num_moments must be >= 2");
         if (gemm_mode != 0 && gemm_mode != 1) fail(KPM_ERR_VALUE, "gemm_mode must be 0 (FP64) or 1 (tensor cores)");
         bool const tc = gemm_mode == 1;
-        double const t0 = now_s();
-        auto const sc = e->scale(0);
-        int64_t const M = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / sc.a);
         e->optimize({0}, {0});
         int64_t const n = e->rows;
         int const vt = e->vtype;
@@ -1988,7 +1990,7 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         d_mu_acc.ensure(sizeof(double) * 2 * M * M);
         KPM_CUDA(cudaMemsetAsync(d_mu_acc.p, 0, sizeof(double) * 2 * M * M, e->stream));
         int const ntiles = e->build_tiles(sh, true);
-        double rec_time = 0;
+        rec_time = 0;
         auto recursion = [&](unsigned char const* host_starters, bool right_side) {
             void const* src = e->device_view(host_starters, static_cast<size_t>(K) * n * ssize);
             KPM_CUDA(cudaMemsetAsync(e->d_x0.p, 0, vec_bytes, e->stream));
@@ -2034,7 +2036,7 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
             KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
             rec_time += ms * 1e-3;
         };
-        double gemm_time = 0;
+        gemm_time = 0;
         for (int64_t b = 0; b < nrand_pad / K; ++b) {
             recursion(starters_l.data() + static_cast<size_t>(b) * K * n * ssize, false);
             recursion(starters_r.data() + static_cast<size_t>(b) * K * n * ssize, true);
@@ -2060,22 +2062,32 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
             KPM_CUDA(cudaMemcpy(&herr, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
             if (herr != 0) fail(KPM_ERR_TIMEOUT, "tensor-core moments GEMM: a bounded device wait expired");
         }
-        // normalise, halve row/column 0 (the collectors store T_0 / 2), damp g_m g_n (Kernel.hpp:48-56)
-        std::vector<double> mu(static_cast<size_t>(2 * M * M));
+        // normalise by the vectors, halve row/column 0 (the collectors store T_0 / 2)
+        mu.assign(static_cast<size_t>(2 * M * M), 0.0);
         KPM_CUDA(cudaMemcpy(mu.data(), d_mu_acc.p, sizeof(double) * mu.size(), cudaMemcpyDeviceToHost));
-        auto g = damping(e->cfg.kernel, e->cfg.kernel_param, M);
         for (int64_t c = 0; c < M; ++c)
             for (int64_t r = 0; r < M; ++r) {
-                double f = g[r] * g[c] / static_cast<double>(num_random);
+                double f = 1.0 / static_cast<double>(num_random);
                 if (r == 0) f *= 0.5;
                 if (c == 0) f *= 0.5;
                 mu[2 * (c * M + r)] *= f;
                 mu[2 * (c * M + r) + 1] *= f;
             }
-        KPM_CUDA(cudaMemcpy(d_mu_acc.p, mu.data(), sizeof(double) * mu.size(), cudaMemcpyHostToDevice));
+}
+
+// KuboBastin (reconstruct.hpp:90-143) of a damped moments matrix over bounds.linspaced(num_points)
+// of system 0, on the GPU in FP64; out: nmu complex values.
+void kubo_bastin(kpm_engine* e, double const* mu, int64_t M, const double* chem, int64_t nmu, double temperature,
+                 int64_t num_points, double* out) {
+        if (num_points < 2) fail(KPM_ERR_VALUE, "num_points >= 2 required");
+        if (nmu > 0 && (!chem || !out)) fail(KPM_ERR_VALUE, "null argument");
+        auto const sc = e->scale(0);
+        DBuf d_mu, d_samples, d_sum, d_chem, d_res;
+        d_mu.ensure(sizeof(double) * 2 * M * M);
+        KPM_CUDA(cudaMemcpyAsync(d_mu.p, mu, sizeof(double) * 2 * M * M, cudaMemcpyHostToDevice, e->stream));
         // energy samples: bounds.linspaced(num_points) scaled (reconstruct.hpp:101-103)
         auto const& bs = e->sys[0];
-        std::vector<double> samples(num_points), chem_s(nmu);
+        std::vector<double> samples(num_points), chem_s(std::max<int64_t>(nmu, 1));
         for (int64_t i = 0; i < num_points; ++i)
             samples[i] = (bs.emin + (bs.emax - bs.emin) * static_cast<double>(i) / static_cast<double>(num_points - 1) - sc.b) / sc.a;
         samples[num_points - 1] = (bs.emax - sc.b) / sc.a;
@@ -2091,17 +2103,76 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
         d_res.ensure(sizeof(double) * 2 * std::max<int64_t>(nmu, 1));
         KPM_CUDA(cudaMemcpyAsync(d_samples.p, samples.data(), sizeof(double) * num_points, cudaMemcpyHostToDevice, e->stream));
         KPM_CUDA(cudaMemcpyAsync(d_chem.p, chem_s.data(), sizeof(double) * nmu, cudaMemcpyHostToDevice, e->stream));
-        KPM_CUDA(kpm::launch_kubo_sum(d_mu_acc.as<double>(), M, d_samples.as<double>(), static_cast<int>(num_points),
+        KPM_CUDA(kpm::launch_kubo_sum(d_mu.as<double>(), M, d_samples.as<double>(), static_cast<int>(num_points),
                                       d_sum.as<double>(), e->stream));
         KPM_CUDA(kpm::launch_kubo_integrate(d_sum.as<double>(), d_samples.as<double>(), static_cast<int>(num_points),
                                             d_chem.as<double>(), static_cast<int>(nmu), inv_kbt, coeff, prefix,
                                             d_res.as<double>(), e->stream));
-        KPM_CUDA(cudaMemcpyAsync(out, d_res.p, sizeof(double) * 2 * nmu, cudaMemcpyDeviceToHost, e->stream));
+        if (nmu > 0)
+            KPM_CUDA(cudaMemcpyAsync(out, d_res.p, sizeof(double) * 2 * nmu, cudaMemcpyDeviceToHost, e->stream));
         KPM_CUDA(cudaStreamSynchronize(e->stream));
+}
+
+void apply_matrix_damping(kpm_engine* e, std::vector<double>& mu, int64_t M) {  // g_m g_n (Kernel.hpp:48-56)
+    auto g = damping(e->cfg.kernel, e->cfg.kernel_param, M);
+    for (int64_t c = 0; c < M; ++c)
+        for (int64_t r = 0; r < M; ++r) {
+            mu[2 * (c * M + r)] *= g[r] * g[c];
+            mu[2 * (c * M + r) + 1] *= g[r] * g[c];
+        }
+}
+
+}  // namespace
+
+int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, const double* chem, int64_t nmu,
+                          double broadening, double temperature, int64_t num_random, int64_t num_points,
+                          int32_t gemm_mode, double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (!left || !right || (nmu > 0 && (!chem || !out))) fail(KPM_ERR_VALUE, "null argument");
+        if (num_random < 1 || num_points < 2) fail(KPM_ERR_VALUE, "num_random >= 1 and num_points >= 2 required");
+        double const t0 = now_s();
+        auto const sc = e->scale(0);
+        int64_t const M = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / sc.a);
+        std::vector<double> mu;
+        double rec_time = 0, gemm_time = 0;
+        conductivity_mu(e, left, right, M, num_random, gemm_mode, mu, rec_time, gemm_time);
+        apply_matrix_damping(e, mu, M);
+        kubo_bastin(e, mu.data(), M, chem, nmu, temperature, num_points, out);
         e->st.moments_time = rec_time + gemm_time;
         e->reset_stats(M, false, false, static_cast<double>(num_random) * 2, 0);
         e->finish_stats();
         e->st.gemm_time = gemm_time;
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_conductivity_moments(kpm_engine* e, const float* left, const float* right, int64_t num_moments,
+                             int64_t num_random, int32_t gemm_mode, double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (!out) fail(KPM_ERR_VALUE, "null output");
+        double const t0 = now_s();
+        std::vector<double> mu;
+        double rec_time = 0, gemm_time = 0;
+        conductivity_mu(e, left, right, num_moments, num_random, gemm_mode, mu, rec_time, gemm_time);
+        std::memcpy(out, mu.data(), sizeof(double) * mu.size());
+        e->st.moments_time = rec_time + gemm_time;
+        e->reset_stats(num_moments, false, false, static_cast<double>(num_random) * 2, 0);
+        e->finish_stats();
+        e->st.gemm_time = gemm_time;
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_kubo_bastin(kpm_engine* e, const double* mu, int64_t num_moments, const double* chem, int64_t nmu,
+                    double temperature, int64_t num_points, double* out) {
+    return guarded([&] {
+        if (!e || !mu) fail(KPM_ERR_VALUE, "null argument");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "conductivity needs a single-system engine");
+        if (num_moments < 1) fail(KPM_ERR_VALUE, "num_moments must be >= 1");
+        double const t0 = now_s();
+        kubo_bastin(e, mu, num_moments, chem, nmu, temperature, num_points, out);
         e->calc_time = now_s() - t0;
     });
 }

@@ -472,3 +472,25 @@ def test_conductivity_zero_temperature_on_a_sample_energy(oracle):
     assert rel_err(got[1:], ref[1:]) < 1e-9
     near = eng.calc_conductivity(x, x, np.array([-1.0 - 1e-9, -1.0 + 1e-9]), 0.6, 0.0, 2, 1000)
     assert min(near.real) - 1e-9 * abs(near.real).max() <= got[0].real <= max(near.real) + 1e-9 * abs(near.real).max()
+
+
+@pytest.mark.parametrize("gemm_mode", [0, 1])
+def test_conductivity_in_two_parts(oracle, gemm_mode):
+    """kpm_conductivity_moments + damping + kpm_kubo_bastin == kpm_calc_conductivity, and (FP64
+    GEMM) equals the oracle's Core::conductivity."""
+    m = TM.graphene("magnetic_field", 6)
+    h = m.hamiltonian.astype(np.complex128)
+    x, y = m.system.x, m.system.y
+    cfg = dict(energy_range=(-9.0, 9.0), kernel="jackson")
+    eng = _native.Engine(h, _native.make_config(**cfg))
+    chem = np.linspace(-1.9, 2.1, 9)
+    whole = eng.calc_conductivity(x, y, chem, 0.6, 0.0, 2, 100, gemm_mode=gemm_mode)
+    M = eng.stats().num_moments
+    mu = eng.conductivity_moments(x, y, M, 2, gemm_mode=gemm_mode)
+    g = _native.damping_coefficients("jackson", 4.0, M)
+    parts = eng.kubo_bastin(mu * g[:, None] * g[None, :], chem, 0.0, 100)
+    assert rel_err(parts, whole) < 1e-12
+    if gemm_mode == 0:
+        ref = oracle.core_conductivity(h, x, y, chem, 0.6, 0.0, 2, 100, matrix_format="ELL", optimal_size=False,
+                                       interleaved=False, **cfg)
+        assert rel_err(parts, ref) < 1e-9
