@@ -856,17 +856,17 @@ struct kpm_engine {
         int vtype, E, LPR, nbatch;
         int64_t rows, nnz;
         int W, staging, device;
-        bool batch_outer, real;
+        bool full_rows, real;
         bool operator==(TuneKey const& o) const {
             return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows &&
                    nnz == o.nnz && W == o.W && staging == o.staging && device == o.device &&
-                   batch_outer == o.batch_outer && real == o.real;
+                   full_rows == o.full_rows && real == o.real;
         }
     };
-    TuneKey tune_key(Shape const& sh, bool batch_outer) const {
+    TuneKey tune_key(Shape const& sh, bool full_rows) const {
         int dev = 0;
         cudaGetDevice(&dev);
-        return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, batch_outer, real_values};
+        return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, full_rows, real_values};
     }
     struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; bool async_copy; };
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
@@ -890,8 +890,15 @@ struct kpm_engine {
     static SharedCache<FuseChoice>& fuse_tuned() { static SharedCache<FuseChoice> c; return c; }
     std::vector<std::array<double, 3>> last_tuning;  // (rows per tile, unroll, ms) of the last tuning run
 
-    Tuned tune_diag(Shape sh, bool sys0, bool batch_outer, kpm::DiagStep base) {
-        TuneKey const key = tune_key(sh, batch_outer);
+    static Shape first_batch(Shape t) {
+        t.nbatch = 1;
+        return t;
+    }
+
+    Tuned tune_diag(Shape sh, bool sys0, bool batch_outer, bool full_rows, kpm::DiagStep base) {
+        // candidates are timed on the first vector batch only: every batch does the same work,
+        // and a multi-batch launch would make the timing cost scale with the batch count
+        TuneKey const key = tune_key(sh, full_rows);
         {
             Tuned hit{};
             if (tuned().find(key, hit)) return hit;
@@ -915,7 +922,7 @@ struct kpm_engine {
                         t.rows_per_tile = (256 / t.LPR) * rpt;
                         base.E = t.E;
                         base.LPR = t.LPR;
-                        base.num_tiles = build_tiles(t, sys0, batch_outer);
+                        base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
                         base.tiles = d_tiles.as<Tile>();
                         base.init = false;
                         base.unroll = unroll;
@@ -930,14 +937,14 @@ struct kpm_engine {
                         if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR, 0, false}; }
                     }
             // the TMA-staged kernel (full rows, 16-byte lanes): tile heights that fit in shared memory
-            if (cfg.staging != 1 && batch_outer && sh.E * kpm::vtype_bytes(vtype) == 16 && sh.LPR > 1 &&
+            if (cfg.staging != 1 && full_rows && sh.E * kpm::vtype_bytes(vtype) == 16 && sh.LPR > 1 &&
                 base.error != nullptr && !base.real_matrix)
                 for (int tr : {32, 64, 128}) {
                     Shape t = sh;
                     t.rows_per_tile = tr;
                     base.E = sh.E;
                     base.LPR = sh.LPR;
-                    base.num_tiles = build_tiles(t, sys0, batch_outer);
+                    base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
                     base.tiles = d_tiles.as<Tile>();
                     base.init = false;
                     base.unroll = 1;
@@ -958,13 +965,13 @@ struct kpm_engine {
                 }
             base.tma_rows = 0;
             // the cp.async pipeline kernel (rows of at most 4 entries, 16-byte lanes)
-            if (cfg.staging != 1 && batch_outer && W <= 4 && sh.E * kpm::vtype_bytes(vtype) == 16 && !base.real_matrix)
+            if (cfg.staging != 1 && full_rows && W <= 4 && sh.E * kpm::vtype_bytes(vtype) == 16 && !base.real_matrix)
                 for (int rpt : {8, 16, 32}) {
                     Shape t = sh;
                     t.rows_per_tile = (256 / sh.LPR) * rpt;
                     base.E = sh.E;
                     base.LPR = sh.LPR;
-                    base.num_tiles = build_tiles(t, sys0, batch_outer);
+                    base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
                     base.tiles = d_tiles.as<Tile>();
                     base.init = false;
                     base.unroll = 1;
@@ -1123,7 +1130,10 @@ struct kpm_engine {
         size_t const step_acc = static_cast<size_t>(ns) * sh.nbatch * sh.K * NV;
         d_acc.ensure(sizeof(double) * step_acc * half);
         d_mu.ensure(sizeof(double) * 2 * ns * nvec * M);
-        bool const batch_outer = !opt_rows;
+        // tiles batch-outermost (L2 then holds one batch's gather window); with a shrinking row
+        // limit the tiles beyond it are launched and do nothing (the kernel clips rows)
+        bool const batch_outer = true;
+        bool const full_rows = !opt_rows;  // the TMA and cp.async kernels do not clip rows
         int ntiles = build_tiles(sh, sys0, batch_outer);
 
         KPM_CUDA(cudaEventRecord(ev_u0, stream));
@@ -1163,8 +1173,8 @@ struct kpm_engine {
         d_pair_error.ensure(sizeof(int));
         KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
         a.error = d_pair_error.as<int>();
-        bool const tma_ok = batch_outer && sh.E * vb == 16 && sh.LPR > 1 && !real_values;
-        bool const async_ok = batch_outer && sh.E * vb == 16 && W <= 4 && !real_values;
+        bool const tma_ok = full_rows && sh.E * vb == 16 && sh.LPR > 1 && !real_values;
+        bool const async_ok = full_rows && sh.E * vb == 16 && W <= 4 && !real_values;
         if (cfg.staging == 2 && tma_ok) {
             sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 64;
             a.tma_rows = sh.rows_per_tile;
@@ -1176,7 +1186,7 @@ struct kpm_engine {
         } else if (cfg.tile_rows > 0) {
             sh.rows_per_tile = cfg.tile_rows;
         } else {
-            Tuned const tu = tune_diag(sh, sys0, batch_outer, a);
+            Tuned const tu = tune_diag(sh, sys0, batch_outer, full_rows, a);
             sh.rows_per_tile = tu.rows_per_tile;
             a.unroll = tu.unroll;
             alt_map = tu.E != sh.E || tu.tma_rows > 0 || tu.async_copy;
@@ -1215,9 +1225,12 @@ struct kpm_engine {
             if (opt_rows) {
                 int32_t const lim = optimal_size(n, M);
                 a.row_limit = lim;
-                // tiles are ordered [tile][batch]: launch those that start below the limit
-                int64_t const t = (lim + sh.rows_per_tile - 1) / sh.rows_per_tile;
-                a.num_tiles = static_cast<int>(std::min<int64_t>(ntiles, t * sh.nbatch));
+                // one batch: the tiles that start below the limit are a prefix of the list;
+                // several (batch-outer order): all are launched, rows beyond the limit are skipped
+                if (sh.nbatch == 1) {
+                    int64_t const t = (lim + sh.rows_per_tile - 1) / sh.rows_per_tile;
+                    a.num_tiles = static_cast<int>(std::min<int64_t>(ntiles, t));
+                }
             }
             KPM_CUDA(kpm::launch_diag_step(a, stream));
             std::swap(r0, r1);
@@ -1258,7 +1271,7 @@ struct kpm_engine {
         int const rpp = 256 / sh.LPR;
         bool const can_pair = !opt_rows && cfg.fuse_steps != 1 && !alt_map;
         FuseChoice choice{1, 0};
-        TuneKey const fkey = tune_key(sh, batch_outer);
+        TuneKey const fkey = tune_key(sh, full_rows);
         bool have_choice = fuse_tuned().find(fkey, choice);
         if (can_pair && cfg.fuse_steps == 2 && !have_choice) {
             choice = FuseChoice{2, cfg.tile_rows > 0 ? cfg.tile_rows : rpp * 8};
