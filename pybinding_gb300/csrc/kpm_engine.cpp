@@ -203,17 +203,26 @@ int64_t required_moments(int kernel, double lambda, double scaled_broadening) {
 // ------------------------------------------------------------------ tridiagonal extremes
 // Extreme eigenvalues of the symmetric tridiagonal (alpha, beta[0..k-2]) by
 // Sturm-sequence bisection: count(x) = #eigenvalues < x.
-int sturm_count(std::vector<double> const& a, std::vector<double> const& b, double x) {
-    int cnt = 0;
-    double q = a[0] - x;
-    if (q < 0) ++cnt;
+// Two counts in one pass: the two recurrences are independent, so interleaving them
+// overlaps their dependent divisions; each count is computed exactly as alone.
+void sturm_count2(std::vector<double> const& a, std::vector<double> const& b, double x0, double x1, int& c0, int& c1) {
+    double const eps = std::numeric_limits<double>::epsilon();
+    int n0 = 0, n1 = 0;
+    double q0 = a[0] - x0, q1 = a[0] - x1;
+    n0 += q0 < 0;
+    n1 += q1 < 0;
     for (size_t i = 1; i < a.size(); ++i) {
         double const bb = b[i - 1] * b[i - 1];
-        if (q == 0) q = std::numeric_limits<double>::epsilon() * (std::abs(b[i - 1]) + 1e-300);
-        q = a[i] - x - bb / q;
-        if (q < 0) ++cnt;
+        double const tiny = eps * (std::abs(b[i - 1]) + 1e-300);
+        if (q0 == 0) q0 = tiny;
+        if (q1 == 0) q1 = tiny;
+        q0 = a[i] - x0 - bb / q0;
+        q1 = a[i] - x1 - bb / q1;
+        n0 += q0 < 0;
+        n1 += q1 < 0;
     }
-    return cnt;
+    c0 = n0;
+    c1 = n1;
 }
 
 void tridiagonal_extremes(std::vector<double> const& a, std::vector<double> const& b, double& mn, double& mx) {
@@ -229,16 +238,24 @@ void tridiagonal_extremes(std::vector<double> const& a, std::vector<double> cons
     double const span = std::max(hi - lo, 1e-300);
     lo -= 1e-12 * span;
     hi += 1e-12 * span;
-    auto bisect = [&](int target) {  // smallest x with count(x) > target
-        double l = lo, h = hi;
-        for (int it = 0; it < 200 && h - l > 1e-15 * std::max(std::abs(l), std::abs(h)) + 1e-300; ++it) {
-            double const m = 0.5 * (l + h);
-            if (sturm_count(a, b, m) > target) h = m; else l = m;
-        }
-        return 0.5 * (l + h);
+    // Bisection for the smallest x with count(x) > target, for target 0 (minimum) and
+    // k - 1 (maximum), both brackets advanced in the same pass; each stops on its own.
+    int const target[2] = {0, static_cast<int>(k) - 1};
+    double l[2] = {lo, lo}, h[2] = {hi, hi};
+    int it[2] = {0, 0};
+    auto open = [&](int j) {
+        return it[j] < 200 && h[j] - l[j] > 1e-15 * std::max(std::abs(l[j]), std::abs(h[j])) + 1e-300;
     };
-    mn = bisect(0);
-    mx = bisect(static_cast<int>(k) - 1);
+    while (open(0) || open(1)) {
+        bool const o0 = open(0), o1 = open(1);
+        double const m0 = 0.5 * (l[0] + h[0]), m1 = 0.5 * (l[1] + h[1]);
+        int c0, c1;
+        sturm_count2(a, b, m0, m1, c0, c1);
+        if (o0) { (c0 > target[0] ? h[0] : l[0]) = m0; ++it[0]; }
+        if (o1) { (c1 > target[1] ? h[1] : l[1]) = m1; ++it[1]; }
+    }
+    mn = 0.5 * (l[0] + h[0]);
+    mx = 0.5 * (l[1] + h[1]);
 }
 
 std::string with_suffix(double v) {
@@ -495,13 +512,17 @@ struct kpm_engine {
         with_scalar(stype, [&](auto z) {
             using T = decltype(z);
             auto const* p = reinterpret_cast<T const*>(values.data());
-            if (cpx) {
-                auto* o = reinterpret_cast<cd*>(vals.data());
-                for (int64_t k = 0; k < nnz; ++k) o[k] = to_cd(p[k]);
-            } else {
-                auto* o = reinterpret_cast<double*>(vals.data());
-                for (int64_t k = 0; k < nnz; ++k) o[k] = to_cd(p[k]).real();
-            }
+            int64_t const chunk = 1 << 20;
+            parallel_for((nnz + chunk - 1) / chunk, [&](int64_t c) {
+                int64_t const k1 = std::min(nnz, (c + 1) * chunk);
+                if (cpx) {
+                    auto* o = reinterpret_cast<cd*>(vals.data());
+                    for (int64_t k = c * chunk; k < k1; ++k) o[k] = to_cd(p[k]);
+                } else {
+                    auto* o = reinterpret_cast<double*>(vals.data());
+                    for (int64_t k = c * chunk; k < k1; ++k) o[k] = to_cd(p[k]).real();
+                }
+            });
         });
         d_lip.ensure(sizeof(int32_t) * (rows + 1));
         d_lix.ensure(sizeof(int32_t) * std::max<int64_t>(nnz, 1));
@@ -537,7 +558,7 @@ struct kpm_engine {
         size_t const es = cpx ? 16 : 8;
         // start vectors: U[0,1) from a fresh default mt19937 per system in H's real type, normalized
         std::vector<unsigned char> v1(es * rows);
-        for (int s = 0; s < nsys; ++s) {
+        parallel_for(nsys, [&](int64_t s) {  // one generator per system: independent
             std::mt19937 gen;
             int64_t const n = sys_rows(s);
             std::vector<double> u(static_cast<size_t>(n));
@@ -556,7 +577,7 @@ struct kpm_engine {
                 if (cpx) reinterpret_cast<cd*>(v1.data())[sys_off[s] + i] = cd(val, 0);
                 else reinterpret_cast<double*>(v1.data())[sys_off[s] + i] = val;
             }
-        }
+        });
         KPM_CUDA(cudaMemcpyAsync(d_lv1.p, v1.data(), v1.size(), cudaMemcpyHostToDevice, stream));
         KPM_CUDA(cudaMemsetAsync(d_lv0.p, 0, es * rows, stream));
         std::vector<std::vector<double>> alpha(nsys), beta(nsys);
@@ -580,13 +601,25 @@ struct kpm_engine {
             KPM_CUDA(cudaMemcpyAsync(hb.data(), dab, sizeof(double) * 3 * nsys, cudaMemcpyDeviceToHost, stream));
             KPM_CUDA(cudaStreamSynchronize(stream));
             std::swap(v0, v1d);
-            bool all = true;
+            std::vector<int> open;
             for (int s = 0; s < nsys; ++s) {
                 if (done[s]) continue;
                 alpha[s].push_back(hb[nsys + s]);
                 beta[s].push_back(std::sqrt(hb[2 * nsys + s]));
-                double mn, mx;
-                tridiagonal_extremes(alpha[s], beta[s], mn, mx);
+                open.push_back(s);
+            }
+            // the bisections cost O(k) per probe: spread them over the host cores once
+            // there are enough of them to pay for the threads
+            std::vector<double> emn(nsys), emx(nsys);
+            auto extremes = [&](int64_t j) {
+                int const s = open[j];
+                tridiagonal_extremes(alpha[s], beta[s], emn[s], emx[s]);
+            };
+            if (open.size() * alpha[open.front()].size() >= 512) parallel_for(static_cast<int64_t>(open.size()), extremes);
+            else for (size_t j = 0; j < open.size(); ++j) extremes(static_cast<int64_t>(j));
+            bool all = true;
+            for (int s : open) {
+                double const mn = emn[s], mx = emx[s];
                 bool const cmin = std::abs((prev_min[s] - mn) / mn) < precision;
                 bool const cmax = std::abs((prev_max[s] - mx) / mx) < precision;
                 if (cmin && cmax) {
