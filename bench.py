@@ -29,6 +29,7 @@ at 4096 sites).
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -74,7 +75,8 @@ def parse():
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2], help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
-                   choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d"])
+                   choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d", "lattice"])
+    p.add_argument("--lattice-sites", type=int, default=4_000_000, help="sites of the lattice-build workload")
     return p.parse_args()
 
 
@@ -647,6 +649,77 @@ def workload_anderson3d(args, stream_of):
           gpu_launches=int(args.steps * (launches + 3)))
 
 
+def workload_lattice(args, stream_of):
+    """Input build: a disordered graphene flake of --lattice-sites sites (onsite U[-0.5, 0.5] eV,
+    float32) built by the GPU builder, end to end through ``build_honeycomb(device="gpu")``
+    (device kernels, the onsite modifier on the host, copies both ways, the SciPy matrix);
+    the host (numpy) build of the same flake is the CPU baseline."""
+    from pybinding_gb300 import _native, lattice as L
+    import scipy.sparse  # noqa: F401  (imported before the timed region)
+    n_req = args.lattice_sites
+    mods = [L.anderson_disorder(1.0, args.seed)]
+    last = {}
+
+    def step():
+        m = L.graphene_flake(n_req, onsite_modifiers=mods, device="gpu")
+        last["m"] = m
+        return m
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    wall = (time.perf_counter() - w0) / args.steps
+    clk = clocks.stop()
+    m = last["m"]
+    n, nnz = m.hamiltonian.shape[0], m.hamiltonian.nnz
+    # device-only time of one build: the same calls through the C ABI, modifier values precomputed
+    v = L.rectangle(*_flake_dims(n_req))
+    v0, v1, sub_pos, origin, s0, s1 = L._honeycomb_frame(v, L.GRAPHENE_A, L.GRAPHENE_A_CC, False)
+    onsite = m.hamiltonian.diagonal().astype(np.float32)
+    dev = []
+    for _ in range(max(1, args.steps)):
+        b = _native.LatticeBuild.honeycomb(s0, s1, origin, v0, v1, sub_pos, L._HONEYCOMB_HOPS, v, 2)
+        b.csr(np.float32, hopping=L.GRAPHENE_T, onsite=onsite)
+        t_build, t_csr, launches = b.times()
+        dev.append(t_build + t_csr)
+        b.close()
+    t_dev = min(dev)
+    foundation = 2 * s0 * s1
+    # algorithmic bytes: foundation positions + flags written and read back, site positions,
+    # onsite values in, CSR out
+    alg = foundation * (12 + 4) * 2 + n * 12 + n * 4 + 4 * (n + 1) + nnz * 8
+    peak = float(_peaks().get("hbm_gbs", 6800.0))
+    t0 = time.perf_counter()
+    ref = L.graphene_flake(n_req, onsite_modifiers=mods)
+    t_cpu = time.perf_counter() - t0
+    same = (ref.hamiltonian.indices.tobytes() == m.hamiltonian.indices.tobytes()
+            and ref.hamiltonian.data.tobytes() == m.hamiltonian.data.tobytes())
+    _line(args, "Msites/s (GPU build of a graphene flake Hamiltonian, end to end)", n / wall / 1e6, "Msites/s", True,
+          wall, {"workload": "graphene flake build: %d sites, Anderson onsite U[-0.5, 0.5], float32 CSR" % n,
+                 "sites": int(n), "nnz": int(nnz), "foundation_sites": int(foundation)},
+          "f32",
+          device_s=t_dev,
+          roofline={"bound": "hbm", "achieved": alg / t_dev / 1e9, "peak": peak, "unit": "GB/s",
+                    "frac": alg / t_dev / 1e9 / peak, "traffic": None, "kernel": "all builder kernels (one build)",
+                    "alg_bytes_per_launch": alg, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+          cpu_baseline={"value": n / t_cpu / 1e6, "unit": "Msites/s", "cores": 1, "kind": "port",
+                        "sample": "the same flake built by the numpy host build (%.2f s), identical CSR: %s"
+                                  % (t_cpu, same)},
+          e2e={"value": n / wall / 1e6, "unit": "Msites/s", "h2d_bytes_per_step": int(n * 4),
+               "d2h_bytes_per_step": int(n * 12 + 4 * (n + 1) + nnz * 8)},
+          clocks=clk, gpu_launches=int(launches * args.steps))
+
+
+def _flake_dims(num_sites, aspect=1.0):
+    from pybinding_gb300 import lattice as L
+    area = num_sites / L.GRAPHENE_SITE_DENSITY
+    w = math.sqrt(area * aspect)
+    return w, area / w
+
+
 def run_workload(args, rank, world, local_rank):
     if args.impl == "reference":
         print(json.dumps({"impl": "reference", "workload": args.workload,
@@ -661,7 +734,7 @@ def run_workload(args, rank, world, local_rank):
     def stream_of(eng):
         return torch.cuda.ExternalStream(eng.stream())
     {"dos_c1": workload_dos_c1, "conductivity": workload_conductivity, "adjoint": workload_adjoint,
-     "anderson3d": workload_anderson3d}[args.workload](args, stream_of)
+     "anderson3d": workload_anderson3d, "lattice": workload_lattice}[args.workload](args, stream_of)
 
 
 def main():

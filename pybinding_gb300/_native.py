@@ -1,4 +1,4 @@
-"""ctypes binding of the engine's C ABI (include/kpm_gb300.h).
+"""ctypes binding of the engine's C ABI (include/kpm_gb300.h, include/kpm_lattice.h).
 
 The shared library is built in-tree (``pybinding_gb300/_build/libkpm_gb300.so``)
 by ``pybinding_gb300.build``. Loading fails loudly when it is missing: there is
@@ -46,7 +46,14 @@ class Stats(C.Structure):
                 ("call_time", C.c_double)]
 
 
-# every exported symbol of include/kpm_gb300.h with (restype, argtypes)
+class Honeycomb(C.Structure):
+    """kpm_honeycomb (include/kpm_lattice.h)"""
+    _fields_ = [("s0", C.c_int32), ("s1", C.c_int32), ("origin", C.c_float * 3), ("a1", C.c_float * 3),
+                ("a2", C.c_float * 3), ("sub", (C.c_float * 3) * 2), ("hop", (C.c_int32 * 2) * 3),
+                ("min_neighbors", C.c_int32)]
+
+
+# every exported symbol of include/kpm_gb300.h and include/kpm_lattice.h with (restype, argtypes)
 _P, _I32, _I64, _D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 SIGNATURES = {
     "kpm_last_error": (C.c_char_p, []),
@@ -72,6 +79,15 @@ SIGNATURES = {
     "kpm_moments_diag_noalloc": (_I32, [_I32, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P, _P]),
     "kpm_damping_coefficients": (_I32, [_I32, _D, _I64, _P]),
     "kpm_required_num_moments": (_I64, [_I32, _D, _D]),
+    # include/kpm_lattice.h
+    "kpm_lattice_honeycomb": (_I32, [_P, _P, _I32, _P]),
+    "kpm_lattice_cubic": (_I32, [_I32, _P]),
+    "kpm_lattice_sizes": (_I32, [_P, _P, _P, _P, _P]),
+    "kpm_lattice_sites": (_I32, [_P, _P, _P, _P]),
+    "kpm_lattice_hoppings": (_I32, [_P, _P, _P]),
+    "kpm_lattice_csr": (_I32, [_P, _I32, _P, _P, _P, _P, _P, _P, _I64, _P]),
+    "kpm_lattice_times": (_I32, [_P, _P, _P, _P]),
+    "kpm_lattice_destroy": (_I32, [_P]),
 }
 
 
@@ -375,3 +391,89 @@ def damping_coefficients(kernel, param, num_moments):
 
 def required_num_moments(kernel, param, scaled_broadening):
     return int(lib().kpm_required_num_moments(KERNEL_CODE[kernel], float(param), float(scaled_broadening)))
+
+
+class LatticeBuild:
+    """Device-side build of a honeycomb flake or a periodic cubic lattice (kpm_lattice.h).
+
+    ``sites()``, ``hoppings()`` and ``csr()`` copy the results to host numpy arrays.
+    """
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def honeycomb(cls, s0, s1, origin, a1, a2, sub, hop, vertices, min_neighbors):
+        p = Honeycomb()
+        p.s0, p.s1 = int(s0), int(s1)
+        for c in range(3):
+            p.origin[c], p.a1[c], p.a2[c] = float(origin[c]), float(a1[c]), float(a2[c])
+            p.sub[0][c], p.sub[1][c] = float(sub[0][c]), float(sub[1][c])
+        for k in range(3):
+            p.hop[k][0], p.hop[k][1] = int(hop[k][0]), int(hop[k][1])
+        p.min_neighbors = int(min_neighbors)
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 2)
+        h = C.c_void_p()
+        check(lib().kpm_lattice_honeycomb(C.byref(p), ptr(v), v.shape[0], C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def cubic(cls, L):
+        h = C.c_void_p()
+        check(lib().kpm_lattice_cubic(int(L), C.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            lib().kpm_lattice_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sizes(self):
+        v = [C.c_int64() for _ in range(4)]
+        check(lib().kpm_lattice_sizes(self._h, *[C.byref(x) for x in v]))
+        return tuple(int(x.value) for x in v)
+
+    def sites(self):
+        n = self.sizes()[0]
+        x, y, z = (np.empty(n, np.float32) for _ in range(3))
+        check(lib().kpm_lattice_sites(self._h, ptr(x), ptr(y), ptr(z)))
+        return x, y, z
+
+    def hoppings(self):
+        nh = self.sizes()[2]
+        rows, cols = np.empty(nh, np.int32), np.empty(nh, np.int32)
+        check(lib().kpm_lattice_hoppings(self._h, ptr(rows), ptr(cols)))
+        return rows, cols
+
+    def csr(self, dtype, hopping=None, hopping_values=None, onsite=None):
+        """(indptr, indices, values) of the Hamiltonian; ``hopping`` is one value for every
+        bond, ``hopping_values`` one per bond in ``hoppings()`` order."""
+        dtype = np.dtype(dtype)
+        n, _, nh, max_nnz = self.sizes()
+        one = None if hopping is None else np.array([hopping], dtype=dtype)
+        hv = None if hopping_values is None else np.ascontiguousarray(hopping_values, dtype=dtype)
+        if hv is not None and hv.size != nh:
+            raise ValueError("hopping_values must hold one value per hopping (%d)" % nh)
+        ons = None if onsite is None else np.ascontiguousarray(onsite, dtype=dtype)
+        if ons is not None and ons.size != n:
+            raise ValueError("onsite must hold one value per site (%d)" % n)
+        indptr = np.empty(n + 1, np.int32)
+        indices = np.empty(max_nnz, np.int32)
+        values = np.empty(max_nnz, dtype)
+        nnz = C.c_int64()
+        check(lib().kpm_lattice_csr(self._h, SCALAR_CODE[dtype], ptr(one), ptr(hv), ptr(ons), ptr(indptr),
+                                    ptr(indices), ptr(values), max_nnz, C.byref(nnz)))
+        k = int(nnz.value)
+        return indptr, indices[:k].copy(), values[:k].copy()
+
+    def times(self):
+        """(device seconds of the site build, of the last CSR assembly, kernels launched)"""
+        b, c, k = C.c_double(), C.c_double(), C.c_int64()
+        check(lib().kpm_lattice_times(self._h, C.byref(b), C.byref(c), C.byref(k)))
+        return b.value, c.value, int(k.value)

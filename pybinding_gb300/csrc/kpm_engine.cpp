@@ -1169,22 +1169,28 @@ struct kpm_engine {
         bool const full_rows = !opt_rows;  // the TMA and cp.async kernels do not clip rows
         int ntiles = build_tiles(sh, sys0, batch_outer);
 
+        // r0 = the starters, in the layout of shape `ls`
+        void const* starter_src = nullptr;
+        auto load_starters = [&](Shape const& ls) {
+            KPM_CUDA(cudaMemsetAsync(d_x0.p, 0, vbytes, stream));
+            if (units) {
+                d_pos.ensure(sizeof(int32_t) * units->size());
+                KPM_CUDA(cudaMemcpyAsync(d_pos.p, units->data(), sizeof(int32_t) * units->size(), cudaMemcpyHostToDevice, stream));
+                KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, ls.K, rows, stream));
+            } else {
+                // starters are in the Hamiltonian's scalar type; the scatter converts them. Host starters:
+                // where the GPU reads host memory through the host page tables (Grace), the scatter
+                // kernel reads them in place; elsewhere they are staged in device memory first
+                if (starter_src == nullptr) {
+                    size_t const in_bytes = static_cast<size_t>(nvec) * rows * scalar_bytes(stype);
+                    starter_src = on_device ? starters : device_view(starters, in_bytes);
+                }
+                KPM_CUDA(kpm::launch_scatter_starters(stype, vtype, starter_src, d_x0.p, d_map.as<int32_t>(),
+                                                      d_sysoff.as<int64_t>(), nsys, nvec, ls.K, ls.nbatch, rows, stream));
+            }
+        };
         KPM_CUDA(cudaEventRecord(ev_u0, stream));
-        KPM_CUDA(cudaMemsetAsync(d_x0.p, 0, vbytes, stream));
-        if (units) {
-            d_pos.ensure(sizeof(int32_t) * units->size());
-            KPM_CUDA(cudaMemcpyAsync(d_pos.p, units->data(), sizeof(int32_t) * units->size(), cudaMemcpyHostToDevice, stream));
-            KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, sh.K, rows, stream));
-        } else {
-            // starters are in the Hamiltonian's scalar type; the scatter converts them. Host starters:
-            // where the GPU reads host memory through the host page tables (Grace), the scatter
-            // kernel reads them in place; elsewhere they are staged in device memory first
-            size_t const in_bytes = static_cast<size_t>(nvec) * rows * scalar_bytes(stype);
-            void const* src = starters;
-            if (!on_device) src = device_view(starters, in_bytes);
-            KPM_CUDA(kpm::launch_scatter_starters(stype, vtype, src, d_x0.p, d_map.as<int32_t>(), d_sysoff.as<int64_t>(),
-                                                  nsys, nvec, sh.K, sh.nbatch, rows, stream));
-        }
+        load_starters(sh);
         KPM_CUDA(cudaEventRecord(ev_u1, stream));
         kpm::DiagStep a{};
         a.vtype = vtype;
@@ -1239,18 +1245,24 @@ struct kpm_engine {
         ntiles = build_tiles(sh, sys0, batch_outer);
         a.tiles = d_tiles.as<Tile>();
         a.num_tiles = ntiles;
-        KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
         KPM_CUDA(cudaEventRecord(ev0, stream));
-        // r1 = H~ r0 / 2 with mu0, mu1 sums
-        a.x = d_x0.p;
-        a.y = d_x1.p;
-        a.acc = d_acc.as<double>();
-        a.init = true;
-        KPM_CUDA(kpm::launch_diag_step(a, stream));
-        a.init = false;
         void* r0 = d_x0.p;
         void* r1 = d_x1.p;
         int64_t n = 2;
+        // r1 = H~ r0 / 2 with mu0, mu1 sums
+        auto first_step = [&]() {
+            KPM_CUDA(cudaMemsetAsync(d_acc.p, 0, sizeof(double) * step_acc * half, stream));
+            a.x = d_x0.p;
+            a.y = d_x1.p;
+            a.acc = d_acc.as<double>();
+            a.init = true;
+            KPM_CUDA(kpm::launch_diag_step(a, stream));
+            a.init = false;
+            r0 = d_x0.p;
+            r1 = d_x1.p;
+            n = 2;
+        };
+        first_step();
         auto single_step = [&]() {
             a.x = r1;
             a.y = r0;
@@ -1328,6 +1340,13 @@ struct kpm_engine {
                     if (ms < best) { best = ms; choice = c; }
                 }
                 fuse_tuned().put(fkey, choice);
+                // the candidates' partial moment sums round differently (FP32 partials over
+                // different tiles): start over with the chosen one, so that this call's moments
+                // are those of every later call
+                load_starters(sh);
+                first_step();
+                KPM_CUDA(cudaMemsetAsync(d_pair_counters.p, 0, sizeof(unsigned) * max_pairs, stream));
+                pair_index = 0;
             } else {
                 choice = FuseChoice{1, 0};
             }

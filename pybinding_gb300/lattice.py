@@ -164,21 +164,10 @@ def _k_core(valid, nbr, min_neighbors):
         valid &= ~drop
 
 
-def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
-                    is_complex=False, is_double=False, min_neighbors=2,
-                    t=GRAPHENE_T, a=GRAPHENE_A, a_cc=GRAPHENE_A_CC, name="graphene",
-                    float_constants=False):
-    """Monolayer graphene (``repository/graphene/lattice.py:6-66``) cut by a polygon.
-
-    ``float_constants`` derives the lattice vectors in float32 arithmetic, as the
-    C++ test fixture does (``cppcore/tests/fixtures.cpp``, ``min_neighbors=1``);
-    the Python repository lattice computes them in double and sets
-    ``min_neighbors=2``.
-
-    Modifiers are callables in the reference's numpy style:
-    ``onsite(energy, x, y, z, sub)`` and ``hopping(energy, x1, y1, z1, x2, y2, z2)``
-    returning the new energy array.
-    """
+def _honeycomb_frame(vertices, a, a_cc, float_constants):
+    """Lattice vectors, sublattice offsets and the foundation (origin, s0 x s1 cells) of a
+    honeycomb lattice cut by the polygon ``vertices``, all float32 values as the reference
+    computes them (``Foundation.cpp:6-23``, ``Lattice.cpp:190-200``)."""
     f32 = np.float32
     if float_constants:
         af, accf = f32(a), f32(a_cc)
@@ -189,9 +178,6 @@ def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
         v0 = np.array([a, 0, 0], f32)
         v1 = np.array([a / 2, a / 2 * math.sqrt(3), 0], f32)
         sub_pos = [np.array([0, -a_cc / 2, 0], f32), np.array([0, a_cc / 2, 0], f32)]
-    # hoppings owned by A (non-conjugate) -> B; B holds the conjugates
-    rel_ab = [(0, 0), (1, -1), (0, -1)]
-    rel = [rel_ab, [(-da, -db) for da, db in rel_ab]]
 
     # Foundation bounds: solve [v0 v1] v = p for each vertex, truncate, pad by one
     m = np.array([[v0[0], v1[0]], [v0[1], v1[1]]], dtype=np.float64)
@@ -205,6 +191,63 @@ def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
     origin = np.zeros(3, f32)
     origin = origin + f32(lo[0]) * v0
     origin = origin + f32(lo[1]) * v1
+    return v0, v1, sub_pos, origin, s0, s1
+
+
+# hoppings owned by A (non-conjugate) -> B as cell offsets along (a1, a2); B holds the conjugates
+_HONEYCOMB_HOPS = [(0, 0), (1, -1), (0, -1)]
+
+
+def _scalar_type(is_complex, is_double):
+    if is_complex:
+        return np.complex128 if is_double else np.complex64
+    return np.float64 if is_double else np.float32
+
+
+def _hopping_energies(dtype, t, nhops, rows, cols, sx, sy, sz, hopping_modifiers):
+    hop = np.full(nhops, t, dtype=dtype)
+    for mod in hopping_modifiers:
+        hop = np.asarray(mod(hop, sx[rows], sy[rows], sz[rows], sx[cols], sy[cols], sz[cols]))
+        hop = hop.astype(dtype) if np.iscomplexobj(dtype(0)) else np.real(hop).astype(dtype)
+    return hop
+
+
+def _onsite_energies(dtype, sx, sy, sz, sub_of, onsite_modifiers):
+    onsite = np.zeros(sx.size, dtype=dtype)
+    for mod in onsite_modifiers:
+        onsite = np.asarray(mod(onsite, sx, sy, sz, sub_of)).astype(dtype)
+    return onsite
+
+
+def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
+                    is_complex=False, is_double=False, min_neighbors=2,
+                    t=GRAPHENE_T, a=GRAPHENE_A, a_cc=GRAPHENE_A_CC, name="graphene",
+                    float_constants=False, device=None):
+    """Monolayer graphene (``repository/graphene/lattice.py:6-66``) cut by a polygon.
+
+    ``float_constants`` derives the lattice vectors in float32 arithmetic, as the
+    C++ test fixture does (``cppcore/tests/fixtures.cpp``, ``min_neighbors=1``);
+    the Python repository lattice computes them in double and sets
+    ``min_neighbors=2``.
+
+    Modifiers are callables in the reference's numpy style:
+    ``onsite(energy, x, y, z, sub)`` and ``hopping(energy, x1, y1, z1, x2, y2, z2)``
+    returning the new energy array.
+
+    ``device="gpu"`` builds the sites and the CSR matrix on the GPU (``kpm_lattice.h``);
+    the modifiers still run here on the numpy arrays. Both builds give identical models.
+    """
+    f32 = np.float32
+    v0, v1, sub_pos, origin, s0, s1 = _honeycomb_frame(vertices, a, a_cc, float_constants)
+    dtype = _scalar_type(is_complex, is_double)
+    if device is not None:
+        if device != "gpu":
+            raise ValueError("device must be None (host build) or 'gpu'")
+        return _build_honeycomb_gpu(vertices, v0, v1, sub_pos, origin, s0, s1, onsite_modifiers,
+                                    hopping_modifiers, dtype, min_neighbors, t, is_complex, is_double, name)
+    rel_ab = _HONEYCOMB_HOPS
+    rel = [rel_ab, [(-da, -db) for da, db in rel_ab]]
+
     bb = np.arange(s1)
     aa = np.arange(s0)
     xs, ys, zs = [], [], []
@@ -260,18 +303,8 @@ def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
     sub_of = np.zeros(nvalid, np.int8)
     sub_of[na_valid:] = 1
 
-    if is_complex:
-        dtype = np.complex128 if is_double else np.complex64
-    else:
-        dtype = np.float64 if is_double else np.float32
-    hop = np.full(rows.size, t, dtype=dtype)
-    for mod in hopping_modifiers:
-        hop = np.asarray(mod(hop, sx[rows], sy[rows], sz[rows], sx[cols], sy[cols], sz[cols]))
-        hop = hop.astype(dtype) if np.iscomplexobj(dtype(0)) else np.real(hop).astype(dtype)
-
-    onsite = np.zeros(nvalid, dtype=dtype)
-    for mod in onsite_modifiers:
-        onsite = np.asarray(mod(onsite, sx, sy, sz, sub_of)).astype(dtype)
+    hop = _hopping_energies(dtype, t, rows.size, rows, cols, sx, sy, sz, hopping_modifiers)
+    onsite = _onsite_energies(dtype, sx, sy, sz, sub_of, onsite_modifiers)
 
     r_all = [rows, cols]
     c_all = [cols, rows]
@@ -284,6 +317,35 @@ def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
         v_all.append(onsite[d])
     h = _csr_sorted(np.concatenate(r_all), np.concatenate(c_all), np.concatenate(v_all), nvalid, dtype)
     system = System(sx, sy, sz, sub_ranges)
+    return Model(h, system, is_complex=is_complex, is_double=is_double, name=name)
+
+
+def _build_honeycomb_gpu(vertices, v0, v1, sub_pos, origin, s0, s1, onsite_modifiers, hopping_modifiers, dtype,
+                         min_neighbors, t, is_complex, is_double, name):
+    """The device build behind ``build_honeycomb(device="gpu")``: positions, polygon
+    membership, dangling-site removal, numbering and the CSR rows run as CUDA kernels."""
+    from ._native import LatticeBuild
+    b = LatticeBuild.honeycomb(s0, s1, origin, v0, v1, sub_pos, _HONEYCOMB_HOPS,
+                               np.asarray(vertices, np.float32), min_neighbors)
+    try:
+        n, n0, nh, _ = b.sizes()
+        sx, sy, sz = b.sites()
+        hop_values = None
+        if hopping_modifiers:
+            rows, cols = b.hoppings()
+            hop_values = _hopping_energies(dtype, t, nh, rows, cols, sx, sy, sz, hopping_modifiers)
+        onsite = None
+        if onsite_modifiers:
+            sub_of = np.zeros(n, np.int8)
+            sub_of[n0:] = 1
+            onsite = _onsite_energies(dtype, sx, sy, sz, sub_of, onsite_modifiers)
+        indptr, indices, values = b.csr(dtype, hopping=None if hop_values is not None else t,
+                                        hopping_values=hop_values, onsite=onsite)
+    finally:
+        b.close()
+    h = sp.csr_matrix((values, indices, indptr), shape=(n, n))
+    h.has_sorted_indices = True
+    system = System(sx, sy, sz, {"A": (0, n0), "B": (n0, n)})
     return Model(h, system, is_complex=is_complex, is_double=is_double, name=name)
 
 
@@ -379,13 +441,29 @@ def graphene_flake(num_sites, aspect=1.0, **kw):
     return build_honeycomb(rectangle(w, h), **kw)
 
 
-def simple_cubic_periodic(L, t=-1.0, onsite=None, dtype=np.float32):
+def simple_cubic_periodic(L, t=-1.0, onsite=None, dtype=np.float32, device=None):
     """Simple cubic L^3 lattice with periodic boundaries, 6 hoppings per site.
 
-    Site index = (z*L + y)*L + x. ``onsite`` is an optional array of L^3 energies.
-    The periodic wrap makes the Hamiltonian real at k = 0.
+    Site index = (z*L + y)*L + x. ``onsite`` is an optional array of L^3 energies
+    (zeros, in ``dtype``, are not stored). The periodic wrap makes the Hamiltonian real
+    at k = 0. ``device="gpu"`` builds the CSR matrix on the GPU (``kpm_lattice.h``, L >= 3).
     """
     n = L ** 3
+    f32 = np.float32
+    ons = None if onsite is None else np.asarray(onsite, dtype)
+    if device is not None:
+        if device != "gpu":
+            raise ValueError("device must be None (host build) or 'gpu'")
+        from ._native import LatticeBuild
+        b = LatticeBuild.cubic(L)
+        try:
+            sx, sy, sz = b.sites()
+            indptr, indices, values = b.csr(dtype, hopping=t, onsite=ons)
+        finally:
+            b.close()
+        h = sp.csr_matrix((values, indices, indptr), shape=(n, n))
+        h.has_sorted_indices = True
+        return Model(h, System(sx, sy, sz, {"A": (0, n)}), name="cubic")
     idx = np.arange(n, dtype=np.int64)
     xi = idx % L
     yi = (idx // L) % L
@@ -398,12 +476,11 @@ def simple_cubic_periodic(L, t=-1.0, onsite=None, dtype=np.float32):
     rows = np.concatenate(rows)
     cols = np.concatenate(cols)
     vals = np.full(rows.size, t, dtype)
-    if onsite is not None:
-        nz = np.nonzero(onsite)[0]
+    if ons is not None:
+        nz = np.nonzero(ons)[0]
         rows = np.concatenate([rows, nz])
         cols = np.concatenate([cols, nz])
-        vals = np.concatenate([vals, np.asarray(onsite, dtype)[nz]])
+        vals = np.concatenate([vals, ons[nz]])
     h = _csr_sorted(rows, cols, vals, n, dtype)
-    f32 = np.float32
     system = System(xi.astype(f32), yi.astype(f32), zi.astype(f32), {"A": (0, n)})
     return Model(h, system, name="cubic")

@@ -1,4 +1,4 @@
-"""The C ABI library builds, loads and exports every entry point of include/kpm_gb300.h.
+"""The C ABI library builds, loads and exports every entry point of include/*.h.
 
 These run without a GPU: only host-side entry points are called (argument
 checks, kernel damping coefficients), never the recursion.
@@ -13,19 +13,23 @@ import scipy.sparse as sp
 
 from pybinding_gb300 import _native
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "kpm_gb300.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+HEADERS = sorted(os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h"))
 
 
 def declared_functions():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^[A-Za-z_][\w\s\*]*?\b(kpm_\w+)\s*\(", text, flags=re.M)))
+    names = set()
+    for header in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", open(header).read(), flags=re.S)
+        names |= set(re.findall(r"^[A-Za-z_][\w\s\*]*?\b(kpm_\w+)\s*\(", text, flags=re.M))
+    return sorted(names)
 
 
 def test_header_declares_the_abi():
     names = declared_functions()
     assert "kpm_create" in names and "kpm_moments_diag" in names and "kpm_calc_dos" in names
-    assert len(names) >= 18
+    assert "kpm_lattice_honeycomb" in names and "kpm_lattice_csr" in names
+    assert len(names) >= 26
 
 
 def test_library_exports_every_declared_symbol():

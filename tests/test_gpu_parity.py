@@ -355,6 +355,23 @@ def test_repeated_calls_replay_the_recursion_graph(dtype, nvec):
         assert rel_err(eng.moments_diag(M, st), fresh(h2, st)) < tol
 
 
+@pytest.mark.parametrize("dtype,nvec", [(np.float32, 64), (np.float32, 16), (np.float64, 8)])
+def test_first_call_gives_the_moments_of_later_calls(dtype, nvec):
+    """The first call on a new shape times its launch options on its own first steps, then
+    starts the recursion over with the chosen one: its moments equal later calls' up to the
+    order of the FP64 atomic adds (FP32 partial sums over other tiles would differ by ~1e-7)."""
+    h = _disordered_flake(17011, 9, np.float64).astype(dtype)  # a size no other test uses
+    rng = np.random.default_rng(1)
+    st = np.where(rng.integers(0, 2, (nvec, h.shape[0])) == 0, -1.0, 1.0).astype(dtype)[None]
+    eng = _native.Engine(h, _native.make_config(energy_range=(-9.5, 9.5)))
+    first = eng.moments_diag(514, st)
+    again = eng.moments_diag(514, st)
+    eng.close()
+    err = rel_err(first, again)
+    print("first vs later call (%s, %d vectors): %.3e" % (np.dtype(dtype).name, nvec, err))
+    assert err < 1e-12
+
+
 @pytest.mark.parametrize("dtype,nvec,tol", [(np.float32, 64, 1e-5), (np.float64, 16, 1e-10),
                                             (np.complex64, 32, 1e-5), (np.complex128, 8, 1e-10)])
 def test_tma_staged_step_matches_register_step_and_oracle(oracle, dtype, nvec, tol):

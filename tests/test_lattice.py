@@ -1,0 +1,160 @@
+"""The GPU builder of KPM inputs (include/kpm_lattice.h) against the host build.
+
+The host build (``pybinding_gb300.lattice``, numpy) restates pybinding's foundation,
+polygon, dangling-site and Hamiltonian code and is pinned by the reference's DOS golden
+arrays (which fix the site order). The device build must give the same model bit for bit:
+positions, sublattice ranges, CSR structure and values.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from pybinding_gb300 import _native, lattice as L
+
+
+def assert_same_model(got, ref):
+    hg, hr = got.hamiltonian, ref.hamiltonian
+    assert hg.shape == hr.shape
+    assert hg.dtype == hr.dtype
+    np.testing.assert_array_equal(hg.indptr, hr.indptr)
+    np.testing.assert_array_equal(hg.indices, hr.indices)
+    # bitwise: compare the raw bytes (signed zeros and NaNs included)
+    assert hg.data.tobytes() == hr.data.tobytes()
+    for a, b in zip(got.system.positions, ref.system.positions):
+        assert a.dtype == b.dtype == np.float32
+        assert a.tobytes() == b.tobytes()
+    assert got.system.sub_ranges == ref.system.sub_ranges
+
+
+# ---------------------------------------------------------------- host-side checks (no GPU)
+
+def test_builder_rejects_bad_arguments_before_touching_the_gpu():
+    with pytest.raises(ValueError, match="L must be >= 3"):
+        _native.LatticeBuild.cubic(2)
+    with pytest.raises(ValueError, match="foundation size"):
+        _native.LatticeBuild.honeycomb(0, 4, np.zeros(3), np.ones(3), np.ones(3), np.zeros((2, 3)),
+                                       L._HONEYCOMB_HOPS, L.rectangle(1.0), 2)
+    with pytest.raises(ValueError, match="min_neighbors"):
+        _native.LatticeBuild.honeycomb(4, 4, np.zeros(3), np.ones(3), np.ones(3), np.zeros((2, 3)),
+                                       L._HONEYCOMB_HOPS, L.rectangle(1.0), -1)
+    with pytest.raises(ValueError, match="device must be"):
+        L.build_honeycomb(L.rectangle(1.0), device="cpu")
+
+
+# ---------------------------------------------------------------- device build (GPU)
+
+def _hexagon(r):
+    ang = np.arange(6) * math.pi / 3
+    return np.stack([r * np.cos(ang), r * np.sin(ang)], axis=1).astype(np.float32)
+
+
+def _triangle(s):
+    # one horizontal edge: exercises the skipped (equal-y) edges of the ray casting
+    return np.array([[-s / 2, -s / 3], [s / 2, -s / 3], [0, 2 * s / 3]], np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("num_sites", [300, 3000, 40000])
+def test_graphene_flake_matches_host_build(num_sites):
+    assert_same_model(L.graphene_flake(num_sites, device="gpu"), L.graphene_flake(num_sites))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", ["hexagon", "triangle", "rectangle_tilted"])
+def test_polygons_match_host_build(shape):
+    if shape == "hexagon":
+        v = _hexagon(4.0)
+    elif shape == "triangle":
+        v = _triangle(9.0)
+    else:
+        c, s = math.cos(0.3), math.sin(0.3)
+        v = (L.rectangle(6.0, 3.5).astype(np.float64) @ np.array([[c, s], [-s, c]])).astype(np.float32)
+    for mn in (1, 2, 3):
+        assert_same_model(L.build_honeycomb(v, min_neighbors=mn, device="gpu"), L.build_honeycomb(v, min_neighbors=mn))
+
+
+@pytest.mark.gpu
+def test_test_fixture_lattice_matches_host_build():
+    """float32 lattice constants and min_neighbors = 1 (the C++ test fixture)."""
+    kw = dict(min_neighbors=1, float_constants=True)
+    assert_same_model(L.build_honeycomb(L.rectangle(0.6, 0.8), device="gpu", **kw),
+                      L.build_honeycomb(L.rectangle(0.6, 0.8), **kw))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["potential_f32", "anderson_f64", "field_c64", "field_c128", "strain_f64",
+                                  "mass_c64"])
+def test_modifiers_match_host_build(case):
+    kw = {
+        "potential_f32": dict(onsite_modifiers=[L.constant_potential(0.5)]),
+        "anderson_f64": dict(onsite_modifiers=[L.anderson_disorder(1.0, 3)], is_double=True),
+        "field_c64": dict(hopping_modifiers=[L.constant_magnetic_field(200.0)], is_complex=True),
+        "field_c128": dict(hopping_modifiers=[L.constant_magnetic_field(200.0)], is_complex=True, is_double=True,
+                           onsite_modifiers=[L.anderson_disorder(0.3, 5)]),
+        "strain_f64": dict(hopping_modifiers=[L.strained_hopping(L.sinusoidal_strain(0.05, 20.0))], is_double=True),
+        "mass_c64": dict(onsite_modifiers=[L.mass_term(0.1)], is_complex=True),
+    }[case]
+    assert_same_model(L.graphene_flake(5000, device="gpu", **kw), L.graphene_flake(5000, **kw))
+
+
+@pytest.mark.gpu
+def test_empty_polygon_gives_an_empty_model():
+    v = np.array([[0.01, 0.01], [0.02, 0.01], [0.02, 0.02]], np.float32)
+    got = L.build_honeycomb(v, device="gpu")
+    ref = L.build_honeycomb(v)
+    assert got.hamiltonian.shape == ref.hamiltonian.shape == (0, 0)
+    assert_same_model(got, ref)
+
+
+@pytest.mark.gpu
+def test_hopping_list_is_in_host_order():
+    v = L.rectangle(3.0, 2.0)
+    b = _native.LatticeBuild.honeycomb(*_frame_args(v), min_neighbors=2)
+    rows, cols = b.hoppings()
+    n, n0, nh, max_nnz = b.sizes()
+    b.close()
+    ref = L.build_honeycomb(v)
+    h = ref.hamiltonian.tocoo()
+    upper = h.row < h.col
+    assert nh == int(upper.sum()) and max_nnz == 2 * nh + n
+    assert np.all(rows < n0) and np.all(cols >= n0)
+    # the same set of bonds; within each direction rows ascend
+    assert set(zip(rows.tolist(), cols.tolist())) == set(zip(h.row[upper].tolist(), h.col[upper].tolist()))
+
+
+def _frame_args(v):
+    v0, v1, sub_pos, origin, s0, s1 = L._honeycomb_frame(v, L.GRAPHENE_A, L.GRAPHENE_A_CC, False)
+    return s0, s1, origin, v0, v1, sub_pos, L._HONEYCOMB_HOPS, v
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex64, np.complex128])
+@pytest.mark.parametrize("size", [3, 5, 17])
+def test_cubic_matches_host_build(dtype, size):
+    rng = np.random.default_rng(size)
+    onsite = rng.uniform(-8.25, 8.25, size ** 3)
+    onsite[::7] = 0.0  # zeros are not stored
+    assert_same_model(L.simple_cubic_periodic(size, onsite=onsite, dtype=dtype, device="gpu"),
+                      L.simple_cubic_periodic(size, onsite=onsite, dtype=dtype))
+    assert_same_model(L.simple_cubic_periodic(size, dtype=dtype, device="gpu"),
+                      L.simple_cubic_periodic(size, dtype=dtype))
+
+
+@pytest.mark.gpu
+def test_large_flake_matches_host_build():
+    """A 1M-site disordered flake: foundation of ~2M sites, several scan tiles per array."""
+    kw = dict(onsite_modifiers=[L.anderson_disorder(1.0, 11)])
+    assert_same_model(L.graphene_flake(1_000_000, device="gpu", **kw), L.graphene_flake(1_000_000, **kw))
+
+
+@pytest.mark.gpu
+def test_gpu_built_model_runs_the_same_kpm():
+    from pybinding_gb300 import kpm
+    ref = L.graphene_flake(4000, onsite_modifiers=[L.anderson_disorder(1.0, 2)])
+    got = L.graphene_flake(4000, onsite_modifiers=[L.anderson_disorder(1.0, 2)], device="gpu")
+    assert_same_model(got, ref)
+    e = np.linspace(-8, 8, 41)
+    # the blocks add their moment partials with FP64 atomics in no fixed order
+    np.testing.assert_allclose(kpm(got).calc_dos(e, 0.1, num_random=2).data,
+                               kpm(ref).calc_dos(e, 0.1, num_random=2).data, rtol=1e-9)
