@@ -7,8 +7,9 @@ boundary. There is no CPU fallback: calls fail if the CUDA library cannot be
 loaded or no GPU is present.
 """
 from . import adjoint
+from .fileio import load, save
 from .chebyshev import (KPM, KPMBatch, Series, SpatialLDOS, dirichlet_kernel, jackson_kernel, kpm, kpm_batch,
                         lorentz_kernel)
 
 __all__ = ["KPM", "KPMBatch", "Series", "SpatialLDOS", "kpm", "kpm_batch", "jackson_kernel", "lorentz_kernel",
-           "dirichlet_kernel", "adjoint"]
+           "dirichlet_kernel", "adjoint", "save", "load"]

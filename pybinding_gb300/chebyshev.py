@@ -42,6 +42,20 @@ class Series:
         return "Series(%s -> %s, %d points)" % (self.labels.get("variable"), self.labels.get("data"),
                                                self.variable.size)
 
+    # pickled state as pybinding's ``@pickleable`` classes store it (support/pickle.py:77-106),
+    # so that ``.pbz`` files carry the same layout either way
+    def __getstate__(self):
+        return dict(version=0, dict=self.__dict__)
+
+    def __setstate__(self, state):
+        if "version" not in state:
+            self.__dict__.update(state)
+            return
+        if state["version"] != 0:
+            raise RuntimeError("Can't create class {} v0 from incompatible data v{}".format(
+                type(self), state["version"]))
+        self.__dict__.update(state["dict"])
+
 
 class SpatialLDOS:
     """Result of :meth:`KPM.calc_spatial_ldos` (``pybinding/chebyshev.py:22-62``)."""

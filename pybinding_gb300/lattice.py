@@ -117,6 +117,26 @@ def rectangle(x, y=None):
     return np.array([[x0, y0], [x0, -y0], [-x0, -y0], [-x0, y0]], dtype=np.float32)
 
 
+def regular_polygon(num_sides, radius, angle=0.0):
+    """Vertices of ``pb.regular_polygon`` (pybinding/shape.py:282-300), float32."""
+    angles = [angle + 2 * n * math.pi / num_sides for n in range(num_sides)]
+    return np.array([(radius * math.sin(a), radius * math.cos(a)) for a in angles], dtype=np.float32)
+
+
+def hexagon_ac(side_width):
+    """Vertices and lattice offset of ``graphene.hexagon_ac`` (repository/graphene/shape.py:8-35):
+    a hexagon with armchair edges, its width adjusted to a whole number of edge atoms, and
+    the lattice moved by (-a/2, 0) so that a carbon hexagon sits at the centre. Returns
+    ``(vertices, lattice_offset)`` for :func:`build_honeycomb`."""
+    side_atoms = math.ceil((side_width / GRAPHENE_A_CC + 1) * 2 / 3)
+    side_atoms += side_atoms % 2
+    side_width = (3 / 2 * side_atoms - 1) * GRAPHENE_A_CC - GRAPHENE_A_CC / 2
+    x0 = side_width * math.sqrt(3) / 2
+    y0 = side_width
+    v = np.array([(0, y0), (x0, y0 / 2), (x0, -y0 / 2), (0, -y0), (-x0, -y0 / 2), (-x0, y0 / 2)], dtype=np.float32)
+    return v, (-GRAPHENE_A / 2, 0.0)
+
+
 def polygon_contains(vertices, px, py):
     """Ray-casting point-in-polygon test in float32 (``Shape.cpp:54-88``)."""
     vx = np.asarray(vertices[:, 0], np.float32)
@@ -164,10 +184,11 @@ def _k_core(valid, nbr, min_neighbors):
         valid &= ~drop
 
 
-def _honeycomb_frame(vertices, a, a_cc, float_constants):
+def _honeycomb_frame(vertices, a, a_cc, float_constants, lattice_offset=(0.0, 0.0)):
     """Lattice vectors, sublattice offsets and the foundation (origin, s0 x s1 cells) of a
     honeycomb lattice cut by the polygon ``vertices``, all float32 values as the reference
-    computes them (``Foundation.cpp:6-23``, ``Lattice.cpp:190-200``)."""
+    computes them (``Foundation.cpp:6-23``, ``Lattice.cpp:190-200``). ``lattice_offset`` is
+    the shape's lattice offset (``Model.cpp:30-34``): it moves the sites, not the bounds."""
     f32 = np.float32
     if float_constants:
         af, accf = f32(a), f32(a_cc)
@@ -189,6 +210,7 @@ def _honeycomb_frame(vertices, a, a_cc, float_constants):
 
     # origin = offset + lo0*v0 + lo1*v1 (float32, Lattice.cpp:190-200)
     origin = np.zeros(3, f32)
+    origin[:2] = np.asarray(lattice_offset, f32)[:2]
     origin = origin + f32(lo[0]) * v0
     origin = origin + f32(lo[1]) * v1
     return v0, v1, sub_pos, origin, s0, s1
@@ -222,7 +244,7 @@ def _onsite_energies(dtype, sx, sy, sz, sub_of, onsite_modifiers):
 def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
                     is_complex=False, is_double=False, min_neighbors=2,
                     t=GRAPHENE_T, a=GRAPHENE_A, a_cc=GRAPHENE_A_CC, name="graphene",
-                    float_constants=False, device=None):
+                    float_constants=False, device=None, lattice_offset=(0.0, 0.0)):
     """Monolayer graphene (``repository/graphene/lattice.py:6-66``) cut by a polygon.
 
     ``float_constants`` derives the lattice vectors in float32 arithmetic, as the
@@ -234,11 +256,14 @@ def build_honeycomb(vertices, onsite_modifiers=(), hopping_modifiers=(),
     ``onsite(energy, x, y, z, sub)`` and ``hopping(energy, x1, y1, z1, x2, y2, z2)``
     returning the new energy array.
 
+    ``lattice_offset`` moves the lattice against the shape, as a shape's ``lattice_offset``
+    does in the reference (``hexagon_ac`` sets one).
+
     ``device="gpu"`` builds the sites and the CSR matrix on the GPU (``kpm_lattice.h``);
     the modifiers still run here on the numpy arrays. Both builds give identical models.
     """
     f32 = np.float32
-    v0, v1, sub_pos, origin, s0, s1 = _honeycomb_frame(vertices, a, a_cc, float_constants)
+    v0, v1, sub_pos, origin, s0, s1 = _honeycomb_frame(vertices, a, a_cc, float_constants, lattice_offset)
     dtype = _scalar_type(is_complex, is_double)
     if device is not None:
         if device != "gpu":

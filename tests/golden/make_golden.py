@@ -4,11 +4,15 @@ Run from the repository root on a machine that has the pybinding source tree:
 
     python tests/golden/make_golden.py /path/to/pybinding
 
-It writes two files next to this script:
+It writes these files next to this script:
 
 * ``kpm_baseline.npz`` -- the reference's own golden arrays for its KPM tests
   (``tests/baseline_data/kpm/*.pbz``: gzip-pickled float32 numpy arrays),
   copied verbatim under their test names.
+* ``system_baselines.npz`` -- site positions, sublattice site counts and hopping
+  pairs of the reference's graphene system baselines (``tests/baseline_data/shape``
+  and ``system``: pickled ``System`` objects, read as data without pybinding).
+* ``pbz/*.pbz`` -- the KPM baseline files themselves, for the ``.pbz`` reader.
 * ``python_impl_moments.npz`` -- diagonal KPM moments computed by the
   reference's pure-NumPy FP64 implementation (``_PythonImpl`` in
   ``pybinding/chebyshev.py:448-583``) on small Hamiltonians and supplied
@@ -75,6 +79,54 @@ def copy_baselines(ref_root):
     return out
 
 
+class _Data:
+    """Stand-in for any pybinding class while unpickling a baseline: keeps its state only."""
+
+    def __setstate__(self, state):
+        self.state = state
+
+
+class _DataUnpickler(pickle.Unpickler):
+    def find_class(self, module, name):
+        if module.split(".")[0] in ("pybinding", "_pybinding"):
+            return type(name, (_Data,), {})
+        return super().find_class(module, name)
+
+
+# the reference's system baselines of nearest-neighbour graphene (monolayer lattice) cut
+# by a polygon: the shapes of tests/test_shape.py:8-14 and hexagon_ac of tests/test_system.py:8
+SYSTEM_CASES = ["shape/polygon_expected[triangle]", "shape/polygon_expected[triangle90]",
+                "shape/polygon_expected[diamond]", "shape/polygon_expected[square]",
+                "shape/polygon_expected[pentagon]", "system/expected[graphene-monolayer]"]
+
+
+def copy_system_baselines(ref_root):
+    """Site positions, per-sublattice site counts and nearest-neighbour hopping pairs of the
+    reference's graphene system baselines (``System`` objects pickled by its tests)."""
+    out = {}
+    for case in SYSTEM_CASES:
+        with gzip.open(os.path.join(ref_root, "tests", "baseline_data", case + ".pbz"), "rb") as fh:
+            system = _DataUnpickler(fh).load()
+        impl = system.state if isinstance(system.state, dict) else system.state.state
+        x, y, z = impl["positions"].state
+        rows, cols = impl["hopping_blocks"].state["data"][0]
+        key = case.split("/")[1]
+        out[key + "/x"], out[key + "/y"], out[key + "/z"] = x, y, z
+        out[key + "/site_counts"] = np.asarray(impl["compressed_sublattices"].state["site_counts"])
+        out[key + "/hop_rows"], out[key + "/hop_cols"] = np.asarray(rows), np.asarray(cols)
+    np.savez_compressed(os.path.join(HERE, "system_baselines.npz"), **out)
+    return out
+
+
+def copy_kpm_pbz(ref_root):
+    """The KPM baseline files themselves (a few hundred bytes each), for the .pbz reader."""
+    dst = os.path.join(HERE, "pbz")
+    os.makedirs(dst, exist_ok=True)
+    for f in sorted(glob.glob(os.path.join(ref_root, "tests", "baseline_data", "kpm", "*.pbz"))):
+        with open(f, "rb") as src, open(os.path.join(dst, os.path.basename(f)), "wb") as out:
+            out.write(src.read())
+
+
 def python_impl_cases(cheb):
     from pybinding_gb300 import lattice as L
     from oracle import oracle as O
@@ -118,7 +170,13 @@ def python_impl_cases(cheb):
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYBINDING_SRC", "")
     if not ref or not os.path.isdir(ref):
-        sys.exit("usage: make_golden.py /path/to/pybinding")
+        sys.exit("usage: make_golden.py /path/to/pybinding [systems]")
+    if sys.argv[2:] == ["systems"]:  # only the system baselines and the .pbz copies
+        print("system baselines:", sorted({k.split("/")[0] for k in copy_system_baselines(ref)}))
+        copy_kpm_pbz(ref)
+        sys.exit(0)
+    copy_system_baselines(ref)
+    copy_kpm_pbz(ref)
     base = copy_baselines(ref)
     print("baselines:", {k: v.shape for k, v in base.items()})
     cheb = load_reference_chebyshev(ref)

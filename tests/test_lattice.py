@@ -1,9 +1,10 @@
-"""The GPU builder of KPM inputs (include/kpm_lattice.h) against the host build.
+"""The builders of KPM inputs against the reference's system baselines and each other.
 
 The host build (``pybinding_gb300.lattice``, numpy) restates pybinding's foundation,
-polygon, dangling-site and Hamiltonian code and is pinned by the reference's DOS golden
-arrays (which fix the site order). The device build must give the same model bit for bit:
-positions, sublattice ranges, CSR structure and values.
+polygon, dangling-site and Hamiltonian code; it is pinned bit for bit by the reference's
+own system baselines (pickled ``System`` objects of its shape and system tests) and, via
+the site order, by its DOS golden arrays. The GPU build (include/kpm_lattice.h) must give
+the same model bit for bit: positions, sublattice ranges, CSR structure and values.
 """
 import math
 
@@ -25,6 +26,55 @@ def assert_same_model(got, ref):
         assert a.dtype == b.dtype == np.float32
         assert a.tobytes() == b.tobytes()
     assert got.system.sub_ranges == ref.system.sub_ranges
+
+
+# ---------------------------------------------------------------- the reference's system baselines
+# nearest-neighbour graphene cut by the shapes of tests/test_shape.py:8-14 and the hexagon
+# of tests/test_system.py:8 (positions, site counts per sublattice, hopping pairs)
+SYSTEM_SHAPES = {
+    "polygon_expected[triangle]": lambda: (L.regular_polygon(3, 1.1), (0.0, 0.0)),
+    "polygon_expected[triangle90]": lambda: (L.regular_polygon(3, 1.1, math.pi / 2), (0.0, 0.0)),
+    "polygon_expected[diamond]": lambda: (L.regular_polygon(4, 1.0), (0.0, 0.0)),
+    "polygon_expected[square]": lambda: (L.regular_polygon(4, 1.0, math.pi / 4), (0.0, 0.0)),
+    "polygon_expected[pentagon]": lambda: (L.regular_polygon(5, 1.0), (0.0, 0.0)),
+    "expected[graphene-monolayer]": lambda: L.hexagon_ac(1.0),
+}
+
+
+@pytest.fixture(scope="module")
+def system_baselines():
+    import os
+    from tests.conftest import GOLDEN
+    return dict(np.load(os.path.join(GOLDEN, "system_baselines.npz")))
+
+
+def assert_matches_system_baseline(model, base, case):
+    x, y, z = model.system.positions
+    assert x.tobytes() == base[case + "/x"].tobytes()  # bit for bit, float32
+    assert y.tobytes() == base[case + "/y"].tobytes()
+    assert z.tobytes() == base[case + "/z"].tobytes()
+    counts = base[case + "/site_counts"]
+    assert model.system.sub_ranges == {"A": (0, int(counts[0])), "B": (int(counts[0]), int(counts.sum()))}
+    h = model.hamiltonian.tocoo()
+    upper = h.row < h.col
+    rows, cols = base[case + "/hop_rows"], base[case + "/hop_cols"]
+    mine = sorted(zip(h.row[upper].tolist(), h.col[upper].tolist()))
+    ref = sorted(zip(np.minimum(rows, cols).tolist(), np.maximum(rows, cols).tolist()))
+    assert mine == ref
+    np.testing.assert_array_equal(h.data[upper], np.float32(L.GRAPHENE_T))
+
+
+@pytest.mark.parametrize("case", sorted(SYSTEM_SHAPES))
+def test_host_build_matches_reference_system_baseline(system_baselines, case):
+    v, offset = SYSTEM_SHAPES[case]()
+    assert_matches_system_baseline(L.build_honeycomb(v, lattice_offset=offset), system_baselines, case)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", sorted(SYSTEM_SHAPES))
+def test_gpu_build_matches_reference_system_baseline(system_baselines, case):
+    v, offset = SYSTEM_SHAPES[case]()
+    assert_matches_system_baseline(L.build_honeycomb(v, lattice_offset=offset, device="gpu"), system_baselines, case)
 
 
 # ---------------------------------------------------------------- host-side checks (no GPU)
