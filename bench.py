@@ -75,14 +75,16 @@ def parse():
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2], help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
-                   choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d", "lattice"])
+                   choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d", "lattice", "sweep"])
+    p.add_argument("--sweep-models", type=int, default=32, help="models of the sweep workload")
+    p.add_argument("--sweep-sites", type=int, default=100_000, help="sites per model of the sweep workload")
     p.add_argument("--lattice-sites", type=int, default=4_000_000, help="sites of the lattice-build workload")
     return p.parse_args()
 
 
 def build_workload(args, rank):
     from pybinding_gb300 import lattice as L
-    import scipy.sparse as sp
+    from pybinding_gb300.chebyshev import block_diagonal
     rng = np.random.default_rng(args.seed + 1000 * rank)
     sizes = rng.integers(args.min_sites, args.max_sites + 1, size=args.flakes)
     hs = []
@@ -90,8 +92,7 @@ def build_workload(args, rank):
         m = L.graphene_flake(int(n), onsite_modifiers=[L.anderson_disorder(1.0, args.seed + 7919 * i + rank)])
         hs.append(m.hamiltonian)
     offsets = np.concatenate([[0], np.cumsum([h.shape[0] for h in hs])]).astype(np.int64)
-    h = sp.block_diag(hs, format="csr").astype(np.float32)
-    h.sort_indices()
+    h = block_diagonal([x.astype(np.float32) for x in hs])
     return hs, h, offsets
 
 
@@ -713,6 +714,84 @@ def workload_lattice(args, stream_of):
           clocks=clk, gpu_launches=int(launches * args.steps))
 
 
+def workload_sweep(args, stream_of):
+    """Disorder sweep (``parallel_for`` over deferred LDOS): --sweep-models graphene flakes of
+    --sweep-sites sites, onsite disorder of width 0..3 eV (float32 H), LDOS at the site nearest
+    the centre on 200 energies in [-8, 8] eV, broadening 0.05 eV (Jackson). End to end per
+    sweep: engines, reorder, Lanczos bounds, one batched recursion, reconstruction."""
+    import pybinding_gb300 as pbg
+    from pybinding_gb300 import lattice as L, parallel
+    from oracle import oracle as O
+    widths = np.linspace(0.0, 3.0, args.sweep_models)
+    models = [L.graphene_flake(args.sweep_sites, onsite_modifiers=[L.anderson_disorder(w, 100 + i)], device="gpu")
+              for i, w in enumerate(widths)]
+    energy = np.linspace(-8, 8, 200)
+    broadening = 0.05
+
+    def jobs():
+        return [pbg.kpm(m).deferred_ldos(energy, broadening, [0, 0]) for m in models]
+
+    def step():
+        js = jobs()
+        parallel.compute_all(js)
+        return js
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        batched = step()
+    wall = (time.perf_counter() - w0) / args.steps
+    clk = clocks.stop()
+    st = parallel.last_batch_stats
+    t0 = time.perf_counter()
+    jobs()
+    t_jobs = time.perf_counter() - t0
+    # the same jobs one by one (each its own engine and recursion), for the batching gain
+    t0 = time.perf_counter()
+    single = jobs()
+    for j in single:
+        j.compute()
+    t_single = time.perf_counter() - t0
+    diff = max(float(np.max(np.abs(b.result[:, 0] - np.squeeze(s.result))) / np.max(np.abs(s.result)))
+               for b, s in zip(batched, single))
+    n = sum(m.hamiltonian.shape[0] for m in models)
+    nnz = sum(m.hamiltonian.nnz for m in models)
+    M = int(st.num_moments)
+    launches = M // 2
+    avg = st.moments_time / launches
+    # one vector (K = 1, FP32): matrix (hi/lo values + index) once, x, y_old, y_new
+    alg = nnz * 12 + 4 * (n + 1) + 3 * n * 4
+    peak = float(_peaks().get("hbm_gbs", 6800.0))
+    # CPU: the oracle's LDOS (one thread) on one model of the sweep
+    h0 = models[-1].hamiltonian
+    idx0 = int(models[-1].system.find_nearest([0, 0]))
+    t0 = time.perf_counter()
+    O.core_ldos(h0, [idx0], energy, broadening)
+    t_cpu = time.perf_counter() - t0
+    _line(args, "LDOS sweep points/s (deferred LDOS of %d models, batched)" % len(models), len(models) / wall,
+          "points/s", True, wall,
+          {"workload": "disorder sweep: %d graphene flakes of %d sites, W = 0..3 eV, LDOS at the centre, "
+                       "200 energies, broadening 0.05 eV" % (len(models), args.sweep_sites),
+           "sites": int(n), "nnz": int(nnz), "moments": M},
+          "f32",
+          sequential_s=t_single, batched_s=wall, batched_vs_sequential_max_rel_diff=diff,
+          recursion_s=st.moments_time, bounds_s=st.bounds_time, jobs_s=t_jobs,
+          batch_assemble_s=parallel.last_batch_times.get("assemble_s"),
+          engine_call_s=parallel.last_batch_times.get("call_s"), reorder_s=st.hamiltonian_time,
+          roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",
+                    "frac": alg / avg / 1e9 / peak, "traffic": None, "kernel": "diag_step_kernel (K = 1)",
+                    "alg_bytes_per_launch": alg, "avg_launch_ms": avg * 1e3,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+          cpu_baseline={"value": 1.0 / t_cpu, "unit": "points/s", "cores": 1, "kind": "port",
+                        "sample": "one model of the sweep (%d sites), the oracle's Core::ldos: %.2f s"
+                                  % (h0.shape[0], t_cpu)},
+          e2e={"value": len(models) / wall, "unit": "points/s", "h2d_bytes_per_step": int(nnz * 12 + 4 * n),
+               "d2h_bytes_per_step": int(len(models) * energy.size * 8)},
+          clocks=clk, gpu_launches=int(args.steps * (launches + 2 * len(models) + 3)))
+
+
 def _flake_dims(num_sites, aspect=1.0):
     from pybinding_gb300 import lattice as L
     area = num_sites / L.GRAPHENE_SITE_DENSITY
@@ -734,7 +813,8 @@ def run_workload(args, rank, world, local_rank):
     def stream_of(eng):
         return torch.cuda.ExternalStream(eng.stream())
     {"dos_c1": workload_dos_c1, "conductivity": workload_conductivity, "adjoint": workload_adjoint,
-     "anderson3d": workload_anderson3d, "lattice": workload_lattice}[args.workload](args, stream_of)
+     "anderson3d": workload_anderson3d, "lattice": workload_lattice,
+     "sweep": workload_sweep}[args.workload](args, stream_of)
 
 
 def main():

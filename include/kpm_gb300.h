@@ -169,6 +169,14 @@ int kpm_calc_dos(kpm_engine* engine, const double* energy, int64_t num_energy, d
 int kpm_calc_ldos(kpm_engine* engine, const int64_t* indices, int64_t num_indices, const double* energy,
                   int64_t num_energy, double broadening, double* out);
 
+/* LDOS of every system of a ragged batch at one site each (sites[s]: the local row of
+ * system s), all systems in one recursion: one vector with a unit entry per system, each
+ * system with its own bounds and moment count, as KPM::calc_ldos per system (KPM.cpp:55-65).
+ * out is [num_systems][num_energy]. The batched form of pybinding's deferred_ldos sweeps
+ * (cppmodule/src/kpm.cpp:84-91 driven by pybinding/parallel.py:29-70). */
+int kpm_calc_ldos_batch(kpm_engine* engine, const int64_t* sites, const double* energy, int64_t num_energy,
+                        double broadening, double* out);
+
 /* Green's function elements (row, cols[j]) (system 0): kpm::Core::greens_vector
  * (Core.cpp:96-117). Indices are checked like cpb::KPM::calc_greens_vector
  * (KPM.cpp:110-121). out: [num_cols][num_energy] complex. */

@@ -8,8 +8,10 @@ loaded or no GPU is present.
 """
 from . import adjoint
 from .fileio import load, save
+from .parallel import NDSweep, Sweep, ndsweep, parallel_for, parallelize, sweep
 from .chebyshev import (KPM, KPMBatch, Series, SpatialLDOS, dirichlet_kernel, jackson_kernel, kpm, kpm_batch,
                         lorentz_kernel)
 
 __all__ = ["KPM", "KPMBatch", "Series", "SpatialLDOS", "kpm", "kpm_batch", "jackson_kernel", "lorentz_kernel",
-           "dirichlet_kernel", "adjoint", "save", "load"]
+           "dirichlet_kernel", "adjoint", "save", "load", "parallelize", "parallel_for", "sweep", "ndsweep",
+           "Sweep", "NDSweep"]

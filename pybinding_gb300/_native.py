@@ -66,6 +66,7 @@ SIGNATURES = {
     "kpm_moments_diag": (_I32, [_P, _I64, _I64, _P, _I32, _I32, _P, _P]),
     "kpm_calc_dos": (_I32, [_P, _P, _I64, _D, _I64, _P]),
     "kpm_calc_ldos": (_I32, [_P, _P, _I64, _P, _I64, _D, _P]),
+    "kpm_calc_ldos_batch": (_I32, [_P, _P, _P, _I64, _D, _P]),
     "kpm_calc_greens": (_I32, [_P, _I64, _P, _I64, _P, _I64, _D, _P]),
     "kpm_moments": (_I32, [_P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _P]),
     "kpm_calc_conductivity": (_I32, [_P, _P, _P, _P, _I64, _D, _D, _I64, _I64, _I32, _P]),
@@ -255,6 +256,16 @@ class Engine:
         out = np.empty((idx.size, e.size), np.float64)
         check(lib().kpm_calc_ldos(self._h, ptr(idx), idx.size, ptr(e), e.size, float(broadening), ptr(out)))
         return out.T  # (energy, indices)
+
+    def calc_ldos_batch(self, sites, energy, broadening):
+        """LDOS of every system at one local site each: [num_systems][num_energy]."""
+        sites = np.ascontiguousarray(sites, dtype=np.int64)
+        if sites.size != self.num_systems:
+            raise ValueError("one LDOS site per system (%d)" % self.num_systems)
+        e = np.ascontiguousarray(energy, dtype=np.float64)
+        out = np.empty((self.num_systems, e.size))
+        check(lib().kpm_calc_ldos_batch(self._h, ptr(sites), ptr(e), e.size, float(broadening), ptr(out)))
+        return out
 
     def calc_greens(self, row, cols, energy, broadening):
         c = np.ascontiguousarray(np.atleast_1d(cols), np.int64)

@@ -219,7 +219,7 @@ class GpuImpl:
 
     def deferred_ldos(self, energy, broadening, position, sublattice=""):
         """``deferred_ldos`` (cppmodule/src/kpm.cpp:84-91): compute on demand."""
-        return Deferred(lambda: self.calc_ldos(energy, broadening, position, sublattice))
+        return DeferredLDOS(self, energy, broadening, position, sublattice)
 
     def calc_conductivity(self, chemical_potential, broadening, temperature, direction, num_random, num_points,
                           gemm_mode=None):
@@ -244,6 +244,28 @@ class Deferred:
     def compute(self):
         self.result = self._fn()
         return self.result
+
+
+class DeferredLDOS(Deferred):
+    """``KPM.deferred_ldos`` (``cppmodule/src/kpm.cpp:84-91``): the LDOS of one model at the
+    site nearest to ``position``, computed on demand. :func:`pybinding_gb300.parallel.parallel_for`
+    runs the deferred LDOS of many single-orbital models together, as one ragged batch."""
+
+    def __init__(self, impl, energy, broadening, position, sublattice=""):
+        super().__init__(lambda: impl.calc_ldos(energy, broadening, position, sublattice))
+        self.impl = impl
+        self.energy = np.asarray(energy, dtype=np.float64)
+        self.broadening = float(broadening)
+        system = impl.model.system
+        idx = np.atleast_1d(system.to_hamiltonian_indices(system.find_nearest(position, sublattice)))
+        self.site = int(idx[0]) if idx.size == 1 else None  # None: multi-orbital, computed alone
+
+    def batch_key(self):
+        """Deferred LDOS with equal keys can share one recursion (None: this one cannot)."""
+        if self.site is None:
+            return None
+        cfg = tuple(sorted((k, v) for k, v in self.impl._cfg_args.items()))
+        return (cfg, np.dtype(self.impl.model.hamiltonian.dtype).str, self.energy.tobytes(), self.broadening)
 
 
 class KPM:
@@ -342,6 +364,35 @@ def kpm(model, energy_range=None, kernel="default", num_threads="auto", silent=F
     return KPM(GpuImpl(model, energy_range or (0, 0), kernel, **kwargs))
 
 
+def block_diagonal(hs):
+    """The block-diagonal CSR matrix of square CSR matrices ``hs`` (sorted indices, int32),
+    in their common scalar type: their index arrays shifted and concatenated."""
+    dt = np.result_type(*[h.dtype for h in hs])
+    rows = np.concatenate([[0], np.cumsum([h.shape[0] for h in hs])]).astype(np.int64)
+    nnz = np.concatenate([[0], np.cumsum([h.nnz for h in hs])]).astype(np.int64)
+    if rows[-1] >= 2 ** 31 or nnz[-1] >= 2 ** 31:
+        raise ValueError("the batch exceeds int32 indices")
+    parts = []
+    for h in hs:
+        if h.shape[0] != h.shape[1]:
+            raise ValueError("Hamiltonians must be square")
+        h = h.copy() if not h.has_sorted_indices else h
+        h.sort_indices()
+        parts.append(h)
+    # int32 arithmetic: every sum is below the 2^31 checked above
+    indptr = np.empty(int(rows[-1]) + 1, np.int32)
+    indices = np.empty(int(nnz[-1]), np.int32)
+    data = np.empty(int(nnz[-1]), dt)
+    indptr[0] = 0
+    for i, p in enumerate(parts):
+        np.add(p.indptr[1:], np.int32(nnz[i]), out=indptr[rows[i] + 1:rows[i + 1] + 1], dtype=np.int32, casting="unsafe")
+        np.add(p.indices, np.int32(rows[i]), out=indices[nnz[i]:nnz[i + 1]], dtype=np.int32, casting="unsafe")
+        data[nnz[i]:nnz[i + 1]] = p.data
+    out = sp.csr_matrix((data, indices, indptr), shape=(int(rows[-1]), int(rows[-1])))
+    out.has_sorted_indices = True
+    return out
+
+
 class KPMBatch:
     """A ragged batch of independent models run together: every Chebyshev step of
     every model is one kernel launch over the block-diagonal matrix."""
@@ -352,9 +403,7 @@ class KPMBatch:
             raise ValueError("empty model batch")
         self.kernel = kernel if kernel is not None else jackson_kernel()
         hs = [sp.csr_matrix(m.hamiltonian) for m in self.models]
-        dt = np.result_type(*[h.dtype for h in hs])
-        h = sp.block_diag([h.astype(dt) for h in hs], format="csr")
-        h.sort_indices()
+        h = block_diagonal(hs)
         self.offsets = np.concatenate([[0], np.cumsum([x.shape[0] for x in hs])]).astype(np.int64)
         args = dict(energy_range=tuple(energy_range or (0, 0)), kernel=self.kernel.name,
                     kernel_param=self.kernel.param)
@@ -374,6 +423,26 @@ class KPMBatch:
     def moments(self, num_moments, starters, average=False):
         """Diagonal moments of every model for supplied starters ``[model][vector][site]``."""
         return self.engine.moments_diag(num_moments, starters, average=average)
+
+    def calc_ldos(self, energy, broadening, position=None, sublattice="", sites=None):
+        """LDOS of every model (``KPM::calc_ldos`` per model, single-orbital models) at the site
+        nearest to ``position`` (one position for all models, or one per model), or at the
+        Hamiltonian rows ``sites``; all models in one recursion. A list of :class:`Series`."""
+        if sites is None:
+            pos = list(position) if (position is not None and np.ndim(position) == 2) else [position] * len(self.models)
+            if len(pos) != len(self.models):
+                raise ValueError("give one position, or one per model")
+            sites = []
+            for m, p in zip(self.models, pos):
+                idx = np.atleast_1d(m.system.to_hamiltonian_indices(m.system.find_nearest(p, sublattice)))
+                if idx.size != 1:
+                    raise ValueError("batched LDOS needs single-orbital models")
+                sites.append(int(idx[0]))
+        out = self.engine.calc_ldos_batch(sites, energy, broadening)
+        return [Series(energy, d, labels=dict(variable="E (eV)", data="LDOS", columns="orbitals")) for d in out]
+
+    def close(self):
+        self.engine.close()
 
 
 def kpm_batch(models, energy_range=None, kernel="default", **kwargs):

@@ -586,54 +586,66 @@ struct kpm_engine {
         std::vector<char> done(nsys, 1);
         for (int s : todo) done[s] = 0;
         double const precision = static_cast<double>(static_cast<float>(cfg.lanczos_precision)) / 100;
-        std::vector<double> hb(3 * nsys, 0.0);  // [bprev | alpha | nrm]
+        // kLzBlock iterations run on the device between host checks: the beta of an iteration
+        // is computed on the device from the previous squared norm, and the host then replays
+        // the convergence test iteration by iteration on the downloaded (alpha, |v|^2), so the
+        // result and the loop count are those of checking after every iteration; systems that
+        // converged early in a block just run a few iterations nobody reads
+        constexpr int kLzBlock = 16;
+        size_t const slot = static_cast<size_t>(nsys);
+        d_lab.ensure(sizeof(double) * slot * (1 + 2 * kLzBlock));
+        double* const dprev = d_lab.as<double>();           // |v|^2 of the iteration before the block
+        double* const dblock = dprev + slot;                 // per iteration j: alpha_j, |v|^2_j
+        KPM_CUDA(cudaMemsetAsync(dprev, 0, sizeof(double) * slot, stream));
+        std::vector<double> hb(2 * kLzBlock * slot);
         void* v0 = d_lv0.p;
         void* v1d = d_lv1.p;
-        for (int it = 0; it < 1000; ++it) {
-            for (int s = 0; s < nsys; ++s) hb[s] = beta[s].empty() ? 0.0 : beta[s].back();
-            std::fill(hb.begin() + nsys, hb.end(), 0.0);
-            double* dab = d_lab.as<double>();
-            KPM_CUDA(cudaMemcpyAsync(dab, hb.data(), sizeof(double) * 3 * nsys, cudaMemcpyHostToDevice, stream));
-            KPM_CUDA(kpm::launch_lanczos_a(cpx, d_lip.as<int32_t>(), d_lix.as<int32_t>(), d_lval.p, v1d, v0,
-                                           d_ltiles.as<Tile>(), lz_tiles, dab, dab + nsys, stream));
-            KPM_CUDA(kpm::launch_lanczos_b(cpx, v1d, v0, d_ltiles.as<Tile>(), lz_tiles, dab + nsys, dab + 2 * nsys, stream));
-            KPM_CUDA(kpm::launch_lanczos_c(cpx, v0, d_ltiles.as<Tile>(), lz_tiles, dab + 2 * nsys, stream));
-            KPM_CUDA(cudaMemcpyAsync(hb.data(), dab, sizeof(double) * 3 * nsys, cudaMemcpyDeviceToHost, stream));
+        std::vector<int> open;
+        for (int it0 = 0; it0 < 1000; it0 += kLzBlock) {
+            int const nb = std::min(kLzBlock, 1000 - it0);
+            KPM_CUDA(cudaMemsetAsync(dblock, 0, sizeof(double) * 2 * slot * nb, stream));
+            for (int j = 0; j < nb; ++j) {
+                double const* np = j == 0 ? dprev : dblock + (2 * j - 1) * slot;
+                double* al = dblock + 2 * j * slot;
+                double* nr = al + slot;
+                KPM_CUDA(kpm::launch_lanczos_a(cpx, d_lip.as<int32_t>(), d_lix.as<int32_t>(), d_lval.p, v1d, v0,
+                                               d_ltiles.as<Tile>(), lz_tiles, np, al, stream));
+                KPM_CUDA(kpm::launch_lanczos_b(cpx, v1d, v0, d_ltiles.as<Tile>(), lz_tiles, al, nr, stream));
+                KPM_CUDA(kpm::launch_lanczos_c(cpx, v0, d_ltiles.as<Tile>(), lz_tiles, nr, stream));
+                std::swap(v0, v1d);
+            }
+            KPM_CUDA(cudaMemcpyAsync(hb.data(), dblock, sizeof(double) * 2 * slot * nb, cudaMemcpyDeviceToHost, stream));
+            KPM_CUDA(cudaMemcpyAsync(dprev, dblock + (2 * nb - 1) * slot, sizeof(double) * slot,
+                                     cudaMemcpyDeviceToDevice, stream));
             KPM_CUDA(cudaStreamSynchronize(stream));
-            std::swap(v0, v1d);
-            std::vector<int> open;
-            for (int s = 0; s < nsys; ++s) {
-                if (done[s]) continue;
-                alpha[s].push_back(hb[nsys + s]);
-                beta[s].push_back(std::sqrt(hb[2 * nsys + s]));
-                open.push_back(s);
-            }
-            // the bisections cost O(k) per probe: spread them over the host cores once
-            // there are enough of them to pay for the threads
-            std::vector<double> emn(nsys), emx(nsys);
-            auto extremes = [&](int64_t j) {
-                int const s = open[j];
-                tridiagonal_extremes(alpha[s], beta[s], emn[s], emx[s]);
-            };
-            if (open.size() * alpha[open.front()].size() >= 512) parallel_for(static_cast<int64_t>(open.size()), extremes);
-            else for (size_t j = 0; j < open.size(); ++j) extremes(static_cast<int64_t>(j));
-            bool all = true;
-            for (int s : open) {
-                double const mn = emn[s], mx = emx[s];
-                bool const cmin = std::abs((prev_min[s] - mn) / mn) < precision;
-                bool const cmax = std::abs((prev_max[s] - mx) / mx) < precision;
-                if (cmin && cmax) {
-                    done[s] = 1;
-                    sys[s].have_bounds = true;
-                    sys[s].emin = mn;
-                    sys[s].emax = mx;
-                    sys[s].loops = it;
-                } else {
-                    all = false;
+            open.clear();
+            for (int s = 0; s < nsys; ++s)
+                if (!done[s]) open.push_back(s);
+            // systems are independent: each replays its iterations of the block on its own
+            auto replay = [&](int64_t q) {
+                int const s = open[q];
+                for (int j = 0; j < nb && !done[s]; ++j) {
+                    alpha[s].push_back(hb[2 * j * slot + s]);
+                    beta[s].push_back(std::sqrt(hb[(2 * j + 1) * slot + s]));
+                    double mn, mx;
+                    tridiagonal_extremes(alpha[s], beta[s], mn, mx);
+                    bool const cmin = std::abs((prev_min[s] - mn) / mn) < precision;
+                    bool const cmax = std::abs((prev_max[s] - mx) / mx) < precision;
+                    if (cmin && cmax) {
+                        done[s] = 1;
+                        sys[s].have_bounds = true;
+                        sys[s].emin = mn;
+                        sys[s].emax = mx;
+                        sys[s].loops = it0 + j;
+                    }
+                    prev_min[s] = mn;
+                    prev_max[s] = mx;
                 }
-                prev_min[s] = mn;
-                prev_max[s] = mx;
-            }
+            };
+            if (open.size() > 1) parallel_for(static_cast<int64_t>(open.size()), replay);
+            else if (!open.empty()) replay(0);
+            bool all = true;
+            for (int s = 0; s < nsys; ++s) all = all && done[s];
             if (all) {
                 st.bounds_time = now_s() - t0;
                 st.lanczos_loops = sys[todo.front()].loops;
@@ -736,19 +748,18 @@ struct kpm_engine {
         double const t0 = now_s();
         compute_bounds();
         map.assign(rows, 0);
-        std::vector<int32_t> oip{0}, oix;
         W = 0;
         // H~ in FP64 (the scaled values of create_reordered evaluated in double), then stored in the
         // recursion type: FP64 as is, FP32 as (hi, lo) pairs
         bool const cpx = kpm::vtype_complex(vtype);
-        std::vector<cd> oval_c;
-        std::vector<double> oval_r;
-        // systems are independent: reorder them in parallel into their own buffers, then join
+        // systems are independent: reorder them in parallel into their own buffers, then write
+        // each one's rows of the padded ELL, again in parallel
         std::vector<ScaleAB> scs(nsys);  // bounds (Lanczos on the GPU) before the threads start
         for (int s = 0; s < nsys; ++s) scs[s] = scale(s);
-        std::vector<std::vector<int32_t>> sip(nsys), six(nsys);
+        std::vector<std::vector<int32_t>> sip(nsys), six(nsys);  // per system: row ends, global columns
         std::vector<std::vector<cd>> svc(cpx ? nsys : 0);
         std::vector<std::vector<double>> svr(cpx ? 0 : nsys);
+        std::vector<int32_t> sys_w(nsys, 1);
         with_scalar(stype, [&](auto zi) {
             using Tin = decltype(zi);
             parallel_for(nsys, [&](int64_t s) {
@@ -759,40 +770,55 @@ struct kpm_engine {
                 else
                     reorder_system<double, Tin>(static_cast<int>(s), sl, scs[s], reorders(), sip[s], six[s], svr[s],
                                                 s == 0 ? &slices : nullptr);
+                int32_t prev = 0;
+                for (int32_t e : sip[s]) {
+                    sys_w[s] = std::max(sys_w[s], e - prev);
+                    prev = e;
+                }
             });
         });
-        for (int s = 0; s < nsys; ++s) {
-            int32_t const base = static_cast<int32_t>(oix.size());
-            for (int32_t e : sip[s]) oip.push_back(base + e);
-            oix.insert(oix.end(), six[s].begin(), six[s].end());
-            if (cpx) oval_c.insert(oval_c.end(), svc[s].begin(), svc[s].end());
-            else oval_r.insert(oval_r.end(), svr[s].begin(), svr[s].end());
-            std::vector<int32_t>().swap(six[s]);
-        }
-        for (int64_t r = 0; r < rows; ++r) W = std::max(W, oip[r + 1] - oip[r]);
-        W = std::max(W, 1);
+        for (int s = 0; s < nsys; ++s) W = std::max(W, sys_w[s]);
+        int64_t total_nnz = 0;
+        for (int s = 0; s < nsys; ++s) total_nnz += sip[s].empty() ? 0 : sip[s].back();
         int const vs = kpm::vtype_vs(vtype);
         std::vector<int32_t> col(static_cast<size_t>(rows) * W);
+        // visit the entries of system s, row by row: f(row, slot, column, value) for stored
+        // entries and pad(row, slot) for the padding slots up to W
+        auto for_rows = [&](int64_t s, auto&& f, auto&& pad) {
+            int64_t const r0 = sys_off[s];
+            int32_t prev = 0;
+            for (size_t q = 0; q < sip[s].size(); ++q) {
+                int64_t const r = r0 + static_cast<int64_t>(q);
+                int j = 0;
+                for (int32_t k = prev; k < sip[s][q]; ++k, ++j)
+                    f(r, j, six[s][k], cpx ? svc[s][k] : cd(svr[s][k], 0.0));
+                for (; j < W; ++j) pad(r, j);
+                prev = sip[s][q];
+            }
+        };
         with_vtype(vtype, [&](auto zc) {
             using Tc = decltype(zc);
-            std::vector<Tc> val(static_cast<size_t>(rows) * W * vs, Tc(0));
-            for (int64_t r = 0; r < rows; ++r) {
-                int j = 0;
-                for (int32_t k = oip[r]; k < oip[r + 1]; ++k, ++j) {
-                    col[r * W + j] = oix[k];
-                    cd const h = cpx ? oval_c[k] : cd(oval_r[k], 0.0);
-                    Tc const hi = from_cd<Tc>(h);
-                    val[(r * W + j) * vs] = hi;
-                    if (vs == 2) val[(r * W + j) * vs + 1] = from_cd<Tc>(h - to_cd(hi));
-                }
-                for (; j < W; ++j) col[r * W + j] = static_cast<int32_t>(r);
-            }
-            h_col = col;
+            std::unique_ptr<Tc[]> val(new Tc[static_cast<size_t>(rows) * W * vs]);  // every slot is written below
+            parallel_for(nsys, [&](int64_t s) {
+                for_rows(
+                    s,
+                    [&](int64_t r, int j, int32_t c, cd const& h) {
+                        col[r * W + j] = c;
+                        Tc const hi = from_cd<Tc>(h);
+                        val[(r * W + j) * vs] = hi;
+                        if (vs == 2) val[(r * W + j) * vs + 1] = from_cd<Tc>(h - to_cd(hi));
+                    },
+                    [&](int64_t r, int j) {
+                        col[r * W + j] = static_cast<int32_t>(r);
+                        for (int q = 0; q < vs; ++q) val[(r * W + j) * vs + q] = Tc(0);
+                    });
+            });
+            size_t const nval = static_cast<size_t>(rows) * W * vs;
             // 64 bytes of tail padding: bulk copies of a tile's entries round their size up to 16 bytes
             d_col.ensure(col.size() * sizeof(int32_t) + 64);
-            d_val.ensure(val.size() * sizeof(Tc) + 64);
+            d_val.ensure(nval * sizeof(Tc) + 64);
             KPM_CUDA(cudaMemcpyAsync(d_col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
-            KPM_CUDA(cudaMemcpyAsync(d_val.p, val.data(), val.size() * sizeof(Tc), cudaMemcpyHostToDevice, stream));
+            KPM_CUDA(cudaMemcpyAsync(d_val.p, val.get(), nval * sizeof(Tc), cudaMemcpyHostToDevice, stream));
             KPM_CUDA(cudaStreamSynchronize(stream));
         });
         // A complex H~ whose values are all real (e.g. a real lattice stored as complex so that
@@ -800,31 +826,39 @@ struct kpm_engine {
         // per entry instead of four (same results: the imaginary parts are exact zeros)
         real_values = false;
         if (cpx) {
-            real_values = std::all_of(oval_c.begin(), oval_c.end(), [](cd const& h) { return h.imag() == 0.0; });
+            std::vector<char> sys_real(nsys, 1);
+            parallel_for(nsys, [&](int64_t s) {
+                sys_real[s] = std::all_of(svc[s].begin(), svc[s].end(), [](cd const& h) { return h.imag() == 0.0; });
+            });
+            real_values = std::all_of(sys_real.begin(), sys_real.end(), [](char c) { return c != 0; });
             if (real_values) {
                 auto upload = [&](auto zr) {
                     using Tr_ = decltype(zr);
                     int const rvs = std::is_same_v<Tr_, float> ? 2 : 1;  // FP32: (hi, lo) pairs
-                    std::vector<Tr_> rv(static_cast<size_t>(rows) * W * rvs, Tr_(0));
-                    for (int64_t r = 0; r < rows; ++r) {
-                        int j = 0;
-                        for (int32_t k = oip[r]; k < oip[r + 1]; ++k, ++j) {
-                            double const h = oval_c[k].real();
-                            Tr_ const hi = static_cast<Tr_>(h);
-                            rv[(r * W + j) * rvs] = hi;
-                            if (rvs == 2) rv[(r * W + j) * rvs + 1] = static_cast<Tr_>(h - static_cast<double>(hi));
-                        }
-                    }
-                    d_val_real.ensure(rv.size() * sizeof(Tr_) + 64);
-                    KPM_CUDA(cudaMemcpyAsync(d_val_real.p, rv.data(), rv.size() * sizeof(Tr_), cudaMemcpyHostToDevice,
-                                             stream));
+                    std::unique_ptr<Tr_[]> rv(new Tr_[static_cast<size_t>(rows) * W * rvs]);
+                    parallel_for(nsys, [&](int64_t s) {
+                        for_rows(
+                            s,
+                            [&](int64_t r, int j, int32_t, cd const& h) {
+                                Tr_ const hi = static_cast<Tr_>(h.real());
+                                rv[(r * W + j) * rvs] = hi;
+                                if (rvs == 2) rv[(r * W + j) * rvs + 1] = static_cast<Tr_>(h.real() - static_cast<double>(hi));
+                            },
+                            [&](int64_t r, int j) {
+                                for (int q = 0; q < rvs; ++q) rv[(r * W + j) * rvs + q] = Tr_(0);
+                            });
+                    });
+                    size_t const n = static_cast<size_t>(rows) * W * rvs;
+                    d_val_real.ensure(n * sizeof(Tr_) + 64);
+                    KPM_CUDA(cudaMemcpyAsync(d_val_real.p, rv.get(), n * sizeof(Tr_), cudaMemcpyHostToDevice, stream));
                     KPM_CUDA(cudaStreamSynchronize(stream));
                 };
                 if (vtype == kpm::V_C64) upload(float{});
                 else upload(double{});
             }
         }
-        opt_nnz = oip.back();
+        h_col = std::move(col);
+        opt_nnz = total_nnz;
         d_map.ensure(sizeof(int32_t) * rows);
         KPM_CUDA(cudaMemcpy(d_map.p, map.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice));
         d_sysoff.ensure(sizeof(int64_t) * (nsys + 1));
@@ -1147,13 +1181,17 @@ struct kpm_engine {
     // reordered positions `units` (system 0). Per-vector moments land in d_mu as
     // [s][v][M] complex double. `opt_rows` applies the optimal-size row limit (system 0).
     void run_diag(int64_t M, int64_t nvec, void const* starters, bool on_device, std::vector<int32_t> const* units,
-                  bool opt_rows) {
+                  bool opt_rows, bool units_per_system = false) {
         if (M < 2 || (M - 2) % 4 != 0) fail(KPM_ERR_VALUE, "num_moments must satisfy (M - 2) % 4 == 0");
         if (nvec < 1) fail(KPM_ERR_VALUE, "num_vectors must be >= 1");
         Shape sh = pick_shape(nvec);
         int const vb = kpm::vtype_bytes(vtype);
         int const NV = kpm::vtype_nv(vtype);
-        bool const sys0 = units != nullptr;
+        // units: nvec unit vectors in system 0, or (units_per_system) one vector holding a
+        // unit entry in every system, at units[s]
+        bool const sys0 = units != nullptr && !units_per_system;
+        if (units_per_system && (nvec != 1 || !units || static_cast<int>(units->size()) != nsys))
+            fail(KPM_ERR_VALUE, "one unit position per system and one vector");
         int const ns = sys0 ? 1 : nsys;
         int64_t const bstride = rows * sh.K;
         size_t const vbytes = static_cast<size_t>(bstride) * sh.nbatch * vb;
@@ -1176,7 +1214,11 @@ struct kpm_engine {
             if (units) {
                 d_pos.ensure(sizeof(int32_t) * units->size());
                 KPM_CUDA(cudaMemcpyAsync(d_pos.p, units->data(), sizeof(int32_t) * units->size(), cudaMemcpyHostToDevice, stream));
-                KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, ls.K, rows, stream));
+                if (units_per_system)
+                    for (int s = 0; s < nsys; ++s)
+                        KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>() + s, 1, ls.K, rows, stream));
+                else
+                    KPM_CUDA(kpm::launch_set_units(vtype, d_x0.p, d_pos.as<int32_t>(), nvec, ls.K, rows, stream));
             } else {
                 // starters are in the Hamiltonian's scalar type; the scatter converts them. Host starters:
                 // where the GPU reads host memory through the host page tables (Grace), the scatter
@@ -1689,6 +1731,37 @@ int kpm_calc_ldos(kpm_engine* e, const int64_t* idx, int64_t nidx, const double*
         e->reset_stats(M, true, opt, static_cast<double>(nidx), 0);
         e->damp_device(e->d_mu.as<double>(), M, nidx, M);
         e->spectral(e->d_mu.as<double>(), M, static_cast<int>(nidx), energy, ne, sc, out);
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
+    });
+}
+
+int kpm_calc_ldos_batch(kpm_engine* e, const int64_t* sites, const double* energy, int64_t ne, double broadening,
+                        double* out) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        if (!sites) fail(KPM_ERR_VALUE, "no LDOS sites");
+        if (ne > 0 && (!energy || !out)) fail(KPM_ERR_VALUE, "null energy or output");
+        for (int s = 0; s < e->nsys; ++s)
+            if (sites[s] < 0 || sites[s] >= e->sys_rows(s)) fail(KPM_ERR_RUNTIME, "LDOS index out of range");
+        double const t0 = now_s();
+        e->compute_bounds();
+        std::vector<int64_t> Ms(e->nsys);
+        int64_t Mmax = 2;
+        for (int s = 0; s < e->nsys; ++s) {
+            Ms[s] = required_moments(e->cfg.kernel, e->cfg.kernel_param, broadening / e->scale(s).a);
+            Mmax = std::max(Mmax, Ms[s]);
+        }
+        e->optimize({0}, {0});
+        std::vector<int32_t> pos(e->nsys);
+        for (int s = 0; s < e->nsys; ++s) pos[s] = e->map[e->sys_off[s] + sites[s]];
+        e->run_diag(Mmax, 1, nullptr, false, &pos, false, true);
+        e->reset_stats(Mmax, true, false, static_cast<double>(e->nsys), 0);
+        for (int s = 0; s < e->nsys; ++s) {
+            double* m = e->d_mu.as<double>() + 2 * s * Mmax;
+            e->damp_device(m, Ms[s], 1, Mmax);
+            e->spectral(m, Ms[s], 1, energy, ne, e->scale(s), out + s * ne);
+        }
         e->finish_stats();
         e->calc_time = now_s() - t0;
     });

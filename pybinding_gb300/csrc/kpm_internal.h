@@ -203,12 +203,12 @@ cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, in
                                cudaStream_t s);
 
 // Lanczos (FP64 or complex FP64, all systems in lockstep, CSR per system in global rows)
-// A: t = H v1; v0 = t - bprev[s] v0; alpha[s] += Re(conj(t) v1)
+// A: t = H v1; v0 = t - sqrt(nrm_prev[s]) v0; alpha[s] += Re(conj(t) v1)
 // B: v0 -= alpha[s] v1; nrm[s] += |v0|^2
 // C: v0 *= 1/sqrt(nrm[s])
 cudaError_t launch_lanczos_a(bool cplx, int32_t const* ip, int32_t const* ix, void const* v,
                              void const* v1, void* v0, Tile const* tiles, int num_tiles,
-                             double const* bprev, double* alpha, cudaStream_t s);
+                             double const* nrm_prev, double* alpha, cudaStream_t s);
 cudaError_t launch_lanczos_b(bool cplx, void const* v1, void* v0, Tile const* tiles, int num_tiles,
                              double const* alpha, double* nrm, cudaStream_t s);
 cudaError_t launch_lanczos_c(bool cplx, void* v0, Tile const* tiles, int num_tiles, double const* nrm,

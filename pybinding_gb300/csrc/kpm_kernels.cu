@@ -1620,10 +1620,10 @@ template<class V>
 __global__ void __launch_bounds__(BLOCK)
 lanczos_a_kernel(int32_t const* __restrict__ ip, int32_t const* __restrict__ ix, V const* __restrict__ hv,
                  V const* __restrict__ v1, V* __restrict__ v0, Tile const* __restrict__ tiles,
-                 double const* __restrict__ bprev, double* __restrict__ alpha) {
+                 double const* __restrict__ nrm_prev, double* __restrict__ alpha) {
     __shared__ double sh[WARPS];
     Tile const t = tiles[blockIdx.x];
-    double const bp = bprev[t.system];
+    double const bp = sqrt(nrm_prev[t.system]);  // beta of the previous iteration (0 at the start)
     double a = 0.0;
     for (int r = t.row_begin + threadIdx.x; r < t.row_end; r += BLOCK) {
         V sum;
@@ -1914,15 +1914,15 @@ cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, in
 }
 
 cudaError_t launch_lanczos_a(bool cplx, int32_t const* ip, int32_t const* ix, void const* v, void const* v1, void* v0,
-                             Tile const* tiles, int num_tiles, double const* bprev, double* alpha, cudaStream_t s) {
+                             Tile const* tiles, int num_tiles, double const* nrm_prev, double* alpha, cudaStream_t s) {
     if (cplx)
         lanczos_a_kernel<double2><<<num_tiles, BLOCK, 0, s>>>(ip, ix, static_cast<double2 const*>(v),
                                                               static_cast<double2 const*>(v1),
-                                                              static_cast<double2*>(v0), tiles, bprev, alpha);
+                                                              static_cast<double2*>(v0), tiles, nrm_prev, alpha);
     else
         lanczos_a_kernel<double><<<num_tiles, BLOCK, 0, s>>>(ip, ix, static_cast<double const*>(v),
                                                              static_cast<double const*>(v1), static_cast<double*>(v0),
-                                                             tiles, bprev, alpha);
+                                                             tiles, nrm_prev, alpha);
     return cudaGetLastError();
 }
 

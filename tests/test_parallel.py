@@ -1,0 +1,116 @@
+"""Parameter sweeps (``pybinding/parallel.py``): factories, batching of deferred LDOS jobs
+into ragged GPU batches, and the sweep results."""
+import numpy as np
+import pytest
+
+import pybinding_gb300 as pbg
+from pybinding_gb300 import lattice as L, parallel
+from pybinding_gb300.chebyshev import Deferred
+
+
+def test_parallelize_makes_the_product_of_the_variables():
+    @pbg.parallelize(a=[1, 2, 3], b=[10, 20])
+    def factory(a, b, energy=np.linspace(0, 1, 4), scale=2.0):
+        return Deferred(lambda: np.full(4, scale * (a + b)))
+
+    assert factory.sequence == [(1, 10), (1, 20), (2, 10), (2, 20), (3, 10), (3, 20)]
+    assert set(factory.fixtures) == {"energy", "scale"}
+    data = pbg.parallel_for(factory)
+    assert [float(d[0]) for d in data] == [22.0, 42.0, 24.0, 44.0, 26.0, 46.0]
+    nd = pbg.ndsweep(factory, labels=dict(axes=["a", "b", "E"]))
+    assert nd.data.shape == (3, 2, 4) and nd.labels["x"] == "a"
+    np.testing.assert_array_equal(nd.data[2, 1], np.full(4, 46.0))
+
+
+def test_sweep_stacks_one_row_per_value():
+    @pbg.parallelize(x=np.linspace(0, 1, 5))
+    def factory(x, energy=np.linspace(-1, 1, 7)):
+        return Deferred(lambda: (x * energy)[:, None])
+
+    s = pbg.sweep(factory, labels=dict(x="x", y="E"))
+    assert s.data.shape == (5, 7)
+    np.testing.assert_allclose(s.data[4], np.linspace(-1, 1, 7))
+    assert s.labels["y"] == "E" and s.labels["title"] == ""
+
+
+def _flake(n, seed, double=False):
+    return L.graphene_flake(n, onsite_modifiers=[L.anderson_disorder(0.5, seed)], is_double=double)
+
+
+def test_deferred_ldos_jobs_are_grouped_into_batches(monkeypatch):
+    """Jobs with equal settings and scalar type share a batch, split at MAX_BATCH_ROWS;
+    other jobs run alone, in order. (The batch runner is replaced: no GPU here.)"""
+    runs = []
+
+    def fake_batch(chunk):
+        runs.append([d.impl.model.hamiltonian.shape[0] for d in chunk])
+        for d in chunk:
+            d.result = np.full((3, 1), float(d.site))
+
+    monkeypatch.setattr(parallel, "_run_ldos_batch", fake_batch)
+    e = np.linspace(-1, 1, 3)
+    f32 = [_flake(n, i) for i, n in enumerate((300, 500, 400))]
+    f64 = [_flake(n, 9 + i, double=True) for i, n in enumerate((350, 450))]
+    jobs = [pbg.kpm(m).deferred_ldos(e, 0.1, [0, 0]) for m in f32 + f64]
+    other = Deferred(lambda: "plain")
+    parallel.compute_all(jobs[:2] + [other] + jobs[2:])
+    assert runs == [[f32[0].hamiltonian.shape[0], f32[1].hamiltonian.shape[0], f32[2].hamiltonian.shape[0]],
+                    [f64[0].hamiltonian.shape[0], f64[1].hamiltonian.shape[0]]]
+    assert other.result == "plain"
+    assert all(j.result is not None for j in jobs)
+    # a row cap splits a group into several batches
+    runs.clear()
+    four = [_flake(n, 30 + i) for i, n in enumerate((500, 500, 300, 300))]
+    rows = [m.hamiltonian.shape[0] for m in four]
+    monkeypatch.setattr(parallel, "MAX_BATCH_ROWS", rows[0] + rows[1])
+    parallel.compute_all([pbg.kpm(m).deferred_ldos(e, 0.1, [0, 0]) for m in four])
+    assert runs == [rows[:2], rows[2:]]
+    # a different broadening is another group
+    runs.clear()
+    monkeypatch.setattr(parallel, "MAX_BATCH_ROWS", 1 << 26)
+    jobs = [pbg.kpm(m).deferred_ldos(e, b, [0, 0]) for m in f32 for b in (0.1, 0.2)]
+    parallel.compute_all(jobs)
+    assert sorted(len(r) for r in runs) == [3, 3]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("double", [True, False])
+def test_batched_ldos_matches_single_model_ldos(double):
+    models = [_flake(n, 20 + i, double) for i, n in enumerate((3000, 1800, 5200, 900))]
+    e = np.linspace(-8, 8, 61)
+    batch = pbg.kpm_batch(models)
+    got = batch.calc_ldos(e, 0.1, position=[0.1, 0.2])
+    batch.close()
+    tol = 1e-9 if double else 2e-5
+    for m, g in zip(models, got):
+        ref = pbg.kpm(m).calc_ldos(e, 0.1, [0.1, 0.2]).data
+        err = np.max(np.abs(g.data - ref)) / np.max(np.abs(ref))
+        print("batched vs single LDOS (%s): %.2e" % ("f64" if double else "f32", err))
+        assert err < tol
+
+
+@pytest.mark.gpu
+def test_sweep_of_deferred_ldos_runs_as_one_batch(monkeypatch):
+    energy = np.linspace(-3, 3, 41)
+    strengths = [0.0, 0.5, 1.0, 2.0, 3.0]
+    batches = []
+    real = parallel._run_ldos_batch
+
+    def spy(chunk):
+        batches.append(len(chunk))
+        real(chunk)
+
+    monkeypatch.setattr(parallel, "_run_ldos_batch", spy)
+
+    @pbg.parallelize(w=strengths)
+    def factory(w, energy=energy, broadening=0.15):
+        model = L.graphene_flake(2500, onsite_modifiers=[L.anderson_disorder(w, 3)], is_double=True)
+        return pbg.kpm(model).deferred_ldos(energy, broadening, position=[0, 0])
+
+    s = pbg.sweep(factory)
+    assert batches == [len(strengths)]
+    assert s.data.shape == (len(strengths), energy.size)
+    for w, row in zip(strengths, s.data):
+        model = L.graphene_flake(2500, onsite_modifiers=[L.anderson_disorder(w, 3)], is_double=True)
+        ref = pbg.kpm(model).calc_ldos(energy, 0.15, [0, 0]).data
+        assert np.max(np.abs(row - ref)) / np.max(np.abs(ref)) < 1e-9
