@@ -120,6 +120,13 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
                const void* values, int32_t num_systems, const int64_t* system_offsets,
                const kpm_config* cfg, kpm_engine** out);
 
+/* A ragged-batch engine made of existing single-system engines (same scalar type), system i
+ * being engines[i]'s Hamiltonian: their checked CSR matrices are concatenated without
+ * another check, and Lanczos bounds a member has already found are kept. The members are
+ * not changed and may be destroyed afterwards. The batched form of many KPM objects
+ * (one per model of a parameter sweep, pybinding/parallel.py:29-70). */
+int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_config* cfg, kpm_engine** out);
+
 /* Release the engine and its device memory. */
 int kpm_destroy(kpm_engine* engine);
 

@@ -60,6 +60,7 @@ SIGNATURES = {
     "kpm_config_default": (None, [_P]),
     "kpm_create": (_I32, [_I32, _I64, _P, _P, _P, _I32, _P, _P, _P]),
     "kpm_destroy": (_I32, [_P]),
+    "kpm_create_batch": (_I32, [_P, _I32, _P, _P]),
     "kpm_set_hamiltonian": (_I32, [_P, _I32, _I64, _P, _P, _P, _I32, _P]),
     "kpm_energy_bounds": (_I32, [_P, _I32, _P, _P, _P]),
     "kpm_scaling_factors": (_I32, [_P, _I32, _P, _P]),
@@ -189,6 +190,24 @@ class Engine:
 
     def set_hamiltonian(self, h, system_offsets=None):
         self._set(h, system_offsets)
+
+    @classmethod
+    def from_engines(cls, engines, config):
+        """A ragged-batch engine whose system i is the Hamiltonian of ``engines[i]`` (single-system
+        engines of one scalar type), made without copying the matrices through Python
+        (``kpm_create_batch``)."""
+        engines = list(engines)
+        arr = (C.c_void_p * len(engines))(*[e._h for e in engines])
+        handle = C.c_void_p()
+        check(lib().kpm_create_batch(arr, len(engines), C.byref(config), C.byref(handle)))
+        self = cls.__new__(cls)
+        self._h = handle
+        self.config = config
+        sizes = [e.rows for e in engines]
+        self.rows, self.num_systems, self.dtype = int(sum(sizes)), len(engines), engines[0].dtype
+        self._nnz = int(sum(e._nnz for e in engines))
+        self.system_offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        return self
 
     def close(self):
         if self._h is not None and _lib is not None:

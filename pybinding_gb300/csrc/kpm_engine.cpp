@@ -398,6 +398,17 @@ struct kpm_engine {
         return d_stage.p;
     }
 
+    // Host-to-device copy of a host buffer on `stream`: where the GPU reads host memory through
+    // the host page tables, a copy kernel reads it in place (a pageable cudaMemcpyAsync is staged
+    // through bounce buffers at a fraction of the link's rate); elsewhere cudaMemcpyAsync. The
+    // host buffer must stay unchanged until the stream has run the copy.
+    void upload_host(void* dst, void const* src, size_t bytes) {
+        if (bytes == 0) return;
+        bool const aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 16) == 0;
+        if (host_reads_direct() && aligned) KPM_CUDA(kpm::launch_copy(dst, src, bytes, stream));
+        else KPM_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream));
+    }
+
     std::vector<unsigned char> h_starters, h_starters_right;  // host starters the engine generates
 
     void drop_graph() {
@@ -527,10 +538,10 @@ struct kpm_engine {
         d_lip.ensure(sizeof(int32_t) * (rows + 1));
         d_lix.ensure(sizeof(int32_t) * std::max<int64_t>(nnz, 1));
         d_lval.ensure(std::max<size_t>(vals.size(), 16));
-        KPM_CUDA(cudaMemcpyAsync(d_lip.p, indptr.data(), sizeof(int32_t) * (rows + 1), cudaMemcpyHostToDevice, stream));
+        upload_host(d_lip.p, indptr.data(), sizeof(int32_t) * (rows + 1));
         if (nnz > 0) {
-            KPM_CUDA(cudaMemcpyAsync(d_lix.p, indices.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, stream));
-            KPM_CUDA(cudaMemcpyAsync(d_lval.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, stream));
+            upload_host(d_lix.p, indices.data(), sizeof(int32_t) * nnz);
+            upload_host(d_lval.p, vals.data(), vals.size());
         }
         std::vector<Tile> tiles;
         for (int s = 0; s < nsys; ++s)
@@ -578,7 +589,7 @@ struct kpm_engine {
                 else reinterpret_cast<double*>(v1.data())[sys_off[s] + i] = val;
             }
         });
-        KPM_CUDA(cudaMemcpyAsync(d_lv1.p, v1.data(), v1.size(), cudaMemcpyHostToDevice, stream));
+        upload_host(d_lv1.p, v1.data(), v1.size());
         KPM_CUDA(cudaMemsetAsync(d_lv0.p, 0, es * rows, stream));
         std::vector<std::vector<double>> alpha(nsys), beta(nsys);
         std::vector<double> prev_min(nsys, std::numeric_limits<double>::max());
@@ -817,8 +828,8 @@ struct kpm_engine {
             // 64 bytes of tail padding: bulk copies of a tile's entries round their size up to 16 bytes
             d_col.ensure(col.size() * sizeof(int32_t) + 64);
             d_val.ensure(nval * sizeof(Tc) + 64);
-            KPM_CUDA(cudaMemcpyAsync(d_col.p, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
-            KPM_CUDA(cudaMemcpyAsync(d_val.p, val.get(), nval * sizeof(Tc), cudaMemcpyHostToDevice, stream));
+            upload_host(d_col.p, col.data(), col.size() * sizeof(int32_t));
+            upload_host(d_val.p, val.get(), nval * sizeof(Tc));
             KPM_CUDA(cudaStreamSynchronize(stream));
         });
         // A complex H~ whose values are all real (e.g. a real lattice stored as complex so that
@@ -850,7 +861,7 @@ struct kpm_engine {
                     });
                     size_t const n = static_cast<size_t>(rows) * W * rvs;
                     d_val_real.ensure(n * sizeof(Tr_) + 64);
-                    KPM_CUDA(cudaMemcpyAsync(d_val_real.p, rv.get(), n * sizeof(Tr_), cudaMemcpyHostToDevice, stream));
+                    upload_host(d_val_real.p, rv.get(), n * sizeof(Tr_));
                     KPM_CUDA(cudaStreamSynchronize(stream));
                 };
                 if (vtype == kpm::V_C64) upload(float{});
@@ -860,9 +871,10 @@ struct kpm_engine {
         h_col = std::move(col);
         opt_nnz = total_nnz;
         d_map.ensure(sizeof(int32_t) * rows);
-        KPM_CUDA(cudaMemcpy(d_map.p, map.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice));
+        upload_host(d_map.p, map.data(), sizeof(int32_t) * rows);
         d_sysoff.ensure(sizeof(int64_t) * (nsys + 1));
-        KPM_CUDA(cudaMemcpy(d_sysoff.p, sys_off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice));
+        KPM_CUDA(cudaMemcpyAsync(d_sysoff.p, sys_off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice, stream));
+        KPM_CUDA(cudaStreamSynchronize(stream));
         idx_src.clear();
         idx_dest.clear();
         for (auto i : src) idx_src.push_back(map[i]);
@@ -1587,6 +1599,78 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
         if (e->cfg.staging < 0 || e->cfg.staging > 3) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2 or 3");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
+        *out = e.release();
+    });
+}
+
+int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_config* cfg, kpm_engine** out) {
+    return guarded([&] {
+        if (!out) fail(KPM_ERR_VALUE, "null output handle");
+        *out = nullptr;
+        if (!engines || num_engines < 1) fail(KPM_ERR_VALUE, "no engines to batch");
+        int64_t rows = 0, nnz = 0;
+        for (int32_t i = 0; i < num_engines; ++i) {
+            kpm_engine const* src = engines[i];
+            if (!src) fail(KPM_ERR_VALUE, "null engine in the batch");
+            if (src->nsys != 1) fail(KPM_ERR_VALUE, "batched engines must hold one system each");
+            if (src->stype != engines[0]->stype) fail(KPM_ERR_VALUE, "batched engines must share the scalar type");
+            rows += src->rows;
+            nnz += src->indptr[src->rows];
+        }
+        if (rows > std::numeric_limits<int32_t>::max() || nnz > std::numeric_limits<int32_t>::max())
+            fail(KPM_ERR_VALUE, "the batch exceeds int32 indices");
+        auto e = std::make_unique<kpm_engine>();
+        if (cfg) e->cfg = *cfg; else kpm_config_default(&e->cfg);
+        e->cfg.min_energy = static_cast<float>(e->cfg.min_energy);
+        e->cfg.max_energy = static_cast<float>(e->cfg.max_energy);
+        if (e->cfg.min_energy > e->cfg.max_energy)
+            fail(KPM_ERR_VALUE, "KPM: Invalid energy range specified (min > max).");
+        if (e->cfg.kernel == KPM_KERNEL_LORENTZ && e->cfg.kernel_param <= 0)
+            fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
+        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
+            fail(KPM_ERR_VALUE, "unknown precision mode");
+        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
+        if (e->cfg.staging < 0 || e->cfg.staging > 3) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2 or 3");
+        // the members' CSR matrices were checked when their engines were made: concatenate them
+        // (columns shifted into their block), each member's copy in parallel
+        int const st = engines[0]->stype;
+        size_t const sb = static_cast<size_t>(scalar_bytes(st));
+        std::vector<int64_t> row_off(num_engines + 1, 0), nz_off(num_engines + 1, 0);
+        for (int32_t i = 0; i < num_engines; ++i) {
+            row_off[i + 1] = row_off[i] + engines[i]->rows;
+            nz_off[i + 1] = nz_off[i] + engines[i]->indptr[engines[i]->rows];
+        }
+        e->stype = st;
+        e->rows = rows;
+        e->nsys = num_engines;
+        e->sys_off = row_off;
+        e->indptr.resize(rows + 1);
+        e->indices.resize(nnz);
+        e->values.resize(static_cast<size_t>(nnz) * sb);
+        e->indptr[0] = 0;
+        parallel_for(num_engines, [&](int64_t i) {
+            kpm_engine const* src = engines[i];
+            int32_t const r0 = static_cast<int32_t>(row_off[i]), z0 = static_cast<int32_t>(nz_off[i]);
+            for (int64_t r = 0; r < src->rows; ++r) e->indptr[r0 + r + 1] = z0 + src->indptr[r + 1];
+            int64_t const n = src->indptr[src->rows];
+            for (int64_t k = 0; k < n; ++k) e->indices[z0 + k] = r0 + src->indices[k];
+            std::memcpy(e->values.data() + static_cast<size_t>(z0) * sb, src->values.data(), static_cast<size_t>(n) * sb);
+        });
+        e->sys.assign(num_engines, kpm_engine::Sys{});
+        for (int32_t i = 0; i < num_engines; ++i) {
+            if (e->cfg.min_energy != e->cfg.max_energy) {
+                e->sys[i].have_bounds = true;
+                e->sys[i].emin = e->cfg.min_energy;
+                e->sys[i].emax = e->cfg.max_energy;
+            } else if (engines[i]->sys[0].have_bounds && engines[i]->cfg.min_energy == engines[i]->cfg.max_energy &&
+                       engines[i]->cfg.lanczos_precision == e->cfg.lanczos_precision) {
+                e->sys[i] = engines[i]->sys[0];  // Lanczos bounds the member already found
+            }
+        }
+        bool const dbl = e->cfg.precision == KPM_PREC_FP64 ||
+                         (e->cfg.precision == KPM_PREC_AUTO && (st == KPM_F64 || st == KPM_C128));
+        bool const cpx = scalar_complex(st);
+        e->vtype = cpx ? (dbl ? kpm::V_C128 : kpm::V_C64) : (dbl ? kpm::V_F64 : kpm::V_F32);
         *out = e.release();
     });
 }

@@ -172,6 +172,9 @@ cudaError_t launch_kubo_integrate(double const* sum_nm, double const* scaled_sam
 cudaError_t launch_off_step(OffStep const& a, cudaStream_t s);
 cudaError_t launch_adj_step(AdjStep const& a, cudaStream_t s);
 // out = a x + b y over n elements of a real vector type (y nullable)
+// dst[0..bytes) = src[0..bytes), both 16-byte aligned; src may be host memory that the GPU
+// reads through the host page tables (a copy at the link's rate, no staging)
+cudaError_t launch_copy(void* dst, void const* src, size_t bytes, cudaStream_t s);
 cudaError_t launch_axpby(int vtype, int64_t n, double a, void const* x, double b, void const* y, void* out,
                          cudaStream_t s);
 bool diag_shape_supported(int vtype, int E, int LPR);

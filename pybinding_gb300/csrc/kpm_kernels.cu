@@ -1901,6 +1901,26 @@ cudaError_t launch_set_units(int vtype, void* dst, int32_t const* pos, int64_t n
     return cudaGetLastError();
 }
 
+__global__ void copy_kernel(uint4* __restrict__ dst, uint4 const* __restrict__ src, size_t n16,
+                            unsigned char* __restrict__ dtail, unsigned char const* __restrict__ stail, int ntail) {
+    size_t const stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
+    if (blockIdx.x == 0 && static_cast<int>(threadIdx.x) < ntail) dtail[threadIdx.x] = stail[threadIdx.x];
+}
+
+cudaError_t launch_copy(void* dst, void const* src, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return cudaSuccess;
+    if ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 16 != 0) return cudaErrorInvalidValue;
+    size_t const n16 = bytes / 16;
+    int const ntail = static_cast<int>(bytes % 16);
+    size_t const want = (n16 + 255) / 256;
+    int const g = static_cast<int>(want < 1 ? 1 : (want > 152 * 8 ? 152 * 8 : want));
+    copy_kernel<<<g, 256, 0, s>>>(static_cast<uint4*>(dst), static_cast<uint4 const*>(src), n16,
+                                  static_cast<unsigned char*>(dst) + n16 * 16,
+                                  static_cast<unsigned char const*>(src) + n16 * 16, ntail);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, int ndest, double* out, cudaStream_t s) {
     if (ndest == 0) return cudaSuccess;
     int const g = (ndest + 127) / 128;

@@ -17,7 +17,8 @@ from copy import copy
 
 import numpy as np
 
-from .chebyshev import DeferredLDOS, KPMBatch
+from . import _native
+from .chebyshev import DeferredLDOS
 
 __all__ = ["parallelize", "parallel_for", "sweep", "ndsweep", "Sweep", "NDSweep", "Factory"]
 
@@ -92,15 +93,15 @@ def _chunks(members):
 def _run_ldos_batch(chunk):
     global last_batch_stats, last_batch_times
     first = chunk[0].impl
-    options = {k: v for k, v in first._cfg_args.items() if k not in ("energy_range", "kernel", "kernel_param")}
     t0 = time.perf_counter()
-    batch = KPMBatch([d.impl.model for d in chunk], first._cfg_args["energy_range"], first.kernel, **options)
+    # the jobs' own engines already hold their checked matrices: concatenate those
+    engine = _native.Engine.from_engines([d.impl.engine for d in chunk], _native.make_config(**first._cfg_args))
     t1 = time.perf_counter()
     try:
-        out = batch.engine.calc_ldos_batch([d.site for d in chunk], chunk[0].energy, chunk[0].broadening)
-        last_batch_stats = batch.engine.stats()
+        out = engine.calc_ldos_batch([d.site for d in chunk], chunk[0].energy, chunk[0].broadening)
+        last_batch_stats = engine.stats()
     finally:
-        batch.close()
+        engine.close()
     last_batch_times = dict(assemble_s=t1 - t0, call_s=time.perf_counter() - t1)
     for d, ldos in zip(chunk, out):
         d.result = ldos[:, None]  # (energies, orbitals), as calc_ldos returns it

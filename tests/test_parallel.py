@@ -114,3 +114,37 @@ def test_sweep_of_deferred_ldos_runs_as_one_batch(monkeypatch):
         model = L.graphene_flake(2500, onsite_modifiers=[L.anderson_disorder(w, 3)], is_double=True)
         ref = pbg.kpm(model).calc_ldos(energy, 0.15, [0, 0]).data
         assert np.max(np.abs(row - ref)) / np.max(np.abs(ref)) < 1e-9
+
+
+def test_batch_engine_from_engines_checks_its_members():
+    from pybinding_gb300 import _native
+    cfg = _native.make_config()
+    a = _native.Engine(_flake(300, 1).hamiltonian, cfg)
+    b = _native.Engine(_flake(400, 2, double=True).hamiltonian, cfg)
+    with pytest.raises(ValueError, match="share the scalar type"):
+        _native.Engine.from_engines([a, b], cfg)
+    two = pbg.kpm_batch([_flake(300, 3), _flake(200, 4)]).engine
+    with pytest.raises(ValueError, match="one system each"):
+        _native.Engine.from_engines([a, two], cfg)
+    c = _native.Engine(_flake(500, 5).hamiltonian, cfg)
+    batch = _native.Engine.from_engines([a, c], cfg)
+    assert batch.num_systems == 2 and batch.rows == a.rows + c.rows
+    np.testing.assert_array_equal(batch.system_offsets, [0, a.rows, a.rows + c.rows])
+    batch.close()
+
+
+@pytest.mark.gpu
+def test_batch_engine_from_engines_matches_block_diagonal_batch():
+    from pybinding_gb300 import _native
+    models = [_flake(n, 40 + i, double=True) for i, n in enumerate((2000, 3100, 700))]
+    cfg = _native.make_config()
+    members = [_native.Engine(m.hamiltonian, cfg) for m in models]
+    members[1].scaling_factors()  # bounds found by a member are kept by the batch
+    joined = _native.Engine.from_engines(members, cfg)
+    ref = pbg.kpm_batch(models).engine
+    e = np.linspace(-8, 8, 51)
+    for s in range(3):
+        assert joined.scaling_factors(s) == ref.scaling_factors(s)
+    np.testing.assert_allclose(joined.calc_dos(e, 0.1, 2), ref.calc_dos(e, 0.1, 2), rtol=1e-12, atol=0)
+    np.testing.assert_allclose(joined.calc_ldos_batch([5, 7, 9], e, 0.1), ref.calc_ldos_batch([5, 7, 9], e, 0.1),
+                               rtol=1e-12, atol=0)
