@@ -148,3 +148,12 @@ def test_batch_engine_from_engines_matches_block_diagonal_batch():
     np.testing.assert_allclose(joined.calc_dos(e, 0.1, 2), ref.calc_dos(e, 0.1, 2), rtol=1e-12, atol=0)
     np.testing.assert_allclose(joined.calc_ldos_batch([5, 7, 9], e, 0.1), ref.calc_ldos_batch([5, 7, 9], e, 0.1),
                                rtol=1e-12, atol=0)
+
+
+def test_batched_ldos_checks_its_sites_before_the_gpu():
+    batch = pbg.kpm_batch([_flake(300, 1), _flake(200, 2)])
+    with pytest.raises(ValueError, match="one LDOS site per system"):
+        batch.engine.calc_ldos_batch([0], np.linspace(-1, 1, 5), 0.1)
+    with pytest.raises(RuntimeError, match="LDOS index out of range"):
+        batch.engine.calc_ldos_batch([0, 10 ** 6], np.linspace(-1, 1, 5), 0.1)
+    batch.close()
