@@ -1763,21 +1763,26 @@ int kpm_calc_dos(kpm_engine* e, const double* energy, int64_t ne, double broaden
             using Tin = decltype(zi);
             using R = real_of<Tin>;
             auto* o = reinterpret_cast<Tin*>(st.data());
-            for (int s = 0; s < e->nsys; ++s) {
+            // each system's generator draws in the reference's order; systems are independent
+            // and run in parallel, and the phases of complex starters are taken in parallel after
+            std::vector<R> draws(is_cplx_v<Tin> ? st.size() / sizeof(Tin) : 0);
+            parallel_for(e->nsys, [&](int64_t s) {
                 int64_t const n = e->sys_rows(s);
-                Tin* base = o + e->sys_off[s] * num_random;
+                int64_t const base = e->sys_off[s] * num_random;
                 std::mt19937 gen;
                 std::uniform_real_distribution<R> dist;
-                for (int64_t v = 0; v < num_random; ++v)
-                    for (int64_t i = 0; i < n; ++i) {
-                        if constexpr (is_cplx_v<Tin>) {
-                            std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
-                            std::complex<R> const k(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
-                            base[v * n + i] = std::exp(k * dist(gen));
-                        } else {
-                            base[v * n + i] = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
-                        }
-                    }
+                for (int64_t q = 0; q < num_random * n; ++q) {
+                    if constexpr (is_cplx_v<Tin>) draws[base + q] = dist(gen);
+                    else o[base + q] = (dist(gen) < 0.5f) ? R(-1.f) : R(1.f);
+                }
+            });
+            if constexpr (is_cplx_v<Tin>) {
+                std::complex<float> const kf = 2 * PI_F * std::complex<float>(0, 1);
+                std::complex<R> const k(static_cast<R>(kf.real()), static_cast<R>(kf.imag()));
+                int64_t const total = static_cast<int64_t>(draws.size()), chunk = 1 << 16;
+                parallel_for((total + chunk - 1) / chunk, [&](int64_t c) {
+                    for (int64_t q = c * chunk; q < std::min(total, (c + 1) * chunk); ++q) o[q] = std::exp(k * draws[q]);
+                });
             }
         });
         e->run_diag(Mmax, num_random, st.data(), false, nullptr, false);
