@@ -256,13 +256,21 @@ class DeferredLDOS(Deferred):
         self.impl = impl
         self.energy = np.asarray(energy, dtype=np.float64)
         self.broadening = float(broadening)
-        system = impl.model.system
-        idx = np.atleast_1d(system.to_hamiltonian_indices(system.find_nearest(position, sublattice)))
-        self.site = int(idx[0]) if idx.size == 1 else None  # None: multi-orbital, computed alone
+        self.position = position
+        self.sublattice = sublattice
 
-    def batch_key(self):
-        """Deferred LDOS with equal keys can share one recursion (None: this one cannot)."""
-        if self.site is None:
+    @property
+    def site(self):
+        """Hamiltonian row of the site nearest to ``position`` in the model as it is now (as
+        ``calc_ldos`` finds it when the job runs); None for a multi-orbital site."""
+        system = self.impl.model.system
+        idx = np.atleast_1d(system.to_hamiltonian_indices(system.find_nearest(self.position, self.sublattice)))
+        return int(idx[0]) if idx.size == 1 else None
+
+    def batch_key(self, site=None):
+        """Deferred LDOS with equal keys can share one recursion (None: this one cannot, e.g. a
+        multi-orbital site). ``site``: the job's :attr:`site`, when already known."""
+        if (self.site if site is None else site) is None:
             return None
         cfg = tuple(sorted((k, v) for k, v in self.impl._cfg_args.items()))
         return (cfg, np.dtype(self.impl.model.hamiltonian.dtype).str, self.energy.tobytes(), self.broadening)

@@ -2119,8 +2119,7 @@ void conductivity_mu(kpm_engine* e, const float* left, const float* right, int64
         // Velocity operators V = H o (x_i - x_j) in H's scalar type (kpm/Moments.cpp:132-155).
         // Left: applied to the random starter in the original order (Starter.cpp:66,78).
         // Right: applied to every collected vector, aligned with the reordered ELL of H~.
-        std::vector<int32_t> hcol(static_cast<size_t>(n) * W);
-        KPM_CUDA(cudaMemcpy(hcol.data(), e->d_col.p, hcol.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        std::vector<int32_t> const& hcol = e->h_col;  // host copy of the device ELL columns
         int const vs = kpm::vtype_vs(vt);
         std::vector<unsigned char> vr_ell(static_cast<size_t>(n) * W * vs * vb, 0);
         std::vector<unsigned char>& starters_l = e->h_starters;  // reused between calls (read in place)
@@ -2150,23 +2149,32 @@ void conductivity_mu(kpm_engine* e, const float* left, const float* right, int64
             using R = real_of<T>;
             auto const* hv = reinterpret_cast<T const*>(e->values.data());
             std::vector<T> vl(e->indices.size());
-            for (int64_t r = 0; r < n; ++r)
-                for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) {
-                    int32_t const c = e->indices[k];
-                    vl[k] = hv[k] * static_cast<T>(left[r] - left[c]);
-                    cd const vrv = to_cd(hv[k]) * static_cast<double>(right[r] - right[c]);
-                    int32_t const nr = e->map[r], nc = e->map[c];
-                    int j = 0;
-                    while (j < W && hcol[static_cast<size_t>(nr) * W + j] != nc) ++j;
-                    if (j == W) fail(KPM_ERR_RUNTIME, "internal: velocity entry outside the H~ pattern");
-                    with_vtype(vt, [&](auto zc) {
-                        using Tc = decltype(zc);
-                        Tc* o = reinterpret_cast<Tc*>(vr_ell.data()) + (static_cast<size_t>(nr) * W + j) * vs;
-                        Tc const hi = from_cd<Tc>(vrv);
-                        o[0] = hi;
-                        if (vs == 2) o[1] = from_cd<Tc>(vrv - to_cd(hi));
-                    });
-                }
+            // every entry writes its own slots: rows in parallel chunks
+            std::atomic<bool> outside{false};
+            int64_t const chunk = 1 << 14;
+            parallel_for((n + chunk - 1) / chunk, [&](int64_t ch) {
+                for (int64_t r = ch * chunk; r < std::min(n, (ch + 1) * chunk); ++r)
+                    for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) {
+                        int32_t const c = e->indices[k];
+                        vl[k] = hv[k] * static_cast<T>(left[r] - left[c]);
+                        cd const vrv = to_cd(hv[k]) * static_cast<double>(right[r] - right[c]);
+                        int32_t const nr = e->map[r], nc = e->map[c];
+                        int j = 0;
+                        while (j < W && hcol[static_cast<size_t>(nr) * W + j] != nc) ++j;
+                        if (j == W) {
+                            outside = true;
+                            continue;
+                        }
+                        with_vtype(vt, [&](auto zc) {
+                            using Tc = decltype(zc);
+                            Tc* o = reinterpret_cast<Tc*>(vr_ell.data()) + (static_cast<size_t>(nr) * W + j) * vs;
+                            Tc const hi = from_cd<Tc>(vrv);
+                            o[0] = hi;
+                            if (vs == 2) o[1] = from_cd<Tc>(vrv - to_cd(hi));
+                        });
+                    }
+            });
+            if (outside) fail(KPM_ERR_RUNTIME, "internal: velocity entry outside the H~ pattern");
             // both starters own a default-seeded generator, so left and right draw the same r;
             // the draws stay in the reference's order (one sequence over vectors, then sites),
             // the rest (phases, the left velocity product) runs in parallel over vectors
@@ -2199,7 +2207,7 @@ void conductivity_mu(kpm_engine* e, const float* left, const float* right, int64
         size_t const vec_bytes = static_cast<size_t>(n) * K * vb;
         DBuf d_v2, d_L, d_R, d_mu_acc, d_samples, d_sum, d_chem, d_res;
         d_v2.ensure(vr_ell.size());
-        KPM_CUDA(cudaMemcpyAsync(d_v2.p, vr_ell.data(), vr_ell.size(), cudaMemcpyHostToDevice, e->stream));
+        e->upload_host(d_v2.p, vr_ell.data(), vr_ell.size());
         // plane row stride: 16-byte multiple for the tensor maps
         int64_t const ld = ((n * K + 3) / 4) * 4;
         if (tc && (M > (int64_t{1} << 20) || n * K > (int64_t{1} << 31) - 64))

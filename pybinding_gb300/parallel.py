@@ -62,15 +62,16 @@ def compute_all(deferred):
     run as ragged batches (in their original order within a batch)."""
     groups, alone = {}, []
     for d in deferred:
-        key = d.batch_key() if isinstance(d, DeferredLDOS) else None
+        site = d.site if isinstance(d, DeferredLDOS) else None
+        key = d.batch_key(site) if site is not None else None
         if key is None:
             alone.append(d)
         else:
-            groups.setdefault(key, []).append(d)
+            groups.setdefault(key, []).append((d, site))
     for members in groups.values():
         for chunk in _chunks(members):
             if len(chunk) == 1:
-                chunk[0].compute()
+                chunk[0][0].compute()
             else:
                 _run_ldos_batch(chunk)
     for d in alone:
@@ -79,26 +80,29 @@ def compute_all(deferred):
 
 def _chunks(members):
     chunk, rows = [], 0
-    for d in members:
+    for d, site in members:
         n = d.impl.model.hamiltonian.shape[0]
         if chunk and rows + n > MAX_BATCH_ROWS:
             yield chunk
             chunk, rows = [], 0
-        chunk.append(d)
+        chunk.append((d, site))
         rows += n
     if chunk:
         yield chunk
 
 
 def _run_ldos_batch(chunk):
+    """Run the (job, site) pairs of ``chunk`` as one ragged batch."""
     global last_batch_stats, last_batch_times
+    sites = [site for _, site in chunk]
+    chunk = [d for d, _ in chunk]
     first = chunk[0].impl
     t0 = time.perf_counter()
     # the jobs' own engines already hold their checked matrices: concatenate those
     engine = _native.Engine.from_engines([d.impl.engine for d in chunk], _native.make_config(**first._cfg_args))
     t1 = time.perf_counter()
     try:
-        out = engine.calc_ldos_batch([d.site for d in chunk], chunk[0].energy, chunk[0].broadening)
+        out = engine.calc_ldos_batch(sites, chunk[0].energy, chunk[0].broadening)
         last_batch_stats = engine.stats()
     finally:
         engine.close()

@@ -43,9 +43,10 @@ def test_deferred_ldos_jobs_are_grouped_into_batches(monkeypatch):
     runs = []
 
     def fake_batch(chunk):
-        runs.append([d.impl.model.hamiltonian.shape[0] for d in chunk])
-        for d in chunk:
-            d.result = np.full((3, 1), float(d.site))
+        runs.append([d.impl.model.hamiltonian.shape[0] for d, _ in chunk])
+        for d, site in chunk:
+            assert site == d.site
+            d.result = np.full((3, 1), float(site))
 
     monkeypatch.setattr(parallel, "_run_ldos_batch", fake_batch)
     e = np.linspace(-1, 1, 3)
