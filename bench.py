@@ -70,7 +70,7 @@ def parse():
     p.add_argument("--cube-vectors", type=int, default=256, help="vectors of the 3D Anderson workload")
     p.add_argument("--cube-moments", type=int, default=8192, help="moments of the 3D Anderson workload")
     p.add_argument("--ldos-sites", type=int, default=4096, help="LDOS sites of the 3D Anderson workload (0: none)")
-    p.add_argument("--staging", default="auto", choices=["auto", "registers", "tma", "async"],
+    p.add_argument("--staging", default="auto", choices=["auto", "registers", "tma", "async", "gather"],
                    help="recursion kernel operands (auto = chosen by timing; pin it under a profiler)")
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2], help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
@@ -297,7 +297,7 @@ def run_gpu(args, rank, world, local_rank):
     fuse = int(eng.stats().steps_per_launch)
     lane_map = (int(eng.stats().elems_per_lane), int(eng.stats().lanes_per_row))
     tiling = {"tile_rows": int(eng.stats().tile_rows), "unroll": int(eng.stats().unroll),
-              "staged_rows": int(eng.stats().staged_rows)}
+              "staged_rows": int(eng.stats().staged_rows), "gather_rows": int(eng.stats().gather_rows)}
     launches = 1 + (M // 2 - 1) // fuse  # init + recursion launches
     avg_launch = rec / launches
     nrows = rows
@@ -371,7 +371,8 @@ def run_gpu(args, rank, world, local_rank):
                "moment_error_vs_fp64": err,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
-                            "kernel": "%s<float,%d,%d>" % (("diag_tma_kernel" if tiling["staged_rows"] > 0 else
+                            "kernel": "%s<float,%d,%d>" % (("diag_gather_kernel" if tiling["gather_rows"] > 0 else
+                                                            "diag_tma_kernel" if tiling["staged_rows"] > 0 else
                                                             "diag_async_kernel" if tiling["staged_rows"] < 0 else
                                                             "diag_step_kernel") if fuse == 1 else "diag_pair_kernel",
                                                            lane_map[0], lane_map[1]),
@@ -640,7 +641,8 @@ def workload_anderson3d(args, stream_of):
           "f32",
           roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",
                     "frac": alg / avg / 1e9 / peak, "traffic": None, "steps_per_launch": fuse,
-                    "kernel": (("diag_tma_kernel" if s.staged_rows > 0 else "diag_async_kernel" if s.staged_rows < 0
+                    "kernel": (("diag_gather_kernel" if s.gather_rows > 0 else
+                                "diag_tma_kernel" if s.staged_rows > 0 else "diag_async_kernel" if s.staged_rows < 0
                                 else "diag_step_kernel") if fuse == 1 else "diag_pair_kernel"),
                     "lane_map": [int(s.elems_per_lane), int(s.lanes_per_row)], "tile_rows": int(s.tile_rows),
                     "unroll": int(s.unroll),

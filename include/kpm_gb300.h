@@ -67,8 +67,9 @@ typedef struct kpm_config {
     int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, or 0 = chosen by timing */
     int32_t staging;          /* diagonal step operands: 0 = chosen by timing, 1 = register loads,
                                  2 = TMA bulk copies into shared memory, 3 = per-thread cp.async
-                                 pipeline (2 and 3: full-system recursions of 16-byte-lane shapes,
-                                 3 also rows of <= 4 entries; others use register loads) */
+                                 pipeline, 4 = TMA bulk copies plus TMA gathers of the neighbour rows
+                                 (2, 3 and 4: full-system recursions of 16-byte-lane shapes, 3 also
+                                 rows of <= 4 entries, 4 FP32 only; others use register loads) */
 } kpm_config;
 
 /* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */
@@ -97,6 +98,7 @@ typedef struct kpm_stats {
     int32_t unroll;           /*   rows per thread per iteration */
     double upload_time;       /* seconds (device): starter upload and scatter of the last diagonal call */
     double call_time;         /* seconds (host wall clock) of the last call, entry to return */
+    int32_t gather_rows;      /* > 0: the step gathered x rows with TMA tile::gather4, tiles of this many rows */
 } kpm_stats;
 
 typedef struct kpm_engine kpm_engine;

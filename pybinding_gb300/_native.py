@@ -22,7 +22,7 @@ SCALAR_CODE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1,
                np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
 KERNEL_CODE = {"jackson": 0, "lorentz": 1, "dirichlet": 2}
 PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2}
-STAGING_CODE = {"auto": 0, "registers": 1, "tma": 2, "async": 3}
+STAGING_CODE = {"auto": 0, "registers": 1, "tma": 2, "async": 3, "gather": 4}
 
 
 class Config(C.Structure):
@@ -43,7 +43,7 @@ class Stats(C.Structure):
                 ("eps", C.c_double), ("steps_per_launch", C.c_int32), ("gemm_time", C.c_double),
                 ("elems_per_lane", C.c_int32), ("lanes_per_row", C.c_int32), ("staged_rows", C.c_int32),
                 ("tile_rows", C.c_int32), ("unroll", C.c_int32), ("upload_time", C.c_double),
-                ("call_time", C.c_double)]
+                ("call_time", C.c_double), ("gather_rows", C.c_int32)]
 
 
 class Honeycomb(C.Structure):

@@ -365,7 +365,7 @@ struct kpm_engine {
     struct RecursionGraphKey {
         void const *x0, *x1, *acc, *tiles, *col, *val;
         int64_t half, bstride, step_acc;
-        int ntiles, vtype, E, LPR, nbatch, unroll, W, tma_rows;
+        int ntiles, vtype, E, LPR, nbatch, unroll, W, tma_rows, gather_rows;
         int32_t row_limit;
         int* error;
         bool real_matrix;
@@ -947,7 +947,7 @@ struct kpm_engine {
         cudaGetDevice(&dev);
         return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, full_rows, real_values};
     }
-    struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; bool async_copy; };
+    struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; bool async_copy; int gather_rows = 0; };
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
     template<class T>
@@ -1276,13 +1276,17 @@ struct kpm_engine {
             sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : (256 / sh.LPR) * 16;
             a.async_copy = true;
             alt_map = true;
+        } else if (cfg.staging == 4 && full_rows && vtype == kpm::V_F32 && sh.E == 4 && sh.K <= 256) {
+            sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 32;
+            a.gather_rows = sh.rows_per_tile;
+            alt_map = true;
         } else if (cfg.tile_rows > 0) {
             sh.rows_per_tile = cfg.tile_rows;
         } else {
             Tuned const tu = tune_diag(sh, sys0, batch_outer, full_rows, a);
             sh.rows_per_tile = tu.rows_per_tile;
             a.unroll = tu.unroll;
-            alt_map = tu.E != sh.E || tu.tma_rows > 0 || tu.async_copy;
+            alt_map = tu.E != sh.E || tu.tma_rows > 0 || tu.async_copy || tu.gather_rows > 0;
             if (alt_map && cfg.fuse_steps == 2 && !opt_rows) {  // two-step launches asked for: default kernel
                 alt_map = false;
                 sh.rows_per_tile = (256 / sh.LPR) * 16;
@@ -1292,6 +1296,7 @@ struct kpm_engine {
                 sh.LPR = tu.LPR;
                 a.tma_rows = tu.tma_rows;
                 a.async_copy = tu.async_copy;
+                a.gather_rows = tu.gather_rows;
             }
             a.E = sh.E;
             a.LPR = sh.LPR;
@@ -1433,6 +1438,7 @@ struct kpm_engine {
             key.W = W;
             key.row_limit = a.row_limit;
             key.tma_rows = a.tma_rows;
+            key.gather_rows = a.gather_rows;
             key.real_matrix = a.real_matrix;
             key.async_copy = a.async_copy;
             key.error = a.error;
@@ -1463,6 +1469,7 @@ struct kpm_engine {
         while (n <= half) single_step();
         last_fuse = choice.steps;
         last_tma_rows = a.async_copy ? -sh.rows_per_tile : a.tma_rows;
+        last_gather_rows = a.gather_rows;
         last_unroll = a.unroll;
         KPM_CUDA(cudaEventRecord(ev1, stream));
         KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
@@ -1484,6 +1491,7 @@ struct kpm_engine {
     Shape last_shape{};
     int last_fuse = 1;
     int last_tma_rows = 0;
+    int last_gather_rows = 0;
     int last_unroll = 1;
     double last_upload_time = 0;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
@@ -1521,6 +1529,7 @@ struct kpm_engine {
         st.elems_per_lane = last_shape.E;
         st.lanes_per_row = last_shape.LPR;
         st.staged_rows = last_tma_rows;
+        st.gather_rows = last_gather_rows;
         st.tile_rows = last_shape.rows_per_tile;
         st.unroll = last_unroll;
         st.upload_time = last_upload_time;
@@ -1597,7 +1606,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
-        if (e->cfg.staging < 0 || e->cfg.staging > 3) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2 or 3");
+        if (e->cfg.staging < 0 || e->cfg.staging > 4) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2, 3 or 4");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
         *out = e.release();
     });
@@ -1630,7 +1639,7 @@ int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
-        if (e->cfg.staging < 0 || e->cfg.staging > 3) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2 or 3");
+        if (e->cfg.staging < 0 || e->cfg.staging > 4) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2, 3 or 4");
         // the members' CSR matrices were checked when their engines were made: concatenate them
         // (columns shifted into their block), each member's copy in parallel
         int const st = engines[0]->stype;

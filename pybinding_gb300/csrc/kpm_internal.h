@@ -46,6 +46,8 @@ struct DiagStep {
                               // K * element size a multiple of 16 bytes; col/val padded by 32 bytes)
     int* error = nullptr;     // TMA-staged kernel: set when a bounded wait gives up
     bool async_copy = false;  // cp.async pipeline kernel (rows of <= 4 entries, 16-byte lanes; full rows)
+    int gather_rows = 0;      // > 0: TMA gather kernel (x rows gathered by tile::gather4 into shared memory),
+                              // tiles of at most this many rows (FP32, E = 4, full rows)
     bool real_matrix = false; // complex vectors with real H~ values: val holds [rows][W][vs] of the
                               // real type (vs of that type: hi/lo pairs for FP32)
 };
