@@ -20,7 +20,7 @@ workload, on rank 0.
 
 `--workload` selects one of the other configurations instead (one JSON line
 each, same keys; they are measurements of the other hot-path rows, not the
-headline): `dos_c1` (60k-site complex128 graphene DOS, 8 vectors, 2048
+headline): `dos_c128_60k` (60k-site complex128 graphene DOS, 8 vectors, 2048
 moments), `conductivity` (1M-site graphene at 20 T, complex128, 16 vectors,
 512 x 512 moments matrix on the tensor cores), `adjoint` (256k-site strained
 graphene, DOS misfit gradient, 32 vectors, 1024 moments, FP32) and
@@ -75,7 +75,7 @@ def parse():
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2], help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
-                   choices=["dos_batch", "dos_c1", "conductivity", "adjoint", "anderson3d", "lattice", "sweep"])
+                   choices=["dos_batch", "dos_c128_60k", "conductivity", "adjoint", "anderson3d", "lattice", "sweep"])
     p.add_argument("--sweep-models", type=int, default=32, help="models of the sweep workload")
     p.add_argument("--sweep-sites", type=int, default=100_000, help="sites per model of the sweep workload")
     p.add_argument("--lattice-sites", type=int, default=4_000_000, help="sites of the lattice-build workload")
@@ -437,7 +437,7 @@ def _line(args, metric, value, unit, hib, t_step, config, dtype, **extra):
     print(json.dumps(out), flush=True)
 
 
-def workload_dos_c1(args, stream_of):
+def workload_dos_c128_60k(args, stream_of):
     """60,000-site complex128 graphene flake (t = -2.8 eV, onsite 0), 8 random-phase vectors,
     2048 moments (2050 after rounding), Jackson, Lanczos bounds, DOS at 1000 energies in [-9, 9]."""
     from pybinding_gb300 import _native, lattice as L
@@ -814,7 +814,7 @@ def run_workload(args, rank, world, local_rank):
 
     def stream_of(eng):
         return torch.cuda.ExternalStream(eng.stream())
-    {"dos_c1": workload_dos_c1, "conductivity": workload_conductivity, "adjoint": workload_adjoint,
+    {"dos_c128_60k": workload_dos_c128_60k, "conductivity": workload_conductivity, "adjoint": workload_adjoint,
      "anderson3d": workload_anderson3d, "lattice": workload_lattice,
      "sweep": workload_sweep}[args.workload](args, stream_of)
 

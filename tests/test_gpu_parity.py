@@ -2,7 +2,7 @@
 reference's FP64 NumPy KPM, and the reference's golden arrays.
 
 Error measure for moments: max_n |mu_n - mu_n^ref| / max_n |mu_n^ref|.
-Tolerances: FP64 recursion <= 1e-10 (the spec bar); FP32 recursion
+Tolerances: FP64 recursion <= 1e-10 (the FP64 accuracy target); FP32 recursion
 vectors with FP64 moment sums <= 1e-5 at these sizes (the measured error is
 printed); reconstructed functions against the reference goldens at the
 reference's own test tolerances.
