@@ -770,9 +770,9 @@ cudaError_t diag_tma_launch(DiagStep const& a, cudaStream_t s) {
 // dependent global round trip on the consumers, and the copies in flight per SM are bounded
 // by the stages, not by registers. FP32 recursions (E = 4, K = 4 LPR <= 256), full rows.
 // Measured on the 32-flake FP32 workload: 4.19 ms per step against 1.32 ms for register
-// loads (one gather4 per row, issued by the producer warp after a dependent load of the
-// row's indices), so it is not among the options timed on a first call; staging = 4
-// selects it.
+// loads, and the same with the next tile's indices prefetched: one gather4 per row takes
+// ~160 SM cycles of TMA issue. So it is not among the options timed on a first call;
+// staging = 4 selects it.
 constexpr int GTH_STAGES = 3;
 
 struct GatherLayout {
