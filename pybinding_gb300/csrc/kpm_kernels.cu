@@ -26,6 +26,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 #include <cstdint>
 #include <cstring>
@@ -35,6 +36,10 @@ namespace {
 
 constexpr int BLOCK = 256;
 constexpr int WARPS = BLOCK / 32;
+
+// Guards the per-kernel launch caches below (shared-memory attributes set, occupancy): engines
+// on different host threads launch concurrently.
+std::mutex g_launch_cache_mutex;
 
 // VS: matrix values per entry. FP32 recursions store each value of H~ as an
 // unevaluated sum hi + lo of two FP32 numbers (hi = fl32(h), lo = fl32(h - hi),
@@ -482,6 +487,7 @@ cudaError_t diag_async_launch(DiagStep const& a, cudaStream_t s) {
     auto fn = a.init ? diag_async_kernel<V, E, LPR, true> : diag_async_kernel<V, E, LPR, false>;
     static void const* done[16];
     static int ndone = 0;
+    std::lock_guard<std::mutex> lock(g_launch_cache_mutex);
     bool set = false;
     for (int i = 0; i < ndone; ++i) set = set || done[i] == reinterpret_cast<void const*>(fn);
     if (!set) {
@@ -734,6 +740,7 @@ cudaError_t diag_tma_launch(DiagStep const& a, cudaStream_t s) {
     static size_t done_smem[32];
     static int done_occ[32];
     static int ndone = 0;
+    std::unique_lock<std::mutex> lock(g_launch_cache_mutex);
     int occ = 0;
     for (int i = 0; i < ndone; ++i)
         if (done_fn[i] == reinterpret_cast<void const*>(fn) && done_smem[i] == smem) occ = done_occ[i];
@@ -947,14 +954,14 @@ diag_gather_kernel(const __grid_constant__ CUtensorMap xmap, int32_t const* __re
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 rows_encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static PFN_cuTensorMapEncodeTiled_v12000 const fn = [] {  // thread-safe one-time lookup
         cudaDriverEntryPointQueryResult q;
         void* p = nullptr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
+    }();
     return fn;
 }
 
@@ -983,6 +990,7 @@ cudaError_t diag_gather_launch(DiagStep const& a, cudaStream_t s) {
     static void const* set_fn[16];
     static size_t set_smem[16];
     static int nset = 0;
+    std::unique_lock<std::mutex> lock(g_launch_cache_mutex);
     int k = 0;
     while (k < nset && set_fn[k] != reinterpret_cast<void const*>(fn)) ++k;
     if (k == nset || set_smem[k] < smem) {
@@ -1487,10 +1495,13 @@ __global__ void kubo_integrate_kernel(double const* __restrict__ sum_nm, double 
 }
 
 int persistent_grid(void const* fn, int num_tiles) {
-    static int sms = 0;
+    constexpr int kMaxDevices = 64;
+    static int sms_of[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_launch_cache_mutex);
+    int& sms = sms_of[dev >= 0 && dev < kMaxDevices ? dev : 0];
     if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }

@@ -541,3 +541,34 @@ def test_tma_gather_step_matches_register_step_and_oracle(oracle, nvec):
             err = rel_err(out[k][s], ref)
             print("gather test %s system %d (K=%d): %.3e" % (k, s, nvec, err))
             assert err <= 1e-5
+
+
+def test_engines_on_two_host_threads_agree_with_one_thread():
+    """ctypes releases the GIL around engine calls: two engines driven from two host threads at
+    once (shared launch caches, process-wide tuning cache) give the moments of one-by-one calls."""
+    import threading
+    hs = [_disordered_flake(n, 30 + i, np.float64) for i, n in enumerate((7001, 5003))]
+    starters = [np.where(np.random.default_rng(i).integers(0, 2, (8, h.shape[0])) == 0, -1.0, 1.0)[None]
+                for i, h in enumerate(hs)]
+    cfg = dict(energy_range=(-9.5, 9.5))
+    ref = [_native.Engine(h, _native.make_config(**cfg)).moments_diag(258, st) for h, st in zip(hs, starters)]
+    out = [None, None]
+    errors = []
+
+    def run(i):
+        try:
+            eng = _native.Engine(hs[i], _native.make_config(**cfg))
+            for _ in range(3):
+                out[i] = eng.moments_diag(258, starters[i])
+            eng.close()
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for i in range(2):
+        assert rel_err(out[i], ref[i]) < 1e-12
