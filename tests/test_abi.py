@@ -169,3 +169,18 @@ def test_optimized_hamiltonian_disconnected_bit_exact(oracle):
             assert np.array_equal(got["h2"].data.view(np.uint8), ref["h2"].data.view(np.uint8))
             assert np.array_equal(got["slices"], ref["slices"])
         eng.close()
+
+
+def test_config_fields_are_checked_on_create():
+    """kpm_create rejects launch options outside their ranges before touching the GPU."""
+    h = _small_h()
+    for field, bad, msg in (("staging", 5, "staging must be"), ("fuse_steps", 3, "fuse_steps must be"),
+                            ("precision", 7, "unknown precision mode")):
+        cfg = _native.make_config()
+        setattr(cfg, field, bad)
+        with pytest.raises(ValueError, match=msg):
+            _native.Engine(h, cfg)
+    for staging in ("auto", "registers", "tma", "async", "gather"):
+        _native.Engine(h, _native.make_config(staging=staging)).close()
+    with pytest.raises(ValueError, match="Invalid energy range"):
+        _native.Engine(h, _native.make_config(energy_range=(1.0, -1.0)))
