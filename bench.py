@@ -72,7 +72,8 @@ def parse():
     p.add_argument("--ldos-sites", type=int, default=4096, help="LDOS sites of the 3D Anderson workload (0: none)")
     p.add_argument("--staging", default="auto", choices=["auto", "registers", "tma", "async", "gather"],
                    help="recursion kernel operands (auto = chosen by timing; pin it under a profiler)")
-    p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2], help="steps per launch (0 = chosen by timing)")
+    p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2, 3],
+                   help="steps per launch (0 = chosen by timing, 3 = all steps in one launch)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
                    choices=["dos_batch", "dos_c128_60k", "conductivity", "adjoint", "anderson3d", "lattice", "sweep"])
@@ -443,7 +444,7 @@ def workload_dos_c128_60k(args, stream_of):
     from pybinding_gb300 import _native, lattice as L
     m = L.graphene_flake(60000, is_complex=True, is_double=True)
     h = m.hamiltonian.astype(np.complex128)
-    eng = _native.Engine(h, _native.make_config())
+    eng = _native.Engine(h, _native.make_config(fuse_steps=args.fuse, staging=args.staging))
     a, b = eng.scaling_factors()
     broadening = _jackson_broadening(2048, a)
     energy = np.linspace(-9, 9, 1000)
@@ -453,9 +454,11 @@ def workload_dos_c128_60k(args, stream_of):
     M = st.num_moments
     work = (M / 2) * h.nnz * 8
     rec = st.moments_time
-    launches = M // 2
-    alg = h.nnz * 20 + 4 * (h.shape[0] + 1) + 3 * h.shape[0] * 8 * 16
-    achieved = alg / (rec / launches) / 1e9
+    steps = M // 2
+    spl = max(1, int(st.steps_per_launch))  # all steps after the first in one launch when > 2
+    launches = 1 + -(-(steps - 1) // spl)
+    alg = h.nnz * 20 + 4 * (h.shape[0] + 1) + 3 * h.shape[0] * 8 * 16  # per step
+    achieved = alg / (rec / steps) / 1e9
     cpu = None
     if args.cpu_seconds > 0:
         from oracle import oracle as O
@@ -476,7 +479,9 @@ def workload_dos_c128_60k(args, stream_of):
           "c128",
           roofline={"bound": "l2 (latency)", "achieved": achieved, "unit": "GB/s",
                     "note": "working set fits in L2; HBM fraction not meaningful",
-                    "avg_launch_us": rec / launches * 1e6, "alg_bytes_per_launch": alg},
+                    "avg_step_us": rec / steps * 1e6, "alg_bytes_per_step": alg, "steps_per_launch": spl,
+                    "kernel": "diag_multi_kernel (all steps, one cooperative launch)" if spl > 2 else
+                              "diag_step_kernel"},
           e2e={"value": work / (wall / args.steps) / 1e9, "unit": "Gnnz*vec/s", "h2d_bytes_per_step": 8000,
                "d2h_bytes_per_step": 8000},
           cpu_baseline=cpu, clocks=clk, time_per_dos_ms=t / args.steps * 1e3,

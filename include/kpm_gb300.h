@@ -64,7 +64,8 @@ typedef struct kpm_config {
     int32_t precision;        /* KPM_PREC_* */
     int32_t batch_width;      /* vectors per recursion block (upper bound); 0 = 256-byte rows */
     int32_t tile_rows;        /* rows per thread block tile; 0 = autotuned on the first call */
-    int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, or 0 = chosen by timing */
+    int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, 3 = all steps in one cooperative
+                                 launch (systems whose vectors fit in L2; else 1), or 0 = chosen by timing */
     int32_t staging;          /* diagonal step operands: 0 = chosen by timing, 1 = register loads,
                                  2 = TMA bulk copies into shared memory, 3 = per-thread cp.async
                                  pipeline, 4 = TMA bulk copies plus TMA gathers of the neighbour rows

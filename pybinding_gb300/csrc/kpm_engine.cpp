@@ -350,7 +350,7 @@ struct kpm_engine {
     int pair_key_nbatch = -1, pair_key_lpr = -1;
     int64_t pair_key_rows = -1;
     int pair_seq = 0;
-    DBuf d_pair_counters, d_pair_error;
+    DBuf d_pair_counters, d_pair_error, d_multi_bar;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1381,17 +1381,39 @@ struct kpm_engine {
             choice = FuseChoice{2, cfg.tile_rows > 0 ? cfg.tile_rows : rpp * 8};
             have_choice = true;
         }
+        // all steps in one cooperative launch (choice steps = 3): recursions whose vectors and
+        // matrix stay in L2, where the per-step launch gap and ramp weigh most
+        size_t const l2_bytes = 2 * vbytes + static_cast<size_t>(rows) * W * (4 + kpm::vtype_vs(vtype) * vb);
+        // (any lane mapping of the register-load step; not the staged kernels)
+        bool const multi_ok = !opt_rows && cfg.fuse_steps != 1 && a.tma_rows == 0 && !a.async_copy &&
+                              a.gather_rows == 0 && l2_bytes <= (size_t{64} << 20);
+        d_multi_bar.ensure(2 * sizeof(unsigned));
+        auto multi_steps = [&](int64_t count) {
+            KPM_CUDA(cudaMemsetAsync(d_multi_bar.p, 0, 2 * sizeof(unsigned), stream));
+            KPM_CUDA(kpm::launch_diag_multi(a, r0, r1, n, n + count - 1, d_acc.as<double>(),
+                                            static_cast<int64_t>(step_acc), d_multi_bar.as<unsigned>(), 1 << 25,
+                                            stream));
+            if (count % 2) std::swap(r0, r1);
+            n += count;
+        };
+        if (cfg.fuse_steps == 3) {  // asked for: one launch where the system fits, else one step per launch
+            choice = FuseChoice{multi_ok ? 3 : 1, 0};
+            have_choice = true;
+        }
         if (can_pair && !have_choice) {
-            // time each candidate on the first steps of this recursion (any partition gives the
-            // same result), then keep the fastest per two steps
+            // time each candidate on four steps of this recursion, keep the fastest, then start
+            // the recursion over with it. The one-launch form is not a candidate: on the 60k-site
+            // complex128 DOS it ran 26.8 us per step against 22.0 us for graph-replayed single
+            // steps (its gathers must bypass L1 for coherence across the grid barrier)
             std::vector<FuseChoice> cands{{1, 0}};
             for (int rpt : {4, 8, 16, 32}) cands.push_back({2, rpp * rpt});
             double best = 1e30;
-            if (half - 1 >= 2 * static_cast<int64_t>(cands.size()) + 2) {
+            if (half - 1 >= 4 * static_cast<int64_t>(cands.size()) + 2) {
                 for (auto const& c : cands) {
                     PairPlan* pp = c.steps == 2 ? pair_plan(sh, c.rows_per_tile) : nullptr;
                     KPM_CUDA(cudaEventRecord(ev_t0, stream));
-                    if (pp) pair_step(pp); else { single_step(); single_step(); }
+                    if (pp) { pair_step(pp); pair_step(pp); }
+                    else for (int k = 0; k < 4; ++k) single_step();
                     KPM_CUDA(cudaEventRecord(ev_t1, stream));
                     KPM_CUDA(cudaEventSynchronize(ev_t1));
                     float ms = 0;
@@ -1415,6 +1437,11 @@ struct kpm_engine {
         if (choice.steps == 2 && can_pair) {
             PairPlan* pp = pair_plan(sh, choice.rows_per_tile);
             while (n + 1 <= half) pair_step(pp);
+        }
+        int64_t multi_count = 0;
+        if (choice.steps == 3 && multi_ok && n <= half) {
+            multi_count = half - n + 1;
+            multi_steps(multi_count);
         }
         if (n == 2 && half >= 3 && !opt_rows) {
             // steady state (no tuning steps ran in this call): replay the captured recursion
@@ -1467,7 +1494,7 @@ struct kpm_engine {
             KPM_CUDA(cudaGraphLaunch(graph_exec, stream));
         }
         while (n <= half) single_step();
-        last_fuse = choice.steps;
+        last_fuse = multi_count > 0 ? static_cast<int>(multi_count) : (choice.steps == 3 ? 1 : choice.steps);
         last_tma_rows = a.async_copy ? -sh.rows_per_tile : a.tma_rows;
         last_gather_rows = a.gather_rows;
         last_unroll = a.unroll;
@@ -1605,7 +1632,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
-        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
+        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 3) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1, 2 or 3");
         if (e->cfg.staging < 0 || e->cfg.staging > 4) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2, 3 or 4");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
         *out = e.release();
@@ -1638,7 +1665,7 @@ int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
-        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
+        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 3) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1, 2 or 3");
         if (e->cfg.staging < 0 || e->cfg.staging > 4) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2, 3 or 4");
         // the members' CSR matrices were checked when their engines were made: concatenate them
         // (columns shifted into their block), each member's copy in parallel

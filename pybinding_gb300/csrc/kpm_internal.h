@@ -148,6 +148,12 @@ struct DiagPair {
 };
 
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s);
+// Steps n0..n1 of the diagonal recursion in one cooperative launch (full rows, register
+// loads): step n reads x = r1, overwrites r0 = y, adds its sums at acc_base + step_acc (n - 1),
+// then swaps r0 and r1; the blocks meet at a grid barrier (bar: two zeroed counters) between
+// steps, whose waits give up after spin_limit polls and set a.error.
+cudaError_t launch_diag_multi(DiagStep const& a, void* r0, void* r1, int64_t n0, int64_t n1, double* acc_base,
+                              int64_t step_acc, unsigned* bar, int spin_limit, cudaStream_t s);
 cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s);
 cudaError_t launch_dense_step(DenseStep const& a, cudaStream_t s);
 

@@ -178,7 +178,10 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
         if (!live[u]) continue;
         P const* xp = reinterpret_cast<P const*>(x + static_cast<int64_t>(rr[u]) * K) + lane;
         xr[u] = XCOH ? ld_l2(xp) : ld_ro(xp);
-        if (!INIT) yo[u] = ld_stream(reinterpret_cast<P const*>(y + static_cast<int64_t>(rr[u]) * K) + lane);
+        if (!INIT) {  // XCOH: rows written earlier in the same launch are read through L2 only
+            P const* yp = reinterpret_cast<P const*>(y + static_cast<int64_t>(rr[u]) * K) + lane;
+            yo[u] = XCOH ? ld_l2(yp) : ld_stream(yp);
+        }
 #pragma unroll
         for (int e = 0; e < E; ++e) { vzero(sum[u][e]); vzero(lo[u][e]); }
     }
@@ -325,6 +328,102 @@ diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, in
     }
     if (cur_sys >= 0)
         diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+}
+
+// ------------------------------------------------------------------ many steps per launch
+// For recursions whose vectors stay in L2, every step in one cooperative launch: the blocks
+// sweep their tiles (the same tiles every step), add their moment partials to the step's
+// accumulator, and meet at a grid barrier before the next step, which saves the launch
+// gap and ramp of each step. The gathers of a step read rows other blocks wrote in the
+// step before, so x and y_old are read through L2 (the XCOH form of the row loop). The
+// barrier is a generation count: the last block to
+// arrive resets the arrival count and releases the next generation; the others poll it
+// with a bounded number of sleeps and, when it runs out, set *err and leave.
+__device__ __forceinline__ unsigned ld_acquire_u(unsigned const* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// bar[0] = arrivals of the current generation, bar[1] = generation
+__device__ bool grid_barrier(unsigned* bar, int* err, int spin_limit) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        unsigned const g = ld_acquire_u(bar + 1);
+        __threadfence();
+        if (atomicAdd(bar, 1u) + 1 == gridDim.x) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            st_release_u(bar + 1, g + 1);
+        } else {
+            int polls = 0;
+            while (ld_acquire_u(bar + 1) == g) {
+                if (++polls > spin_limit || *reinterpret_cast<int volatile*>(err) != 0) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+template<class V, int E, int LPR, class MV = V>
+__global__ void __launch_bounds__(BLOCK)
+diag_multi_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W, V* r0, V* r1,
+                  int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles, int nbatch,
+                  double* __restrict__ acc_base, int64_t step_acc, int64_t n0, int64_t n1, unsigned* bar,
+                  int* err, int spin_limit) {
+    using R = typename Tr<V>::R;
+    constexpr bool CPLX = Tr<V>::C;
+    constexpr int K = E * LPR;
+    constexpr int RPP = BLOCK / LPR;
+    constexpr int NV = CPLX ? 3 : 2;
+    __shared__ R red[WARPS * K * NV];
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    int const G = gridDim.x;
+    for (int64_t n = n0; n <= n1; ++n) {
+        V const* x_all = r1;  // T_{n-1}
+        V* y_all = r0;        // T_{n-2} -> T_n
+        double* acc = acc_base + step_acc * (n - 1);
+        R m2[E], m3r[E], m3i[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
+        int cur_sys = -1, cur_batch = -1;
+        for (int ti = blockIdx.x; ti < num_tiles; ti += G) {
+            Tile const t = tiles[ti];
+            if (t.system != cur_sys || t.batch != cur_batch) {
+                if (cur_sys >= 0)
+                    diag_flush<V, E, LPR>(m2, m3r, m3i, red,
+                                          acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+                cur_sys = t.system;
+                cur_batch = t.batch;
+            }
+            V const* __restrict__ x = x_all + t.batch * batch_stride;
+            V* __restrict__ y = y_all + t.batch * batch_stride;
+            for (int r = t.row_begin + slot; r < t.row_end; r += RPP) {
+                int rr[1] = {r};
+                bool live[1] = {true};
+                diag_rows<V, E, LPR, false, 1, true, MV>(col, val, W, x, y, rr, live, lane, m2, m3r, m3i);
+            }
+        }
+        if (cur_sys >= 0)
+            diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+        V* const tmp = r0;
+        r0 = r1;
+        r1 = tmp;
+        if (n < n1 && !grid_barrier(bar, err, spin_limit)) return;
+    }
 }
 
 // ------------------------------------------------------------------ diagonal step, cp.async pipeline
@@ -2036,6 +2135,49 @@ cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s) {
 
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s) {
 #define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return diag_launch<V, e, l>(a, s);
+    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
+    KPM_DIAG_ALT_F32(KPM_DISPATCH) KPM_DIAG_ALT_F64(KPM_DISPATCH) KPM_DIAG_ALT_C64(KPM_DISPATCH)
+#undef KPM_DISPATCH
+    return cudaErrorInvalidValue;
+}
+
+template<class V, int E, int LPR>
+cudaError_t diag_multi_launch(DiagStep const& a, void* r0, void* r1, int64_t n0, int64_t n1, double* acc_base,
+                              int64_t step_acc, unsigned* bar, int spin_limit, cudaStream_t s) {
+    if (a.num_tiles == 0 || n1 < n0) return cudaSuccess;
+    if (a.error == nullptr || bar == nullptr) return cudaErrorInvalidValue;
+    auto run = [&](auto fn, auto const* val) {
+        // every block must be resident at once: at most SMs x occupancy blocks
+        int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
+        int32_t const* col = a.col;
+        int W = a.W;
+        V* p0 = static_cast<V*>(r0);
+        V* p1 = static_cast<V*>(r1);
+        int64_t bstride = a.batch_stride;
+        Tile const* tiles = a.tiles;
+        int num_tiles = a.num_tiles, nbatch = a.nbatch;
+        int* err = a.error;
+        int spin = spin_limit;
+        void* args[] = {&col, &val, &W, &p0, &p1, &bstride, &tiles, &num_tiles, &nbatch, &acc_base, &step_acc,
+                        &n0, &n1, &bar, &err, &spin};
+        return cudaLaunchCooperativeKernel(reinterpret_cast<void const*>(fn), dim3(g), dim3(BLOCK), args, 0, s);
+    };
+    if (a.real_matrix) {
+        if constexpr (Tr<V>::C) {
+            using MR = typename Tr<V>::R;
+            return run(diag_multi_kernel<V, E, LPR, MR>, static_cast<MR const*>(a.val));
+        } else {
+            return cudaErrorInvalidValue;
+        }
+    }
+    return run(diag_multi_kernel<V, E, LPR, V>, static_cast<V const*>(a.val));
+}
+
+cudaError_t launch_diag_multi(DiagStep const& a, void* r0, void* r1, int64_t n0, int64_t n1, double* acc_base,
+                              int64_t step_acc, unsigned* bar, int spin_limit, cudaStream_t s) {
+#define KPM_DISPATCH(V, e, l) \
+    if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) \
+        return diag_multi_launch<V, e, l>(a, r0, r1, n0, n1, acc_base, step_acc, bar, spin_limit, s);
     KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
     KPM_DIAG_ALT_F32(KPM_DISPATCH) KPM_DIAG_ALT_F64(KPM_DISPATCH) KPM_DIAG_ALT_C64(KPM_DISPATCH)
 #undef KPM_DISPATCH

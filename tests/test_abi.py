@@ -174,7 +174,7 @@ def test_optimized_hamiltonian_disconnected_bit_exact(oracle):
 def test_config_fields_are_checked_on_create():
     """kpm_create rejects launch options outside their ranges before touching the GPU."""
     h = _small_h()
-    for field, bad, msg in (("staging", 5, "staging must be"), ("fuse_steps", 3, "fuse_steps must be"),
+    for field, bad, msg in (("staging", 5, "staging must be"), ("fuse_steps", 4, "fuse_steps must be"),
                             ("precision", 7, "unknown precision mode")):
         cfg = _native.make_config()
         setattr(cfg, field, bad)

@@ -572,3 +572,36 @@ def test_engines_on_two_host_threads_agree_with_one_thread():
     assert not errors, errors
     for i in range(2):
         assert rel_err(out[i], ref[i]) < 1e-12
+
+
+@pytest.mark.parametrize("dtype,nvec,tol", [(np.float64, 8, 1e-10), (np.float32, 64, 1e-5), (np.complex128, 8, 1e-10),
+                                            (np.complex64, 16, 1e-5)])
+def test_all_steps_in_one_launch_match_single_steps_and_oracle(oracle, dtype, nvec, tol):
+    """fuse_steps = 3: every step of the recursion in one cooperative launch with a grid barrier
+    between steps (systems that fit in L2), against one launch per step and the FP64 oracle, on
+    a ragged batch; the complex128 case has a real H stored complex (the real-value path)."""
+    hs = [_disordered_flake(n, 50 + i, np.float64) for i, n in enumerate((3001, 1502, 2203))]
+    hs = [h.astype(dtype) for h in hs]
+    rng = (-9.5, 9.5)
+    M = 258
+    a, b = oracle.scale(*rng)
+    starters = [oracle.random_starters(h.shape[0], nvec, dtype) for h in hs]
+    flat = np.concatenate([st.ravel() for st in starters])
+    out = {}
+    for fuse in (3, 1):
+        batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, fuse_steps=fuse)
+        out[fuse] = batch.engine.moments_diag(M, flat)
+        spl = batch.engine.stats().steps_per_launch
+        assert (spl == M // 2 - 1) == (fuse == 3), spl
+        out[fuse * 10] = batch.engine.moments_diag(M, flat)  # the second call of the same shape
+        batch.close()
+    assert rel_err(out[3], out[1]) < (1e-12 if tol < 1e-9 else 1e-6)
+    for s, h in enumerate(hs):
+        h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
+        r = oracle.optimize(h64, [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(h64.dtype), r["reorder_map"]), M,
+                                  slices=r["slices"])
+        for k in (3, 30, 1):
+            err = rel_err(out[k][s], ref)
+            print("one-launch test %s fuse %d system %d: %.3e" % (np.dtype(dtype).name, k, s, err))
+            assert err <= tol
