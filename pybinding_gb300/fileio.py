@@ -6,8 +6,8 @@ get ``.pbz`` appended on save and are found with it on load
 ``{"version": v, "dict": __dict__}`` (``pybinding/support/pickle.py:77-106``).
 
 Files written by pybinding load here as well: numpy arrays and plain Python data as
-they are, and pybinding's ``results.Series`` as :class:`pybinding_gb300.Series` (same
-attributes: ``variable``, ``data``, ``labels``). Other pybinding classes have no
+they are, and pybinding's ``results.Series``, ``Sweep`` and ``NDSweep`` as this
+package's classes of the same names and attributes. Other pybinding classes have no
 counterpart in this package and raise ``pickle.UnpicklingError`` naming the class.
 """
 from __future__ import annotations
@@ -42,7 +42,9 @@ def save(obj, file):
 
 def _pybinding_classes():
     from .chebyshev import Series
-    return {("pybinding.results", "Series"): Series}
+    from .parallel import NDSweep, Sweep
+    return {("pybinding.results", "Series"): Series, ("pybinding.results", "Sweep"): Sweep,
+            ("pybinding.results", "NDSweep"): NDSweep}
 
 
 class _Unpickler(pickle.Unpickler):

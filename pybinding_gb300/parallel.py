@@ -121,7 +121,24 @@ def parallel_for(factory, make_result=None):
     return make_result(data) if make_result else data
 
 
-class Sweep:
+class _Pickleable:
+    """Pickled state in the layout of pybinding's ``@pickleable`` result classes
+    (``pybinding/support/pickle.py:77-106``), so ``.pbz`` files carry the same state either way."""
+
+    def __getstate__(self):
+        return dict(version=0, dict=self.__dict__)
+
+    def __setstate__(self, state):
+        if "version" not in state:
+            self.__dict__.update(state)
+            return
+        if state["version"] != 0:
+            raise RuntimeError("Can't create class {} v0 from incompatible data v{}".format(
+                type(self), state["version"]))
+        self.__dict__.update(state["dict"])
+
+
+class Sweep(_Pickleable):
     """2D parameter sweep result (``pybinding/results.py:772-800``): ``data[i, j]`` at
     ``x[i]``, ``y[j]``."""
 
@@ -133,7 +150,7 @@ class Sweep:
         self.tags = tags
 
 
-class NDSweep:
+class NDSweep(_Pickleable):
     """N-dimensional sweep result (``pybinding/results.py:1027-1052``)."""
 
     def __init__(self, variables, data, labels=None, tags=None):

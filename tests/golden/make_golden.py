@@ -12,7 +12,9 @@ It writes these files next to this script:
 * ``system_baselines.npz`` -- site positions, sublattice site counts and hopping
   pairs of the reference's graphene system baselines (``tests/baseline_data/shape``
   and ``system``: pickled ``System`` objects, read as data without pybinding).
-* ``pbz/*.pbz`` -- the KPM baseline files themselves, for the ``.pbz`` reader.
+* ``pbz/*.pbz`` -- the KPM baseline files themselves, for the ``.pbz`` reader;
+  ``pbz_sweeps/*.pbz`` -- the reference's sweep baselines (pickled ``Sweep`` and
+  ``NDSweep`` of deferred KPM LDOS), for the sweep tests.
 * ``python_impl_moments.npz`` -- diagonal KPM moments computed by the
   reference's pure-NumPy FP64 implementation (``_PythonImpl`` in
   ``pybinding/chebyshev.py:448-583``) on small Hamiltonians and supplied
@@ -119,11 +121,19 @@ def copy_system_baselines(ref_root):
 
 
 def copy_kpm_pbz(ref_root):
-    """The KPM baseline files themselves (a few hundred bytes each), for the .pbz reader."""
+    """The KPM baseline files themselves (a few hundred bytes each), for the .pbz reader, and
+    the two sweep baselines (pickled ``Sweep`` / ``NDSweep`` of deferred KPM LDOS,
+    tests/test_parallel.py:14-50)."""
     dst = os.path.join(HERE, "pbz")
     os.makedirs(dst, exist_ok=True)
     for f in sorted(glob.glob(os.path.join(ref_root, "tests", "baseline_data", "kpm", "*.pbz"))):
         with open(f, "rb") as src, open(os.path.join(dst, os.path.basename(f)), "wb") as out:
+            out.write(src.read())
+    dst = os.path.join(HERE, "pbz_sweeps")
+    os.makedirs(dst, exist_ok=True)
+    for name in ("sweep.pbz", "ndsweep.pbz"):
+        with open(os.path.join(ref_root, "tests", "baseline_data", "parallel", name), "rb") as src, \
+                open(os.path.join(dst, name), "wb") as out:
             out.write(src.read())
 
 

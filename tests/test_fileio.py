@@ -97,3 +97,25 @@ def test_other_pybinding_classes_are_named_in_the_error(tmp_path):
             pickle.dump(SpatialMap(), f, protocol=4)
     with pytest.raises(pickle.UnpicklingError, match="pybinding.results.SpatialMap"):
         pbg.load(tmp_path / "map.pbz")
+
+
+def test_reads_the_reference_sweep_baselines():
+    """pybinding's pickled Sweep and NDSweep (tests/baseline_data/parallel/*.pbz) load as
+    this package's classes with the reference's attributes, and round-trip."""
+    folder = os.path.join(GOLDEN, "pbz_sweeps")
+    s = pbg.load(os.path.join(folder, "sweep.pbz"))
+    assert isinstance(s, pbg.Sweep)
+    assert s.x.shape == (10,) and s.y.shape == (10,) and s.data.shape == (10, 10)
+    assert s.labels["title"] == "test sweep" and s.labels["x"] == "V (eV)" and s.labels["data"] == "LDOS"
+    nd = pbg.load(os.path.join(folder, "ndsweep.pbz"))
+    assert isinstance(nd, pbg.NDSweep)
+    assert [len(v) for v in nd.variables] == [5, 4, 10] and nd.data.shape == (5, 4, 10)
+    np.testing.assert_array_equal(nd.variables[0], np.linspace(0, 0.1, 5))
+
+
+def test_sweep_results_round_trip(tmp_path):
+    s = pbg.Sweep(np.arange(3.0), np.arange(4.0), np.arange(12.0).reshape(3, 4), labels=dict(x="V"), tags={"a": 1})
+    pbg.save(s, tmp_path / "s")
+    got = pbg.load(tmp_path / "s")
+    assert isinstance(got, pbg.Sweep) and got.labels["x"] == "V" and got.tags == {"a": 1}
+    np.testing.assert_array_equal(got.data, s.data)

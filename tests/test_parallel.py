@@ -158,3 +158,66 @@ def test_batched_ldos_checks_its_sites_before_the_gpu():
     with pytest.raises(RuntimeError, match="LDOS index out of range"):
         batch.engine.calc_ldos_batch([0, 10 ** 6], np.linspace(-1, 1, 5), 0.1)
     batch.close()
+
+
+# the reference's sweep tests (tests/test_parallel.py:14-50): deferred KPM LDOS of graphene
+# hexagons (hexagon_ac(15), 22,686 sites) under constant potentials, Lorentz kernel,
+# broadening 0.15 eV, energies linspace(0, 0.1, 10); compared as the reference does
+# (rtol 1e-3, atol 1e-6)
+def _sweep_baselines():
+    import os
+    from tests.conftest import GOLDEN
+    folder = os.path.join(GOLDEN, "pbz_sweeps")
+    return pbg.load(os.path.join(folder, "sweep.pbz")), pbg.load(os.path.join(folder, "ndsweep.pbz"))
+
+
+def _hexagon_model(*potentials):
+    v, offset = L.hexagon_ac(15)
+    return L.build_honeycomb(v, onsite_modifiers=[L.constant_potential(p) for p in potentials], lattice_offset=offset)
+
+
+def test_oracle_reproduces_the_reference_sweep_baselines(oracle):
+    """The inputs of the reference's sweeps (hexagon_ac with its lattice offset, the potentials,
+    the nearest site of sublattice B) through the oracle's Core::ldos match its baselines."""
+    sweep, ndsweep = _sweep_baselines()
+    energy = np.linspace(0, 0.1, 10)
+    for i, v in enumerate(np.linspace(0, 0.1, 10)):
+        m = _hexagon_model(v)
+        ldos = oracle.core_ldos(m.hamiltonian, [m.system.find_nearest([0, 0], "B")], energy, 0.15, kernel="lorentz")
+        np.testing.assert_allclose(ldos[:, 0], sweep.data[i], rtol=1e-3, atol=1e-6)
+    v1s, v2s, _ = ndsweep.variables
+    for i, j in ((0, 0), (4, 3), (1, 2)):
+        m = _hexagon_model(v1s[i], v2s[j])
+        ldos = oracle.core_ldos(m.hamiltonian, [m.system.find_nearest([0, 0])], energy, 0.15, kernel="lorentz")
+        np.testing.assert_allclose(ldos[:, 0], ndsweep.data[i, j], rtol=1e-3, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_sweep_matches_the_reference_sweep_baseline():
+    expected, _ = _sweep_baselines()
+
+    @pbg.parallelize(v=np.linspace(0, 0.1, 10))
+    def factory(v, energy=np.linspace(0, 0.1, 10)):
+        kpm = pbg.kpm(_hexagon_model(v), kernel=pbg.lorentz_kernel())
+        return kpm.deferred_ldos(energy, broadening=0.15, position=[0, 0], sublattice="B")
+
+    labels = dict(title="test sweep", x="V (eV)", y="E (eV)", data="LDOS")
+    result = pbg.sweep(factory, labels=labels)
+    np.testing.assert_allclose(result.x, expected.x)
+    np.testing.assert_allclose(result.y, expected.y)
+    np.testing.assert_allclose(result.data, expected.data, rtol=1e-3, atol=1e-6)
+    assert result.labels == expected.labels
+
+
+@pytest.mark.gpu
+def test_ndsweep_matches_the_reference_ndsweep_baseline():
+    _, expected = _sweep_baselines()
+
+    @pbg.parallelize(v1=np.linspace(0, 0.1, 5), v2=np.linspace(-0.2, 0.2, 4))
+    def factory(v1, v2, energy=np.linspace(0, 0.1, 10)):
+        kpm = pbg.kpm(_hexagon_model(v1, v2), kernel=pbg.lorentz_kernel())
+        return kpm.deferred_ldos(energy, broadening=0.15, position=[0, 0])
+
+    result = pbg.ndsweep(factory)
+    assert result.data.shape == expected.data.shape
+    np.testing.assert_allclose(result.data, expected.data, rtol=1e-3, atol=1e-6)
