@@ -208,3 +208,41 @@ def test_gpu_built_model_runs_the_same_kpm():
     # the blocks add their moment partials with FP64 atomics in no fixed order
     np.testing.assert_allclose(kpm(got).calc_dos(e, 0.1, num_random=2).data,
                                kpm(ref).calc_dos(e, 0.1, num_random=2).data, rtol=1e-9)
+
+
+def _mass_hexagon():
+    v, offset = L.hexagon_ac(10)
+    return L.build_honeycomb(v, onsite_modifiers=[L.mass_term(1)], lattice_offset=offset)
+
+
+def test_mass_term_ldos_is_sublattice_antisymmetric_in_the_oracle(oracle):
+    """The inputs of the reference's test_ldos_sublattice (tests/test_kpm.py:117-123): with a
+    mass term the A and B LDOS at the centre mirror each other in energy (oracle, CPU)."""
+    m = _mass_hexagon()
+    e = np.linspace(-5, 5, 50)
+    a, b = (oracle.core_ldos(m.hamiltonian, [m.system.find_nearest([0, 0], sub)], e, 0.1)[:, 0] for sub in "AB")
+    np.testing.assert_allclose(a, b[::-1], rtol=1e-3, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_ldos_sublattice():
+    """tests/test_kpm.py:117-123 of the reference through the pb.kpm-compatible API."""
+    from pybinding_gb300 import kpm
+    k = kpm(_mass_hexagon(), silent=True)
+    a, b = (k.calc_ldos(np.linspace(-5, 5, 50), 0.1, [0, 0], sub) for sub in ("A", "B"))
+    np.testing.assert_allclose(a.data, b.data[::-1], rtol=1e-3, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_kpm_reuse():
+    """tests/test_kpm.py:104-114 of the reference: one KPM object used for several
+    calculations gives what fresh objects give."""
+    from pybinding_gb300 import kpm
+    v, offset = L.hexagon_ac(10)
+    model = L.build_honeycomb(v, lattice_offset=offset)
+    k = kpm(model, silent=True)
+    energy = np.linspace(-5, 5, 50)
+    for position in [0, 0], [6, 0]:
+        actual = k.calc_ldos(energy, 0.1, position)
+        expected = kpm(model).calc_ldos(energy, 0.1, position)
+        np.testing.assert_allclose(actual.data, expected.data, rtol=1e-3, atol=1e-6)
