@@ -46,6 +46,12 @@ METRIC = "KPM Gnnz*vec/s (batched FP32 recursion, FP64 moment sums; moment err v
 UNIT = "Gnnz*vec/s"
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one diag_step_kernel<float,4,16> launch
+# (64 FP32 vectors per row) on the 4-flake case of the same workload: 1,070,628,096 bytes over
+# 1,362,158 rows (profiles/diag_step_dos_batch.md)
+DIAG_STEP_DRAM_BYTES_PER_ROW = 1070628096.0 / 1362158
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -314,13 +320,9 @@ def run_gpu(args, rank, world, local_rank):
     except (OSError, ValueError):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "diag_step_traffic.json")))
-        if prof.get("steps_per_launch", 1) == fuse:
-            traffic = prof.get("dram_bytes_per_launch_scaled_to_bench")
-    except (OSError, ValueError):
-        pass
+    # DRAM traffic per launch from an ncu capture of the same kernel and lane mapping, scaled
+    # to this workload's rows (traffic grows with rows x vectors)
+    traffic = DIAG_STEP_DRAM_BYTES_PER_ROW * nrows if (fuse == 1 and lane_map == (4, 16) and R == 64) else None
 
     e2e = None
     if not args.no_e2e:
