@@ -48,7 +48,7 @@ UNIT = "Gnnz*vec/s"
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one diag_step_kernel<float,4,16> launch
 # (64 FP32 vectors per row) on the 4-flake case of the same workload: 1,070,628,096 bytes over
-# 1,362,158 rows (profiles/diag_step_dos_batch.md)
+# 1,362,158 rows (ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum, one launch)
 DIAG_STEP_DRAM_BYTES_PER_ROW = 1070628096.0 / 1362158
 
 
@@ -76,10 +76,10 @@ def parse():
     p.add_argument("--cube-vectors", type=int, default=256, help="vectors of the 3D Anderson workload")
     p.add_argument("--cube-moments", type=int, default=8192, help="moments of the 3D Anderson workload")
     p.add_argument("--ldos-sites", type=int, default=4096, help="LDOS sites of the 3D Anderson workload (0: none)")
-    p.add_argument("--staging", default="auto", choices=["auto", "registers", "tma", "async", "gather"],
-                   help="recursion kernel operands (auto = chosen by timing; pin it under a profiler)")
-    p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2, 3],
-                   help="steps per launch (0 = chosen by timing, 3 = all steps in one launch)")
+    p.add_argument("--staging", default="auto", choices=["auto", "registers", "prefetch"],
+                   help="diagonal step's matrix entries: per-row loads or staged a chunk ahead (auto = by timing)")
+    p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2],
+                   help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
     p.add_argument("--workload", default="dos_batch",
                    choices=["dos_batch", "dos_c128_60k", "conductivity", "adjoint", "anderson3d", "lattice", "sweep"])
@@ -177,32 +177,51 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def cpu_reference(hs, args, threads, target_seconds, seed):
-    """Time the oracle's multithreaded DefaultCompute restatement on one flake of the workload."""
-    from oracle import oracle as O
-    # the flake closest to the mean size, its own Lanczos-free bounds (the bench's scale is per flake)
-    sizes = np.array([h.shape[0] for h in hs])
-    h = hs[int(np.argmin(np.abs(sizes - sizes.mean())))].astype(np.float32)
-    a, b = O.scale(-9.0, 9.0)
-    r = O.optimize(h, [0], [0], a, b)
-    n = h.shape[0]
-    k = 8
-    R = k * threads
-    rng = np.random.default_rng(seed)
-    st = np.stack([rademacher(rng, n) for _ in range(R)])
-    st = O.reorder_vector(st, r["reorder_map"])
-    nnz = h.nnz
-    # calibrate: a short run, then size M for about target_seconds
-    M0 = 34
-    _, sec0 = O.bench_diag(r["h2"], r["slices"], st, M0, k, threads)
-    rate = (M0 / 2) * nnz * R / sec0
-    steps = max(8, int(target_seconds * rate / (nnz * R)))
-    M = O.round_num_moments(2 * steps)
-    _, sec = O.bench_diag(r["h2"], r["slices"], st, M, k, threads)
-    work = (M / 2) * nnz * R
-    return dict(value=work / sec / 1e9, seconds=sec, M=M, R=R, n=n, nnz=nnz,
-                sample="one %d-site flake of the workload (nnz %d), %d Rademacher vectors in %d-vector batches, "
-                       "%d moments, ELL interleaved, %d threads" % (n, nnz, R, k, M, threads))
+class CpuWorkload:
+    """The timed CPU baseline over the whole batched workload: the oracle's restatement of the
+    reference's DefaultCompute DOS path (ELL, interleaved recursion, 8-vector float batches --
+    the reference's float SIMD batch on AVX, kpm/default/Compute.cpp:52-88 with
+    support/simd.hpp:35-43), built -O3 with FMA contraction (and -mcpu=native on aarch64), every
+    (flake, batch) pair on one pool of all host threads. Each sample runs every flake with all its
+    vectors for a moment count sized to the time target: the metric is a rate, and the rate of a
+    step does not depend on how many steps run."""
+
+    K = 8
+
+    def __init__(self, hs, vectors, seed, threads):
+        from oracle import oracle as O
+        self.O = O
+        self.threads = threads
+        self.vectors = vectors
+        a, b = O.scale(-9.0, 9.0)  # timing only: one range for all flakes
+        rng = np.random.default_rng(seed)
+        self.systems = []
+        self.nnz = 0
+        for h in hs:
+            r = O.optimize(h.astype(np.float32), [0], [0], a, b)
+            st = np.stack([rademacher(rng, h.shape[0]) for _ in range(vectors)])
+            self.systems.append((r["h2"], r["slices"], O.reorder_vector(st, r["reorder_map"])))
+            self.nnz += int(h.nnz)
+        self.rate = None
+
+    def sample(self, target_seconds):
+        """One timed sample of about target_seconds; returns (Gnnz*vec/s, seconds, M)."""
+        O = self.O
+        if self.rate is None:  # calibrate on 8 steps
+            _, sec0 = O.bench_diag_multi(self.systems, 18, self.K, self.threads)
+            self.rate = 9 * self.nnz * self.vectors / sec0
+        steps = max(8, int(target_seconds * self.rate / (self.nnz * self.vectors)))
+        M = O.round_num_moments(2 * steps)
+        _, sec = O.bench_diag_multi(self.systems, M, self.K, self.threads)
+        work = (M / 2) * self.nnz * self.vectors
+        self.rate = work / sec
+        return work / sec / 1e9, sec, M
+
+    def describe(self, M):
+        return ("all %d flakes of the workload (nnz %d), %d Rademacher vectors each in %d-vector float batches, "
+                "%d moments per sample, ELL interleaved, %d threads, timed build -O3 %s" % (
+                    len(self.systems), self.nnz, self.vectors, self.K, M, self.threads,
+                    " ".join(self.O._fast_flags()[1:])))
 
 
 def run_reference(args, rank, world):
@@ -210,21 +229,36 @@ def run_reference(args, rank, world):
         return
     hs, _, _ = build_workload(args, 0)
     threads = os.cpu_count() or 1
+    cpu = CpuWorkload(hs, args.vectors, args.seed, threads)
     vals = []
     last = None
     for i in range(args.warmup + args.steps):
-        res = cpu_reference(hs, args, threads, args.cpu_seconds / 2, args.seed + i)
+        v, sec, M = cpu.sample(args.cpu_seconds / 2)
         if i >= args.warmup:
-            vals.append(res["value"])
-            last = res
+            vals.append(v)
+            last = (sec, M)
     v = float(np.median(vals))
+    cfg = workload_config(args, hs)
+    cfg["sample_moments"] = int(last[1])
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": last["seconds"] * 1e3, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": last[0] * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-           "config": workload_config(args, hs),
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": last["sample"]},
+           "config": cfg,
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu.describe(last[1])},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def oracle_check(h, a, b, starters, M, got64, got32):
+    """The FP64 oracle's moments of two vectors of one flake (the CPU leg's checker): errors of
+    the engine's FP64 and FP32 moments of those vectors, relative to max |mu|."""
+    from oracle import oracle as O
+    r = O.optimize(h.astype(np.float64), [0], [0], a, b)
+    ref = O.moments_diag(r["h2"], O.reorder_vector(starters.astype(np.float64), r["reorder_map"]), M,
+                         slices=r["slices"])
+    scale = np.max(np.abs(ref))
+    return {"fp64_vs_oracle": float(np.max(np.abs(got64 - ref)) / scale),
+            "fp32_vs_oracle": float(np.max(np.abs(got32 - ref)) / scale)}
 
 
 def workload_config(args, hs):
@@ -304,7 +338,7 @@ def run_gpu(args, rank, world, local_rank):
     fuse = int(eng.stats().steps_per_launch)
     lane_map = (int(eng.stats().elems_per_lane), int(eng.stats().lanes_per_row))
     tiling = {"tile_rows": int(eng.stats().tile_rows), "unroll": int(eng.stats().unroll),
-              "staged_rows": int(eng.stats().staged_rows), "gather_rows": int(eng.stats().gather_rows)}
+              "prefetch": int(eng.stats().prefetch)}
     launches = 1 + (M // 2 - 1) // fuse  # init + recursion launches
     avg_launch = rec / launches
     nrows = rows
@@ -347,24 +381,70 @@ def run_gpu(args, rank, world, local_rank):
         e2e = {"value": rate_e / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(starters.nbytes), "d2h_bytes_per_step": int(nsys * M * 16)}
 
+    # the same workload in the plain FP64 recursion (the other half of the metric): timed on the
+    # device like `value`, then its moments are the error reference of the FP32 ones (the two
+    # engines' Lanczos bounds are the same bits: its sums run in a fixed order)
     err = None
+    fp64 = None
     if not args.no_error:
         m32 = eng.moments_diag(args.moments, None, average=False, on_device_ptr=d_st.data_ptr(), num_vectors=R)
+        bounds32 = [eng.energy_bounds(s) for s in range(nsys)]
+        scales = [eng.scaling_factors(s) for s in range(nsys)]
         eng.close()
-        cfg64 = _native.make_config(precision="fp64")
-        e64 = _native.Engine(h, cfg64, system_offsets=offsets)
-        m64 = e64.moments_diag(args.moments, None, average=False, on_device_ptr=d_st.data_ptr(), num_vectors=R)
+        e64 = _native.Engine(h, _native.make_config(precision="fp64"), system_offsets=offsets)
+        same_bounds = all(e64.energy_bounds(s) == bounds32[s] for s in range(nsys))
+        s64 = torch.cuda.ExternalStream(e64.stream())
+
+        def step64():
+            return e64.moments_diag(args.moments, None, average=False, on_device_ptr=d_st.data_ptr(), num_vectors=R)
+
+        m64 = step64()  # warm (tuning) + the reference moments
+        n64 = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(s64)
+        rec64 = []
+        for _ in range(n64):
+            step64()
+            rec64.append(e64.stats().moments_time)
+        g1.record(s64)
+        torch.cuda.synchronize()
+        t64 = g0.elapsed_time(g1) * 1e-3 / n64
+        st64 = e64.stats()
+        fuse64 = int(st64.steps_per_launch)
+        launches64 = 1 + (M // 2 - 1) // fuse64
+        alg64 = nnz * (8 + 4) + 4 * (nrows + 1) + (3 if fuse64 == 1 else 4) * nrows * R * 8
+        avg64 = float(np.median(rec64)) / launches64
+        fp64 = {"value": work / t64 / 1e9, "unit": UNIT, "ms_per_step": t64 * 1e3, "timed_steps": n64,
+                "kernel": "%s<double,%d,%d>" % ("diag_step_kernel" if fuse64 == 1 else "diag_pair_kernel",
+                                                 int(st64.elems_per_lane), int(st64.lanes_per_row)),
+                "roofline": {"bound": "hbm", "achieved": alg64 / avg64 / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": alg64 / avg64 / 1e9 / peak, "alg_bytes_per_launch": alg64,
+                             "avg_launch_ms": avg64 * 1e3}}
         e64.close()
         # per-vector moments, and the stochastic-trace moments (average over the vectors of a
         # flake, as the reference's BatchAccumulator returns them), each relative to its max |mu|
         err = {"per_vector_max": float(np.max(np.abs(m32 - m64)) / np.max(np.abs(m64))),
-               "vector_averaged_max": float(np.max(np.abs(m32.mean(1) - m64.mean(1))) / np.max(np.abs(m64.mean(1))))}
+               "vector_averaged_max": float(np.max(np.abs(m32.mean(1) - m64.mean(1))) / np.max(np.abs(m64.mean(1)))),
+               "reference": "FP64 recursion of the same workload (GPU), identical Lanczos bounds: %s" % same_bounds}
     else:
         eng.close()
 
     cpu = None
     if rank == 0:
-        cpu = cpu_reference(hs, args, os.cpu_count() or 1, args.cpu_seconds, args.seed)
+        # CPU leg: the timed CPU baseline on the whole workload, and the FP64 oracle as the checker of
+        # the largest flake's first two vectors (the FP64 GPU run above is pinned to it there)
+        cpu_run = CpuWorkload(hs, R, args.seed, os.cpu_count() or 1)
+        v, sec, Ms = cpu_run.sample(args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": cpu_run.describe(Ms)}
+        del cpu_run
+        if err is not None:
+            big = int(np.argmax([x.shape[0] for x in hs]))
+            a, b = scales[big]
+            st_big = starters[R * int(offsets[big]):R * int(offsets[big + 1])].reshape(R, -1)[:2]
+            chk = oracle_check(hs[big].astype(np.float32), a, b, st_big, M, m64[big, :2], m32[big, :2])
+            err.update({"oracle_flake_sites": int(hs[big].shape[0]), "oracle_vectors": 2, **chk})
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -374,15 +454,13 @@ def run_gpu(args, rank, world, local_rank):
                "moment_error_vs_fp64": err,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
-                            "kernel": "%s<float,%d,%d>" % (("diag_gather_kernel" if tiling["gather_rows"] > 0 else
-                                                            "diag_tma_kernel" if tiling["staged_rows"] > 0 else
-                                                            "diag_async_kernel" if tiling["staged_rows"] < 0 else
+                            "kernel": "%s<float,%d,%d>" % (("diag_pf_kernel" if tiling["prefetch"] else
                                                             "diag_step_kernel") if fuse == 1 else "diag_pair_kernel",
                                                            lane_map[0], lane_map[1]),
                             "steps_per_launch": fuse, "tiling": tiling, "alg_bytes_per_launch": alg_bytes,
                             "avg_launch_ms": avg_launch * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-               "cpu_baseline": {"value": cpu["value"], "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": cpu["sample"]},
+               "cpu_baseline": cpu,
+               "fp64": fp64,
                "e2e": e2e,
                "clocks": clk,
                "gpu_launches": int(args.steps * (launches + 3))}
@@ -468,11 +546,15 @@ def workload_dos_c128_60k(args, stream_of):
         rng = np.random.default_rng(1)
         st0 = np.exp(2j * np.pi * rng.random((8, h.shape[0])))
         st0 = O.reorder_vector(st0, r["reorder_map"])
-        Ms = 130
-        _, sec = O.bench_diag(r["h2"], r["slices"], st0, Ms, 8, 1)
-        cpu = {"value": (Ms / 2) * h.nnz * 8 / sec / 1e9, "unit": "Gnnz*vec/s", "cores": 1, "kind": "port",
-               "sample": "the same flake and 8 complex128 vectors, %d moments, 1 thread (the reference's DOS "
-                         "runs one batch of 8 vectors on one thread)" % Ms}
+        Ms = 514
+        threads = os.cpu_count() or 1
+        _, sec = O.bench_diag(r["h2"], r["slices"], st0, Ms, 2, threads)
+        cpu = {"value": (Ms / 2) * h.nnz * 8 / sec / 1e9, "unit": "Gnnz*vec/s", "cores": min(threads, 4),
+               "kind": "port",
+               "sample": "the same flake and 8 complex128 vectors in 2-vector batches (the reference's complex128 "
+                         "SIMD batch, support/simd.hpp:35-43), %d moments, a pool of %d threads of which the 4 "
+                         "batches keep 4 busy (kpm/default/Compute.cpp:52-88), timed build -O3 %s" % (
+                             Ms, threads, " ".join(O._fast_flags()[1:]))}
     _line(args, "KPM DOS (complex128) Gnnz*vec/s", work / (t / args.steps) / 1e9, "Gnnz*vec/s", True,
           t / args.steps,
           {"workload": "graphene DOS: 60k sites complex128, 8 random-phase vectors, 2048 moments, 1000 energies",
@@ -648,9 +730,8 @@ def workload_anderson3d(args, stream_of):
           "f32",
           roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",
                     "frac": alg / avg / 1e9 / peak, "traffic": None, "steps_per_launch": fuse,
-                    "kernel": (("diag_gather_kernel" if s.gather_rows > 0 else
-                                "diag_tma_kernel" if s.staged_rows > 0 else "diag_async_kernel" if s.staged_rows < 0
-                                else "diag_step_kernel") if fuse == 1 else "diag_pair_kernel"),
+                    "kernel": ("diag_pf_kernel" if s.prefetch else "diag_step_kernel") if fuse == 1
+                              else "diag_pair_kernel",
                     "lane_map": [int(s.elems_per_lane), int(s.lanes_per_row)], "tile_rows": int(s.tile_rows),
                     "unroll": int(s.unroll),
                     "alg_bytes_per_launch": alg, "avg_launch_ms": avg * 1e3,

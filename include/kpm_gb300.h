@@ -64,13 +64,12 @@ typedef struct kpm_config {
     int32_t precision;        /* KPM_PREC_* */
     int32_t batch_width;      /* vectors per recursion block (upper bound); 0 = 256-byte rows */
     int32_t tile_rows;        /* rows per thread block tile; 0 = autotuned on the first call */
-    int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, 3 = all steps in one cooperative
-                                 launch (systems whose vectors fit in L2; else 1), or 0 = chosen by timing */
-    int32_t staging;          /* diagonal step operands: 0 = chosen by timing, 1 = register loads,
-                                 2 = TMA bulk copies into shared memory, 3 = per-thread cp.async
-                                 pipeline, 4 = TMA bulk copies plus TMA gathers of the neighbour rows
-                                 (2, 3 and 4: full-system recursions of 16-byte-lane shapes, 3 also
-                                 rows of <= 4 entries, 4 FP32 only; others use register loads) */
+    int32_t fuse_steps;       /* Chebyshev steps per launch: 1, 2, or 0 = chosen by timing */
+    int32_t staging;          /* diagonal step's matrix entries: 0 = chosen by timing, 1 = loaded per
+                                 row, 2 = staged in shared memory a chunk of rows ahead by cp.async */
+    int32_t num_threads;      /* host threads for the engine's setup work (reorder, starters, Lanczos
+                                 checks); 0 = all cores. DefaultCompute's num_threads
+                                 (cppmodule/src/kpm.cpp:14); the recursion itself runs on the GPU */
 } kpm_config;
 
 /* Stats of the last calculation: kpm::Stats (kpm/Stats.hpp:19-45). */
@@ -93,13 +92,14 @@ typedef struct kpm_stats {
     double gemm_time;         /* seconds: device time of the conductivity's moments GEMM (0 otherwise) */
     int32_t elems_per_lane;   /* recursion kernel lane mapping used last: vector elements per lane */
     int32_t lanes_per_row;    /*   and lanes per matrix row (their product = vectors per block) */
-    int32_t staged_rows;      /*   0 = register loads, > 0 = TMA-staged tiles of this many rows,
-                                   < 0 = cp.async-pipelined tiles of -staged_rows rows */
+    int32_t staged_rows;      /*   always 0 (register loads) */
     int32_t tile_rows;        /*   rows per tile */
     int32_t unroll;           /*   rows per thread per iteration */
     double upload_time;       /* seconds (device): starter upload and scatter of the last diagonal call */
     double call_time;         /* seconds (host wall clock) of the last call, entry to return */
-    int32_t gather_rows;      /* > 0: the step gathered x rows with TMA tile::gather4, tiles of this many rows */
+    int32_t gather_rows;      /* always 0 (kept for layout compatibility) */
+    int32_t prefetch;         /* > 0: the diagonal step staged each warp's ELL entries in shared memory
+                                 a chunk ahead (diag_pf_kernel); 3 or 4 = registers held to that many blocks per SM */
 } kpm_stats;
 
 typedef struct kpm_engine kpm_engine;
@@ -270,6 +270,15 @@ int kpm_optimized_hamiltonian(kpm_engine* engine, const int32_t* src, int64_t n_
                               void* out_values, int64_t* out_nnz, int32_t* out_map, int32_t* out_slices,
                               int64_t* out_num_slices, int32_t* out_src, int32_t* out_dest, int64_t* offsets);
 
+/* Progress reports of the stochastic DOS (kpm_calc_dos): the progress_callback of
+ * cppmodule/src/kpm.cpp:14,25,35 as kpm::DefaultCompute calls it (kpm/default/Compute.cpp:64-87,
+ * 133-144): fn(-1, total) when the moments start, fn(delta, total) as parts of the recursion
+ * complete (the deltas add up to total = num_random vectors), fn(total, total) at the end.
+ * Called on the thread that called kpm_calc_dos, between waits on the GPU (which keeps running).
+ * fn = NULL turns reporting off. */
+typedef void (*kpm_progress_fn)(int64_t delta, int64_t total, void* user);
+int kpm_set_progress_callback(kpm_engine* engine, kpm_progress_fn fn, void* user);
+
 /* The engine's CUDA stream (a cudaStream_t) for interop: callers may record
  * events on it or order their own work after the engine's. No reference
  * counterpart (the reference has no device). Initialises the device. */
@@ -293,7 +302,10 @@ int kpm_get_stream(kpm_engine* engine, void** stream);
  * num_moments/2 * K * 2 (real) or 3 (complex) doubles) are rejected with
  * KPM_ERR_VALUE and a message. The first call on each device looks up that
  * array's device address with the device current; make that first call
- * before any stream capture. Every call shares the array, so calls that
+ * before any stream capture. The address is kept for the life of the process:
+ * after cudaDeviceReset (or anything else that destroys the device's primary
+ * context) it is stale, and this entry point must not be called again. The
+ * stream must belong to the current device (checked: KPM_ERR_VALUE). Every call shares the array, so calls that
  * overlap on the GPU race; the call clears what must start at zero. Work is
  * queued on `stream` (a cudaStream_t; NULL = default stream) and the call
  * returns without waiting for it.

@@ -995,8 +995,12 @@ struct Core {
 // ELL matrix, interleaved diagonal recursion, k vectors per batch stored
 // row-major (vectors interleaved per row, like Eigen's row-major batch),
 // one std::thread per core pulling batches from a shared counter.
-template<class T>
-void batch_interleaved(Ell<T> const& e, SliceMap const& map, T const* r0_in, int64_t k, int64_t M, T* mu_out) {
+// KC > 0 fixes the batch width at compile time (the reference's batches are SIMD-register
+// wide, support/simd.hpp:35-43), so that the per-row loops over the batch vectorise fully.
+template<class T, int KC>
+void batch_interleaved(Ell<T> const& e, SliceMap const& map, T const* r0_in, int64_t k_runtime, int64_t M,
+                       T* mu_out) {
+    int64_t const k = KC > 0 ? KC : k_runtime;
     auto const n = e.rows;
     Vec<T> r0(r0_in, r0_in + n * k), r1(n * k, T{0});
     for (int64_t c = 0; c < e.width; ++c)
@@ -1055,6 +1059,18 @@ void batch_interleaved(Ell<T> const& e, SliceMap const& map, T const* r0_in, int
                 mu_out[j * M + 2 * nn + 1] = T(2) * m5[j] - m1[j];
             }
         }
+    }
+}
+
+template<class T>
+void batch_any_width(Ell<T> const& e, SliceMap const& map, T const* r0, int64_t k, int64_t M, T* mu_out) {
+    switch (k) {
+        case 1: batch_interleaved<T, 1>(e, map, r0, k, M, mu_out); break;
+        case 2: batch_interleaved<T, 2>(e, map, r0, k, M, mu_out); break;
+        case 4: batch_interleaved<T, 4>(e, map, r0, k, M, mu_out); break;
+        case 8: batch_interleaved<T, 8>(e, map, r0, k, M, mu_out); break;
+        case 16: batch_interleaved<T, 16>(e, map, r0, k, M, mu_out); break;
+        default: batch_interleaved<T, 0>(e, map, r0, k, M, mu_out); break;
     }
 }
 
@@ -1473,7 +1489,7 @@ template<class T> struct BenchF {
                 std::fill(block.begin(), block.end(), T{0});
                 for (int64_t j = 0; j < kk; ++j)
                     for (int64_t i = 0; i < n; ++i) block[i * k + j] = rr[(c0 + j) * n + i];
-                batch_interleaved(ell, oh.map, block.data(), k, M, mu.data());
+                batch_any_width(ell, oh.map, block.data(), k, M, mu.data());
                 for (int64_t j = 0; j < kk; ++j)
                     std::copy(mu.begin() + j * M, mu.begin() + (j + 1) * M, out + (c0 + j) * M);
             }
@@ -1484,6 +1500,60 @@ template<class T> struct BenchF {
         *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
 };
+// The same over several independent systems at once (e.g. the flakes of a disorder
+// ensemble, each with its own optimized matrix): every (system, batch) pair goes to one
+// shared pool of `threads` workers, as if each system's DOS ran concurrently on one thread
+// pool. Per system s: n[s] rows, CSR ip[s]/ix[s]/v[s], SliceMap slices[s] (nslices[s]),
+// starters r0[s] (R x n[s]). mu_out: nsys x R x M. Returns seconds in *seconds.
+template<class T> struct BenchMultiF {
+    static void run(int32_t nsys, int64_t const* n, void* const* ip, void* const* ix, void* const* v,
+                    void* const* slices, int64_t const* nslices, void* const* r0, int64_t R, int64_t M, int64_t k,
+                    int32_t threads, void* mu_out, double* seconds) {
+        std::vector<Ell<T>> ells;
+        std::vector<SliceMap> maps(nsys);
+        ells.reserve(nsys);
+        for (int32_t s = 0; s < nsys; ++s) {
+            ells.push_back(csr_to_ell(csr_from<T>(n[s], static_cast<int32_t const*>(ip[s]),
+                                                  static_cast<int32_t const*>(ix[s]), v[s])));
+            auto const* sl = static_cast<int32_t const*>(slices[s]);
+            maps[s].data.assign(sl, sl + nslices[s]);
+        }
+        auto out = static_cast<T*>(mu_out);
+        int64_t const nbatch = (R + k - 1) / k;
+        std::atomic<int64_t> next{0};
+        auto t0 = std::chrono::steady_clock::now();
+        auto worker = [&] {
+            Vec<T> block, mu(k * M);
+            for (;;) {
+                auto const item = next.fetch_add(1);
+                if (item >= nbatch * nsys) break;
+                auto const s = item / nbatch, b = item % nbatch;
+                auto const ns = n[s];
+                auto const* rr = static_cast<T const*>(r0[s]);
+                auto const c0 = b * k;
+                auto const kk = std::min<int64_t>(k, R - c0);
+                block.assign(ns * k, T{0});
+                for (int64_t j = 0; j < kk; ++j)
+                    for (int64_t i = 0; i < ns; ++i) block[i * k + j] = rr[(c0 + j) * ns + i];
+                batch_any_width(ells[s], maps[s], block.data(), k, M, mu.data());
+                for (int64_t j = 0; j < kk; ++j)
+                    std::copy(mu.begin() + j * M, mu.begin() + (j + 1) * M, out + (s * R + c0 + j) * M);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+        for (auto& t : pool) t.join();
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+extern "C" int orc_bench_diag_multi(int32_t dtype, int32_t nsys, int64_t const* n, void* const* ip, void* const* ix,
+                                    void* const* v, void* const* slices, int64_t const* nslices, void* const* r0,
+                                    int64_t R, int64_t M, int64_t k, int32_t threads, void* mu_out, double* seconds) {
+    return guarded([&] {
+        dispatch<BenchMultiF>(dtype, nsys, n, ip, ix, v, slices, nslices, r0, R, M, k, threads, mu_out, seconds);
+    });
+}
+
 extern "C" int orc_bench_diag(int32_t dtype, int64_t n, int32_t const* ip, int32_t const* ix, void const* v, int32_t const* slices,
                    int64_t nslices, void const* r0, int64_t R, int64_t M, int64_t k, int32_t threads, void* mu_out,
                    double* seconds) {

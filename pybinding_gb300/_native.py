@@ -22,7 +22,10 @@ SCALAR_CODE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1,
                np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
 KERNEL_CODE = {"jackson": 0, "lorentz": 1, "dirichlet": 2}
 PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2}
-STAGING_CODE = {"auto": 0, "registers": 1, "tma": 2, "async": 3, "gather": 4}
+STAGING_CODE = {"auto": 0, "registers": 1, "prefetch": 2}
+
+
+PROGRESS_FN = C.CFUNCTYPE(None, C.c_int64, C.c_int64, C.c_void_p)
 
 
 class Config(C.Structure):
@@ -31,7 +34,7 @@ class Config(C.Structure):
                 ("kernel_param", C.c_double), ("matrix_format", C.c_int32), ("optimal_size", C.c_int32),
                 ("interleaved", C.c_int32), ("lanczos_precision", C.c_double), ("precision", C.c_int32),
                 ("batch_width", C.c_int32), ("tile_rows", C.c_int32), ("fuse_steps", C.c_int32),
-                ("staging", C.c_int32)]
+                ("staging", C.c_int32), ("num_threads", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -43,7 +46,7 @@ class Stats(C.Structure):
                 ("eps", C.c_double), ("steps_per_launch", C.c_int32), ("gemm_time", C.c_double),
                 ("elems_per_lane", C.c_int32), ("lanes_per_row", C.c_int32), ("staged_rows", C.c_int32),
                 ("tile_rows", C.c_int32), ("unroll", C.c_int32), ("upload_time", C.c_double),
-                ("call_time", C.c_double), ("gather_rows", C.c_int32)]
+                ("call_time", C.c_double), ("gather_rows", C.c_int32), ("prefetch", C.c_int32)]
 
 
 class Honeycomb(C.Structure):
@@ -78,6 +81,7 @@ SIGNATURES = {
     "kpm_report": (_I32, [_P, _I32, _P, _I64]),
     "kpm_optimized_hamiltonian": (_I32, [_P, _P, _I64, _P, _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "kpm_get_stream": (_I32, [_P, _P]),
+    "kpm_set_progress_callback": (_I32, [_P, PROGRESS_FN, _P]),
     "kpm_moments_diag_noalloc": (_I32, [_I32, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P, _P]),
     "kpm_damping_coefficients": (_I32, [_I32, _D, _I64, _P]),
     "kpm_required_num_moments": (_I64, [_I32, _D, _D]),
@@ -132,7 +136,7 @@ def check(rc):
 
 def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, matrix_format="ELL",
                 optimal_size=True, interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0,
-                tile_rows=0, fuse_steps=0, staging="auto"):
+                tile_rows=0, fuse_steps=0, staging="auto", num_threads=0):
     c = Config()
     lib().kpm_config_default(C.byref(c))
     c.min_energy, c.max_energy = float(energy_range[0]), float(energy_range[1])
@@ -147,6 +151,7 @@ def make_config(energy_range=(0.0, 0.0), kernel="jackson", kernel_param=4.0, mat
     c.tile_rows = int(tile_rows)
     c.fuse_steps = int(fuse_steps)
     c.staging = STAGING_CODE[staging]
+    c.num_threads = 0 if num_threads in (None, "auto") else int(num_threads)
     return c
 
 
@@ -362,6 +367,16 @@ class Engine:
         check(lib().kpm_adjoint_diag(self._h, num_moments, nvec, ptr(keep), ptr(w), int(checkpoint), ptr(gv), ptr(go),
                                      C.byref(nout)))
         return gv, go
+
+    def set_progress_callback(self, callback):
+        """``callback(delta, total)`` during calc_dos (kpm_set_progress_callback); None turns it off."""
+        if callback is None:
+            self._progress = None
+            check(lib().kpm_set_progress_callback(self._h, None, None))
+            return
+        fn = PROGRESS_FN(lambda delta, total, user: callback(int(delta), int(total)))
+        self._progress = fn  # kept alive as long as the engine may call it
+        check(lib().kpm_set_progress_callback(self._h, fn, None))
 
     def stream(self):
         """The engine's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""

@@ -27,7 +27,7 @@ import math
 import numpy as np
 import scipy.sparse as sp
 
-from . import _native
+from . import _binding
 
 __all__ = ["DiagonalMoments", "dos", "moments_weights"]
 
@@ -63,14 +63,14 @@ class DiagonalMoments:
         self.indptr = h.indptr.astype(np.int32)
         self.indices = h.indices.astype(np.int32)
         self.rows = h.shape[0]
-        self.num_moments = _native.round_num_moments(int(num_moments))
+        self.num_moments = _binding.round_num_moments(int(num_moments))
         self.dtype = np.dtype(np.float64 if precision == "fp64" else np.float32)
         st = np.atleast_2d(np.asarray(starters))
         if st.shape[1] != self.rows:
             raise ValueError("starters must have shape (num_vectors, %d)" % self.rows)
         self.starters = np.ascontiguousarray(st, self.dtype)
         self.checkpoint = int(checkpoint)
-        self._cfg = _native.make_config(energy_range=tuple(float(x) for x in energy_range), precision=precision)
+        self._cfg = dict(energy_range=tuple(float(x) for x in energy_range), precision=precision)
         self._engine = None
 
     @property
@@ -86,7 +86,7 @@ class DiagonalMoments:
     def _engine_for(self, values):
         h = self.matrix(values)
         if self._engine is None:
-            self._engine = _native.Engine(h, self._cfg)
+            self._engine = _binding.Engine(h, self._cfg)
         else:
             self._engine.set_hamiltonian(h)
         return self._engine

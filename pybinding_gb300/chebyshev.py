@@ -17,13 +17,14 @@ from __future__ import annotations
 import numpy as np
 import scipy.sparse as sp
 
-from . import _native
+from . import _binding
+from .fileio import Versioned
 
 __all__ = ["KPM", "kpm", "kpm_batch", "jackson_kernel", "lorentz_kernel", "dirichlet_kernel", "Series",
-           "SpatialLDOS", "KPMBatch"]
+           "SpatialLDOS", "KPMBatch", "ComputeProgressReporter"]
 
 
-class Series:
+class Series(Versioned):
     """A 1D (or column-wise 2D) data series over a variable: the part of
     ``pybinding.results.Series`` (``pybinding/results.py:162-215``) that KPM returns."""
 
@@ -41,20 +42,6 @@ class Series:
     def __repr__(self):
         return "Series(%s -> %s, %d points)" % (self.labels.get("variable"), self.labels.get("data"),
                                                self.variable.size)
-
-    # pickled state as pybinding's ``@pickleable`` classes store it (support/pickle.py:77-106),
-    # so that ``.pbz`` files carry the same layout either way
-    def __getstate__(self):
-        return dict(version=0, dict=self.__dict__)
-
-    def __setstate__(self, state):
-        if "version" not in state:
-            self.__dict__.update(state)
-            return
-        if state["version"] != 0:
-            raise RuntimeError("Can't create class {} v0 from incompatible data v{}".format(
-                type(self), state["version"]))
-        self.__dict__.update(state["dict"])
 
 
 class SpatialLDOS:
@@ -89,10 +76,10 @@ class Kernel:
         self.param = float(param)
 
     def damping_coefficients(self, num_moments):
-        return _native.damping_coefficients(self.name, self.param, num_moments)
+        return _binding.damping_coefficients(self.name, self.param, num_moments)
 
     def required_num_moments(self, scaled_broadening):
-        return _native.required_num_moments(self.name, self.param, scaled_broadening)
+        return _binding.required_num_moments(self.name, self.param, scaled_broadening)
 
     def __repr__(self):
         return "%s_kernel(%s)" % (self.name, "" if self.name != "lorentz" else self.param)
@@ -117,8 +104,7 @@ class KPMStats:
     """``KPMStats`` (``cppmodule/src/kpm.cpp:50-66``) from the engine's ``kpm_stats``."""
 
     def __init__(self, s):
-        for name, _ in s._fields_:
-            setattr(self, name, getattr(s, name))
+        self.__dict__.update(vars(s))
         self.uses_full_system = bool(self.uses_full_system)
 
 
@@ -126,12 +112,24 @@ def _dtype_of(model):
     return np.dtype(sp.csr_matrix(model.hamiltonian).dtype)
 
 
+def _is_multiorbital(model):
+    """``Model::is_multiorbital``: more Hamiltonian rows than sites (duck-typed models that do not
+    say so themselves are judged by their system's sizes)."""
+    flag = getattr(model, "is_multiorbital", None)
+    if flag is not None:
+        return bool(flag() if callable(flag) else flag)
+    system = getattr(model, "system", None)
+    size = getattr(system, "hamiltonian_size", None)
+    sites = getattr(system, "num_sites", None)
+    return size is not None and sites is not None and size != sites
+
+
 class GpuImpl:
     """The ``impl`` object of :class:`KPM`: ``_cpp.KPM`` semantics on the CUDA engine."""
 
     def __init__(self, model, energy_range=(0, 0), kernel=None, matrix_format="ELL", optimal_size=True,
                  interleaved=True, lanczos_precision=0.002, precision="auto", batch_width=0, tile_rows=0,
-                 moments_gemm="fp64", staging="auto", **_):
+                 moments_gemm="fp64", staging="auto", num_threads="auto", progress_callback=None, **_):
         if moments_gemm not in ("fp64", "tensor"):
             raise ValueError("moments_gemm must be 'fp64' or 'tensor'")
         self.kernel = kernel if kernel is not None else jackson_kernel()
@@ -140,9 +138,12 @@ class GpuImpl:
                               kernel_param=self.kernel.param, matrix_format=matrix_format,
                               optimal_size=optimal_size, interleaved=interleaved,
                               lanczos_precision=lanczos_precision, precision=precision, batch_width=batch_width,
-                              tile_rows=tile_rows, staging=staging)
+                              tile_rows=tile_rows, staging=staging,
+                              num_threads=0 if num_threads in (None, "auto") else int(num_threads))
         self._model = model
-        self._engine = _native.Engine(model.hamiltonian, _native.make_config(**self._cfg_args))
+        self._engine = _binding.Engine(model.hamiltonian, self._cfg_args)
+        if progress_callback is not None:
+            self._engine.set_progress_callback(progress_callback)
 
     # -------------------------------------------------------------- properties
     @property
@@ -201,7 +202,10 @@ class GpuImpl:
         return ldos
 
     def calc_spatial_ldos(self, energy, broadening, shape, sublattice=""):
-        """``KPM::calc_spatial_ldos`` (KPM.cpp:67-94): every site inside ``shape``."""
+        """``KPM::calc_spatial_ldos`` (KPM.cpp:67-94): every site inside ``shape``, single-orbital
+        models only (site index = Hamiltonian index), like the reference."""
+        if _is_multiorbital(self._model):
+            raise RuntimeError("This function doesn't currently support multi-orbital models")
         system = self._model.system
         x, y, z = system.positions
         contains = shape(x, y, z) if callable(shape) else shape.contains(x, y, z)
@@ -355,6 +359,33 @@ class KPM:
         return Series(chemical_potential, data, labels=dict(variable=r"$\mu$ (eV)", data=r"$\sigma (e^2/h)$"))
 
 
+class ComputeProgressReporter:
+    """The default progress callback of :func:`kpm` (``pybinding/chebyshev.py:320-336``): prints
+    when the moments of a DOS start, then the share of the vectors done."""
+
+    def __init__(self, stream=None):
+        self.stream = stream
+        self.done = 0
+
+    def _print(self, text, end="\n"):
+        import sys
+        out = self.stream or sys.stdout
+        out.write(text + end)
+        out.flush()
+
+    def __call__(self, delta, total):
+        if total == 1:
+            return  # short jobs are not reported
+        if delta < 0:  # start
+            self.done = 0
+            self._print("Computing KPM moments...")
+        elif delta == total:  # finish (increments are smaller than the total)
+            self._print("\r100%")
+        else:
+            self.done += delta
+            self._print("\r%3d%%" % (100 * self.done // total), end="")
+
+
 def kpm(model, energy_range=None, kernel="default", num_threads="auto", silent=False, **kwargs):
     """GB300 KPM for ``model`` -- same signature as ``pb.kpm`` (pybinding/chebyshev.py:339-378).
 
@@ -362,14 +393,18 @@ def kpm(model, energy_range=None, kernel="default", num_threads="auto", silent=F
     ``optimal_size``, ``interleaved``, ``lanczos_precision``; plus the GPU knobs
     ``precision`` ("auto", "fp64", "fp32"), ``batch_width`` and ``moments_gemm``
     ("fp64": the conductivity's moments matrix on the FP64 CUDA cores; "tensor": on
-    the tensor cores from FP32 planes, three-product TF32 split). ``num_threads``
-    and ``silent`` are accepted for compatibility (the GPU needs no CPU threads
-    and prints no progress).
+    the tensor cores from FP32 planes, three-product TF32 split). ``num_threads`` is the
+    number of host threads for the engine's setup work (the recursion runs on the GPU).
+    ``progress_callback(delta, total)`` follows the reference's protocol during ``calc_dos``
+    (a :class:`ComputeProgressReporter` unless ``silent``).
     """
     if kernel == "default":
         kernel = jackson_kernel()
-    kwargs.pop("progress_callback", None)
-    return KPM(GpuImpl(model, energy_range or (0, 0), kernel, **kwargs))
+    if "progress_callback" not in kwargs:
+        kwargs["progress_callback"] = ComputeProgressReporter()
+    if silent:
+        kwargs["progress_callback"] = None
+    return KPM(GpuImpl(model, energy_range or (0, 0), kernel, num_threads=num_threads, **kwargs))
 
 
 def block_diagonal(hs):
@@ -418,7 +453,7 @@ class KPMBatch:
         args.update({k: v for k, v in kwargs.items() if k in ("matrix_format", "optimal_size", "interleaved",
                                                               "lanczos_precision", "precision", "batch_width",
                                                               "tile_rows", "fuse_steps", "staging")})
-        self.engine = _native.Engine(h, _native.make_config(**args), system_offsets=self.offsets)
+        self.engine = _binding.Engine(h, args, system_offsets=self.offsets)
 
     def scaling_factors(self):
         return [self.engine.scaling_factors(s) for s in range(len(self.models))]

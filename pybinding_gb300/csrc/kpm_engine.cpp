@@ -275,10 +275,21 @@ std::string pretty_time(double s) {
     return buf;
 }
 
-// Runs f(0 .. count-1) on up to hardware_concurrency threads (host-side setup work).
+// Host threads for the setup work of the engine call running on this thread: the engine's
+// num_threads (kpm::DefaultCompute's num_threads, cppmodule/src/kpm.cpp:14), 0 = all cores.
+thread_local int tl_host_threads = 0;
+struct HostThreads {
+    int saved;
+    explicit HostThreads(int n) : saved(tl_host_threads) { tl_host_threads = n; }
+    ~HostThreads() { tl_host_threads = saved; }
+};
+
+// Runs f(0 .. count-1) on up to hardware_concurrency (or num_threads) threads (host-side setup work).
 template<class F>
 void parallel_for(int64_t count, F&& f) {
-    int64_t const nt = std::max<int64_t>(1, std::min<int64_t>(count, std::thread::hardware_concurrency()));
+    int64_t hw = std::thread::hardware_concurrency();
+    if (tl_host_threads > 0) hw = std::min<int64_t>(hw, tl_host_threads);
+    int64_t const nt = std::max<int64_t>(1, std::min<int64_t>(count, hw));
     if (nt <= 1) {
         for (int64_t i = 0; i < count; ++i) f(i);
         return;
@@ -333,7 +344,7 @@ struct kpm_engine {
 
     // Lanczos device state
     bool lz_uploaded = false;
-    DBuf d_lip, d_lix, d_lval, d_lv0, d_lv1, d_ltiles, d_lab;
+    DBuf d_lip, d_lix, d_lval, d_lv0, d_lv1, d_ltiles, d_lab, d_lpart, d_lsys;
     int lz_tiles = 0;
 
     // recursion buffers
@@ -350,7 +361,7 @@ struct kpm_engine {
     int pair_key_nbatch = -1, pair_key_lpr = -1;
     int64_t pair_key_rows = -1;
     int pair_seq = 0;
-    DBuf d_pair_counters, d_pair_error, d_multi_bar;
+    DBuf d_pair_counters, d_pair_error;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -365,11 +376,9 @@ struct kpm_engine {
     struct RecursionGraphKey {
         void const *x0, *x1, *acc, *tiles, *col, *val;
         int64_t half, bstride, step_acc;
-        int ntiles, vtype, E, LPR, nbatch, unroll, W, tma_rows, gather_rows;
+        int ntiles, vtype, E, LPR, nbatch, unroll, W, prefetch;
         int32_t row_limit;
-        int* error;
         bool real_matrix;
-        bool async_copy;
         bool operator==(RecursionGraphKey const& o) const { return std::memcmp(this, &o, sizeof o) == 0; }
     };
     RecursionGraphKey graph_key{};
@@ -411,6 +420,19 @@ struct kpm_engine {
 
     std::vector<unsigned char> h_starters, h_starters_right;  // host starters the engine generates
 
+    // Progress of the stochastic DOS (DefaultCompute::progress_start/update/finish,
+    // kpm/default/Compute.cpp:64-87,133-144): fn(-1, total) before the recursion, increments
+    // adding up to `total` vectors as segments of the recursion complete, fn(total, total) at the
+    // end; called on the calling thread, which waits on the segments' events.
+    kpm_progress_fn progress_fn = nullptr;
+    void* progress_user = nullptr;
+    int64_t progress_total = 0;  // > 0 while a DOS call reports progress
+    static constexpr int kProgressSegments = 8;
+    cudaEvent_t progress_ev[kProgressSegments] = {};
+    void progress(int64_t delta) {
+        if (progress_fn && progress_total > 0) progress_fn(delta, progress_total, progress_user);
+    }
+
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
@@ -418,6 +440,8 @@ struct kpm_engine {
 
     ~kpm_engine() {
         drop_graph();
+        for (auto& ev : progress_ev)
+            if (ev) cudaEventDestroy(ev);
         if (ev_t0) cudaEventDestroy(ev_t0);
         if (ev_t1) cudaEventDestroy(ev_t1);
         if (ev_u0) cudaEventDestroy(ev_u0);
@@ -544,12 +568,19 @@ struct kpm_engine {
             upload_host(d_lval.p, vals.data(), vals.size());
         }
         std::vector<Tile> tiles;
-        for (int s = 0; s < nsys; ++s)
+        std::vector<int32_t> sys_tiles{0};  // tiles of system s: sys_tiles[s] .. sys_tiles[s + 1] - 1
+        for (int s = 0; s < nsys; ++s) {
             for (int64_t r = sys_off[s]; r < sys_off[s + 1]; r += 2048)
                 tiles.push_back({static_cast<int32_t>(r), static_cast<int32_t>(std::min(sys_off[s + 1], r + 2048)), s, 0});
+            sys_tiles.push_back(static_cast<int32_t>(tiles.size()));
+        }
         lz_tiles = static_cast<int>(tiles.size());
         d_ltiles.ensure(sizeof(Tile) * tiles.size());
         KPM_CUDA(cudaMemcpyAsync(d_ltiles.p, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, stream));
+        d_lpart.ensure(sizeof(double) * tiles.size());
+        d_lsys.ensure(sizeof(int32_t) * sys_tiles.size());
+        KPM_CUDA(cudaMemcpyAsync(d_lsys.p, sys_tiles.data(), sizeof(int32_t) * sys_tiles.size(), cudaMemcpyHostToDevice,
+                                 stream));
         d_lv0.ensure(es * rows);
         d_lv1.ensure(es * rows);
         d_lab.ensure(sizeof(double) * 3 * nsys);
@@ -620,8 +651,10 @@ struct kpm_engine {
                 double* al = dblock + 2 * j * slot;
                 double* nr = al + slot;
                 KPM_CUDA(kpm::launch_lanczos_a(cpx, d_lip.as<int32_t>(), d_lix.as<int32_t>(), d_lval.p, v1d, v0,
-                                               d_ltiles.as<Tile>(), lz_tiles, np, al, stream));
-                KPM_CUDA(kpm::launch_lanczos_b(cpx, v1d, v0, d_ltiles.as<Tile>(), lz_tiles, al, nr, stream));
+                                               d_ltiles.as<Tile>(), lz_tiles, np, d_lpart.as<double>(),
+                                               d_lsys.as<int32_t>(), nsys, al, stream));
+                KPM_CUDA(kpm::launch_lanczos_b(cpx, v1d, v0, d_ltiles.as<Tile>(), lz_tiles, al, d_lpart.as<double>(),
+                                               d_lsys.as<int32_t>(), nsys, nr, stream));
                 KPM_CUDA(kpm::launch_lanczos_c(cpx, v0, d_ltiles.as<Tile>(), lz_tiles, nr, stream));
                 std::swap(v0, v1d);
             }
@@ -947,7 +980,7 @@ struct kpm_engine {
         cudaGetDevice(&dev);
         return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, full_rows, real_values};
     }
-    struct Tuned { int rows_per_tile, unroll, E, LPR, tma_rows; bool async_copy; int gather_rows = 0; };
+    struct Tuned { int rows_per_tile, unroll, E, LPR, prefetch = 0; };
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
     template<class T>
@@ -982,7 +1015,7 @@ struct kpm_engine {
             Tuned hit{};
             if (tuned().find(key, hit)) return hit;
         }
-        Tuned best{(256 / sh.LPR) * 16, 1, sh.E, sh.LPR, 0, false};
+        Tuned best{(256 / sh.LPR) * 16, 1, sh.E, sh.LPR};
         // lane mappings of this K: the default (16 bytes per lane) and, when the row allows,
         // half the elements per lane over twice the lanes
         std::vector<std::pair<int, int>> maps{{sh.E, sh.LPR}};
@@ -994,7 +1027,7 @@ struct kpm_engine {
             for (auto const& mp : maps)
                 for (int unroll : {1, 2})
                     for (int rpt : {1, 2, 4, 8, 16, 32, 64}) {
-                        if (rpt < 2 * unroll) continue;
+                        if (rpt < 2 * unroll || cfg.staging == 2) continue;
                         Shape t = sh;
                         t.E = mp.first;
                         t.LPR = mp.second;
@@ -1013,64 +1046,38 @@ struct kpm_engine {
                         float ms = 0;
                         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
                         last_tuning.push_back({static_cast<double>(t.rows_per_tile), static_cast<double>(unroll), ms / 3});
-                        if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR, 0, false}; }
+                        if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR}; }
                     }
-            // the TMA-staged kernel (full rows, 16-byte lanes): tile heights that fit in shared memory
-            if (cfg.staging != 1 && full_rows && sh.E * kpm::vtype_bytes(vtype) == 16 && sh.LPR > 1 &&
-                base.error != nullptr && !base.real_matrix)
-                for (int tr : {32, 64, 128}) {
+            // the step with prefetched ELL entries (diag_pf_kernel): tiles of whole warp chunks
+            // (8 warps x 16 rows), register allocation held to 4 blocks per SM or not
+            base.unroll = 1;
+            base.E = sh.E;
+            base.LPR = sh.LPR;
+            for (int pf : {3, 4})
+                for (int chunks : {1, 2, 4, 8}) {
+                    if (cfg.staging == 1) break;
                     Shape t = sh;
-                    t.rows_per_tile = tr;
-                    base.E = sh.E;
-                    base.LPR = sh.LPR;
+                    t.rows_per_tile = 128 * chunks;
                     base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
                     base.tiles = d_tiles.as<Tile>();
                     base.init = false;
-                    base.unroll = 1;
-                    base.tma_rows = tr;
-                    cudaError_t const le = kpm::launch_diag_step(base, stream);
-                    if (le != cudaSuccess) {  // e.g. too much shared memory for this height
+                    base.prefetch = pf;
+                    cudaError_t const le = kpm::launch_diag_step(base, stream);  // warm
+                    if (le == cudaErrorInvalidValue) {  // rows too wide for the shared-memory chunks
                         cudaGetLastError();
-                        continue;
-                    }
-                    KPM_CUDA(cudaEventRecord(ev0, stream));
-                    for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
-                    KPM_CUDA(cudaEventRecord(ev1, stream));
-                    KPM_CUDA(cudaEventSynchronize(ev1));
-                    float ms = 0;
-                    KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                    last_tuning.push_back({static_cast<double>(tr), -1.0, ms / 3});
-                    if (ms < best_ms) { best_ms = ms; best = Tuned{tr, 1, sh.E, sh.LPR, tr, false}; }
-                }
-            base.tma_rows = 0;
-            // the cp.async pipeline kernel (rows of at most 4 entries, 16-byte lanes)
-            if (cfg.staging != 1 && full_rows && W <= 4 && sh.E * kpm::vtype_bytes(vtype) == 16 && !base.real_matrix)
-                for (int rpt : {8, 16, 32}) {
-                    Shape t = sh;
-                    t.rows_per_tile = (256 / sh.LPR) * rpt;
-                    base.E = sh.E;
-                    base.LPR = sh.LPR;
-                    base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
-                    base.tiles = d_tiles.as<Tile>();
-                    base.init = false;
-                    base.unroll = 1;
-                    base.async_copy = true;
-                    cudaError_t const le = kpm::launch_diag_step(base, stream);
-                    if (le != cudaSuccess) {
-                        cudaGetLastError();
-                        base.async_copy = false;
                         break;
                     }
+                    KPM_CUDA(le);
                     KPM_CUDA(cudaEventRecord(ev0, stream));
                     for (int i = 0; i < 3; ++i) KPM_CUDA(kpm::launch_diag_step(base, stream));
                     KPM_CUDA(cudaEventRecord(ev1, stream));
                     KPM_CUDA(cudaEventSynchronize(ev1));
                     float ms = 0;
                     KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                    last_tuning.push_back({static_cast<double>(t.rows_per_tile), -2.0, ms / 3});
-                    if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, 1, sh.E, sh.LPR, 0, true}; }
+                    last_tuning.push_back({static_cast<double>(t.rows_per_tile), static_cast<double>(-pf), ms / 3});
+                    if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, 1, sh.E, sh.LPR, pf}; }
                 }
-            base.async_copy = false;
+            base.prefetch = 0;
         }
         tuned().put(key, best);
         return best;
@@ -1262,41 +1269,26 @@ struct kpm_engine {
         a.x = d_x0.p;
         a.y = d_x1.p;
         a.acc = d_acc.as<double>();
-        bool alt_map = false;  // a thinner lane mapping or the TMA-staged kernel: single-step launches only
+        bool alt_map = false;  // a thinner lane mapping: single-step launches only
         d_pair_error.ensure(sizeof(int));
         KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
-        a.error = d_pair_error.as<int>();
-        bool const tma_ok = full_rows && sh.E * vb == 16 && sh.LPR > 1 && !real_values;
-        bool const async_ok = full_rows && sh.E * vb == 16 && W <= 4 && !real_values;
-        if (cfg.staging == 2 && tma_ok) {
-            sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 64;
-            a.tma_rows = sh.rows_per_tile;
-            alt_map = true;
-        } else if (cfg.staging == 3 && async_ok) {
-            sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : (256 / sh.LPR) * 16;
-            a.async_copy = true;
-            alt_map = true;
-        } else if (cfg.staging == 4 && full_rows && vtype == kpm::V_F32 && sh.E == 4 && sh.K <= 256) {
-            sh.rows_per_tile = cfg.tile_rows > 0 ? cfg.tile_rows : 32;
-            a.gather_rows = sh.rows_per_tile;
-            alt_map = true;
-        } else if (cfg.tile_rows > 0) {
+        if (cfg.tile_rows > 0) {
             sh.rows_per_tile = cfg.tile_rows;
+            if (cfg.staging == 2 && kpm::diag_pf_supported(vtype, W, sh.LPR)) a.prefetch = 4;
         } else {
             Tuned const tu = tune_diag(sh, sys0, batch_outer, full_rows, a);
             sh.rows_per_tile = tu.rows_per_tile;
             a.unroll = tu.unroll;
-            alt_map = tu.E != sh.E || tu.tma_rows > 0 || tu.async_copy || tu.gather_rows > 0;
+            a.prefetch = tu.prefetch;
+            alt_map = tu.E != sh.E;
             if (alt_map && cfg.fuse_steps == 2 && !opt_rows) {  // two-step launches asked for: default kernel
                 alt_map = false;
                 sh.rows_per_tile = (256 / sh.LPR) * 16;
                 a.unroll = 1;
+                a.prefetch = 0;
             } else {
                 sh.E = tu.E;
                 sh.LPR = tu.LPR;
-                a.tma_rows = tu.tma_rows;
-                a.async_copy = tu.async_copy;
-                a.gather_rows = tu.gather_rows;
             }
             a.E = sh.E;
             a.LPR = sh.LPR;
@@ -1381,30 +1373,9 @@ struct kpm_engine {
             choice = FuseChoice{2, cfg.tile_rows > 0 ? cfg.tile_rows : rpp * 8};
             have_choice = true;
         }
-        // all steps in one cooperative launch (choice steps = 3): recursions whose vectors and
-        // matrix stay in L2, where the per-step launch gap and ramp weigh most
-        size_t const l2_bytes = 2 * vbytes + static_cast<size_t>(rows) * W * (4 + kpm::vtype_vs(vtype) * vb);
-        // (any lane mapping of the register-load step; not the staged kernels)
-        bool const multi_ok = !opt_rows && cfg.fuse_steps != 1 && a.tma_rows == 0 && !a.async_copy &&
-                              a.gather_rows == 0 && l2_bytes <= (size_t{64} << 20);
-        d_multi_bar.ensure(2 * sizeof(unsigned));
-        auto multi_steps = [&](int64_t count) {
-            KPM_CUDA(cudaMemsetAsync(d_multi_bar.p, 0, 2 * sizeof(unsigned), stream));
-            KPM_CUDA(kpm::launch_diag_multi(a, r0, r1, n, n + count - 1, d_acc.as<double>(),
-                                            static_cast<int64_t>(step_acc), d_multi_bar.as<unsigned>(), 1 << 25,
-                                            stream));
-            if (count % 2) std::swap(r0, r1);
-            n += count;
-        };
-        if (cfg.fuse_steps == 3) {  // asked for: one launch where the system fits, else one step per launch
-            choice = FuseChoice{multi_ok ? 3 : 1, 0};
-            have_choice = true;
-        }
         if (can_pair && !have_choice) {
             // time each candidate on four steps of this recursion, keep the fastest, then start
-            // the recursion over with it. The one-launch form is not a candidate: on the 60k-site
-            // complex128 DOS it ran 26.8 us per step against 22.0 us for graph-replayed single
-            // steps (its gathers must bypass L1 for coherence across the grid barrier)
+            // the recursion over with it
             std::vector<FuseChoice> cands{{1, 0}};
             for (int rpt : {4, 8, 16, 32}) cands.push_back({2, rpp * rpt});
             double best = 1e30;
@@ -1438,10 +1409,18 @@ struct kpm_engine {
             PairPlan* pp = pair_plan(sh, choice.rows_per_tile);
             while (n + 1 <= half) pair_step(pp);
         }
-        int64_t multi_count = 0;
-        if (choice.steps == 3 && multi_ok && n <= half) {
-            multi_count = half - n + 1;
-            multi_steps(multi_count);
+        int progress_segments = 0;
+        if (progress_total > 0 && progress_fn && n <= half) {
+            // reported progress: the remaining steps in segments, each followed by an event that
+            // the host waits on below (the launches are all queued first, so the GPU never idles)
+            int64_t const n0 = n, left = half - n + 1;
+            for (int k = 0; k < kProgressSegments; ++k) {
+                if (!progress_ev[k]) KPM_CUDA(cudaEventCreateWithFlags(&progress_ev[k], cudaEventDisableTiming));
+                int64_t const stop = n0 + left * (k + 1) / kProgressSegments;
+                while (n < stop) single_step();
+                KPM_CUDA(cudaEventRecord(progress_ev[k], stream));
+            }
+            progress_segments = kProgressSegments;
         }
         if (n == 2 && half >= 3 && !opt_rows) {
             // steady state (no tuning steps ran in this call): replay the captured recursion
@@ -1464,11 +1443,8 @@ struct kpm_engine {
             key.unroll = a.unroll;
             key.W = W;
             key.row_limit = a.row_limit;
-            key.tma_rows = a.tma_rows;
-            key.gather_rows = a.gather_rows;
             key.real_matrix = a.real_matrix;
-            key.async_copy = a.async_copy;
-            key.error = a.error;
+            key.prefetch = a.prefetch;
             if (graph_exec == nullptr || !(key == graph_key)) {
                 drop_graph();
                 KPM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -1494,19 +1470,22 @@ struct kpm_engine {
             KPM_CUDA(cudaGraphLaunch(graph_exec, stream));
         }
         while (n <= half) single_step();
-        last_fuse = multi_count > 0 ? static_cast<int>(multi_count) : (choice.steps == 3 ? 1 : choice.steps);
-        last_tma_rows = a.async_copy ? -sh.rows_per_tile : a.tma_rows;
-        last_gather_rows = a.gather_rows;
+        last_fuse = choice.steps;
         last_unroll = a.unroll;
+        last_prefetch = a.prefetch;
         KPM_CUDA(cudaEventRecord(ev1, stream));
         KPM_CUDA(kpm::launch_collect_diag(vtype, d_acc.as<double>(), ns, sh.nbatch, sh.K, half, M, nvec, false,
                                           d_mu.as<double>(), stream));
         int pair_err = 0;
         KPM_CUDA(cudaMemcpyAsync(&pair_err, d_pair_error.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        for (int k = 0; k < progress_segments; ++k) {
+            KPM_CUDA(cudaEventSynchronize(progress_ev[k]));
+            progress(progress_total * (k + 1) / progress_segments - progress_total * k / progress_segments);
+        }
         KPM_CUDA(cudaStreamSynchronize(stream));
         if (pair_err)
-            fail(KPM_ERR_TIMEOUT, "a recursion launch gave up waiting (a neighbouring tile of a two-step launch, or "
-                                  "a staged copy); results discarded");
+            fail(KPM_ERR_TIMEOUT, "a two-step recursion launch gave up waiting for a neighbouring tile; results "
+                                  "discarded");
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         st.moments_time = ms * 1e-3;
@@ -1517,9 +1496,8 @@ struct kpm_engine {
     }
     Shape last_shape{};
     int last_fuse = 1;
-    int last_tma_rows = 0;
-    int last_gather_rows = 0;
     int last_unroll = 1;
+    int last_prefetch = 0;
     double last_upload_time = 0;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
     cudaEvent_t ev_u0 = nullptr, ev_u1 = nullptr;  // starter upload + scatter of the last diagonal call
@@ -1555,8 +1533,9 @@ struct kpm_engine {
         st.steps_per_launch = last_fuse;
         st.elems_per_lane = last_shape.E;
         st.lanes_per_row = last_shape.LPR;
-        st.staged_rows = last_tma_rows;
-        st.gather_rows = last_gather_rows;
+        st.staged_rows = 0;
+        st.prefetch = last_prefetch;
+        st.gather_rows = 0;
         st.tile_rows = last_shape.rows_per_tile;
         st.unroll = last_unroll;
         st.upload_time = last_upload_time;
@@ -1614,6 +1593,7 @@ void kpm_config_default(kpm_config* c) {
     c->tile_rows = 0;
     c->fuse_steps = 0;
     c->staging = 0;
+    c->num_threads = 0;
 }
 
 int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const int32_t* indices, const void* values,
@@ -1632,8 +1612,8 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
-        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 3) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1, 2 or 3");
-        if (e->cfg.staging < 0 || e->cfg.staging > 4) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2, 3 or 4");
+        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
+        if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
         *out = e.release();
     });
@@ -1665,8 +1645,8 @@ int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
         if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
             fail(KPM_ERR_VALUE, "unknown precision mode");
-        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 3) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1, 2 or 3");
-        if (e->cfg.staging < 0 || e->cfg.staging > 4) fail(KPM_ERR_VALUE, "staging must be 0, 1, 2, 3 or 4");
+        if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
+        if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
         // the members' CSR matrices were checked when their engines were made: concatenate them
         // (columns shifted into their block), each member's copy in parallel
         int const st = engines[0]->stype;
@@ -1725,6 +1705,7 @@ int kpm_set_hamiltonian(kpm_engine* e, int32_t scalar_type, int64_t rows, const 
                         const int64_t* system_offsets) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         e->set_h(scalar_type, rows, indptr, indices, values, num_systems, system_offsets);
     });
 }
@@ -1732,6 +1713,7 @@ int kpm_set_hamiltonian(kpm_engine* e, int32_t scalar_type, int64_t rows, const 
 int kpm_energy_bounds(kpm_engine* e, int32_t system, double* mn, double* mx, int32_t* loops) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (system < 0 || system >= e->nsys) fail(KPM_ERR_VALUE, "system index out of range");
         e->compute_bounds();
         if (mn) *mn = e->sys[system].emin;
@@ -1743,6 +1725,7 @@ int kpm_energy_bounds(kpm_engine* e, int32_t system, double* mn, double* mx, int
 int kpm_scaling_factors(kpm_engine* e, int32_t system, double* a, double* b) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (system < 0 || system >= e->nsys) fail(KPM_ERR_VALUE, "system index out of range");
         auto const s = e->scale(system);
         if (a) *a = s.a;
@@ -1754,6 +1737,7 @@ int kpm_moments_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
                      int32_t starters_on_device, int32_t average, double* out, int64_t* num_moments_out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (!starters || !out) fail(KPM_ERR_VALUE, "null starters or output");
         int64_t const M = round_moments(num_moments);
         double const t0 = now_s();
@@ -1778,6 +1762,7 @@ int kpm_moments_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
 int kpm_calc_dos(kpm_engine* e, const double* energy, int64_t ne, double broadening, int64_t num_random, double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (num_random < 1) fail(KPM_ERR_VALUE, "num_random must be >= 1");
         if (ne > 0 && (!energy || !out)) fail(KPM_ERR_VALUE, "null energy or output");
         double const t0 = now_s();
@@ -1821,7 +1806,15 @@ int kpm_calc_dos(kpm_engine* e, const double* energy, int64_t ne, double broaden
                 });
             }
         });
+        e->progress_total = e->progress_fn ? num_random : 0;
+        struct ProgressEnd {  // no reports outside this call, also after an exception
+            kpm_engine* e;
+            ~ProgressEnd() { e->progress_total = 0; }
+        } progress_end{e};
+        e->progress(-1);
         e->run_diag(Mmax, num_random, st.data(), false, nullptr, false);
+        e->progress(num_random);
+        e->progress_total = 0;
         e->reset_stats(Mmax, true, false, static_cast<double>(num_random) * e->nsys, 0);
         e->d_mu_avg.ensure(sizeof(double) * 2 * e->nsys * Mmax);
         KPM_CUDA(kpm::launch_average(e->d_mu.as<double>(), e->nsys, num_random, Mmax, e->d_mu_avg.as<double>(), e->stream));
@@ -1839,6 +1832,7 @@ int kpm_calc_ldos(kpm_engine* e, const int64_t* idx, int64_t nidx, const double*
                   double broadening, double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "LDOS needs a single-system engine");
         if (nidx < 1 || !idx) fail(KPM_ERR_VALUE, "no LDOS indices");
         double const t0 = now_s();
@@ -1865,6 +1859,7 @@ int kpm_calc_ldos_batch(kpm_engine* e, const int64_t* sites, const double* energ
                         double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (!sites) fail(KPM_ERR_VALUE, "no LDOS sites");
         if (ne > 0 && (!energy || !out)) fail(KPM_ERR_VALUE, "null energy or output");
         for (int s = 0; s < e->nsys; ++s)
@@ -1896,6 +1891,7 @@ int kpm_calc_greens(kpm_engine* e, int64_t row, const int64_t* cols, int64_t nco
                     double broadening, double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "Green's function needs a single-system engine");
         if (ncols < 1 || !cols) fail(KPM_ERR_VALUE, "no Green's function columns");
         int64_t const size = e->rows;
@@ -2011,6 +2007,7 @@ int kpm_moments(kpm_engine* e, int64_t num_moments, const double* alpha, int64_t
                 const double* op_values, double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "moments() needs a single-system engine");
         int64_t const n = e->rows;
         // KPM.cpp:20-33 (checked in the reference's unordered_map order: operator, beta, alpha)
@@ -2400,6 +2397,7 @@ int kpm_calc_conductivity(kpm_engine* e, const float* left, const float* right, 
                           int32_t gemm_mode, double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (!left || !right || (nmu > 0 && (!chem || !out))) fail(KPM_ERR_VALUE, "null argument");
         if (num_random < 1 || num_points < 2) fail(KPM_ERR_VALUE, "num_random >= 1 and num_points >= 2 required");
         double const t0 = now_s();
@@ -2422,6 +2420,7 @@ int kpm_conductivity_moments(kpm_engine* e, const float* left, const float* righ
                              int64_t num_random, int32_t gemm_mode, double* out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (!out) fail(KPM_ERR_VALUE, "null output");
         double const t0 = now_s();
         std::vector<double> mu;
@@ -2464,6 +2463,7 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
                      int64_t* num_moments_out) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (!starters || !dl_dmu || !out_grad_values) fail(KPM_ERR_VALUE, "null argument");
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "adjoint gradients need a single-system engine");
         if (kpm::vtype_complex(e->vtype) || e->stype == KPM_C64 || e->stype == KPM_C128)
@@ -2512,8 +2512,8 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         d_seg.ensure(vec * seg_len);
         d_lam.ensure(vec * 2);
         d_roll.ensure(vec * 2);
-        d_gt.ensure(static_cast<size_t>(vb) * n * W);  // gradient sums in the vectors' precision
-        d_gd.ensure(static_cast<size_t>(vb) * n);
+        d_gt.ensure(sizeof(double) * n * W);  // FP64 gradient sums
+        d_gd.ensure(sizeof(double) * n);
         KPM_CUDA(cudaMemsetAsync(d_gt.p, 0, d_gt.bytes, e->stream));
         KPM_CUDA(cudaMemsetAsync(d_gd.p, 0, d_gd.bytes, e->stream));
         auto* ck = static_cast<unsigned char*>(d_ck.p);
@@ -2630,10 +2630,8 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         std::vector<double> gt(static_cast<size_t>(n) * W), gd(static_cast<size_t>(n));
-        for (size_t i = 0; i < gt.size(); ++i)
-            gt[i] = vb == 4 ? reinterpret_cast<float const*>(gt_raw.data())[i] : reinterpret_cast<double const*>(gt_raw.data())[i];
-        for (size_t i = 0; i < gd.size(); ++i)
-            gd[i] = vb == 4 ? reinterpret_cast<float const*>(gd_raw.data())[i] : reinterpret_cast<double const*>(gd_raw.data())[i];
+        std::memcpy(gt.data(), gt_raw.data(), sizeof(double) * gt.size());
+        std::memcpy(gd.data(), gd_raw.data(), sizeof(double) * gd.size());
         // gt[p][t] holds G[col(p, t)][p]: entry (i, j) of the input is found in row map[j]
         double const f = 2.0 / sc.a;
         for (int64_t i = 0; i < n; ++i)
@@ -2706,6 +2704,7 @@ int kpm_optimized_hamiltonian(kpm_engine* e, const int32_t* src, int64_t n_src, 
                               int32_t* oslices, int64_t* onslices, int32_t* osrc, int32_t* odest, int64_t* offsets) {
     return guarded([&] {
         if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
         if (e->nsys != 1) fail(KPM_ERR_VALUE, "needs a single-system engine");
         if (n_src < 1 || n_dest < 1) fail(KPM_ERR_VALUE, "empty index lists");
         for (int64_t i = 0; i < n_src; ++i) if (src[i] < 0 || src[i] >= e->rows) fail(KPM_ERR_VALUE, "src index out of range");
@@ -2741,6 +2740,15 @@ int kpm_optimized_hamiltonian(kpm_engine* e, const int32_t* src, int64_t n_src, 
         offsets[0] = find_offset(os);
         offsets[1] = find_offset(od);
         e->map = saved_map;
+    });
+}
+
+int kpm_set_progress_callback(kpm_engine* e, kpm_progress_fn fn, void* user) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
+        e->progress_fn = fn;
+        e->progress_user = user;
     });
 }
 

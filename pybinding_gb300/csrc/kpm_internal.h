@@ -42,12 +42,9 @@ struct DiagStep {
     double* acc;
     bool init;
     int unroll = 1;           // rows per thread per iteration (1 or 2), chosen by the autotuner
-    int tma_rows = 0;         // > 0: TMA-staged kernel, tiles of at most this many rows (full rows only,
-                              // K * element size a multiple of 16 bytes; col/val padded by 32 bytes)
-    int* error = nullptr;     // TMA-staged kernel: set when a bounded wait gives up
-    bool async_copy = false;  // cp.async pipeline kernel (rows of <= 4 entries, 16-byte lanes; full rows)
-    int gather_rows = 0;      // > 0: TMA gather kernel (x rows gathered by tile::gather4 into shared memory),
-                              // tiles of at most this many rows (FP32, E = 4, full rows)
+    int prefetch = 0;         // > 0: ELL entries copied to shared memory a chunk ahead (diag_pf_kernel),
+                              // register allocation for 3 or 4 resident blocks per SM (3 or 4);
+                              // chosen by the autotuner; unroll is then 1
     bool real_matrix = false; // complex vectors with real H~ values: val holds [rows][W][vs] of the
                               // real type (vs of that type: hi/lo pairs for FP32)
 };
@@ -113,8 +110,8 @@ struct AdjStep {
     const void* vp;           // nullable
     double a0, am, ap;
     const void* g;            // row vectors of the gradient term (with gt)
-    void* gt;                 // nullable
-    void* gd;                 // set with gt
+    void* gt;                 // nullable; FP64 gradient sums [rows][W]
+    void* gd;                 // set with gt; FP64 [rows]
     const Tile* tiles;
     int num_tiles;
 };
@@ -148,12 +145,6 @@ struct DiagPair {
 };
 
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s);
-// Steps n0..n1 of the diagonal recursion in one cooperative launch (full rows, register
-// loads): step n reads x = r1, overwrites r0 = y, adds its sums at acc_base + step_acc (n - 1),
-// then swaps r0 and r1; the blocks meet at a grid barrier (bar: two zeroed counters) between
-// steps, whose waits give up after spin_limit polls and set a.error.
-cudaError_t launch_diag_multi(DiagStep const& a, void* r0, void* r1, int64_t n0, int64_t n1, double* acc_base,
-                              int64_t step_acc, unsigned* bar, int spin_limit, cudaStream_t s);
 cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s);
 cudaError_t launch_dense_step(DenseStep const& a, cudaStream_t s);
 
@@ -188,6 +179,8 @@ cudaError_t launch_axpby(int vtype, int64_t n, double a, void const* x, double b
 bool diag_shape_supported(int vtype, int E, int LPR);
 // diag_step_kernel instantiations, thinner lane mappings included (what launch_diag_step runs)
 bool diag_step_supported(int vtype, int E, int LPR);
+// the prefetched-entries step (DiagStep::prefetch) fits rows of W entries in shared memory
+bool diag_pf_supported(int vtype, int W, int LPR);
 
 // moments from the accumulated sums: out[(s*nbatch*K + v) * M + n] complex double,
 // or averaged over `nvec` vectors per system into out[s * M + n] when average.
@@ -214,14 +207,18 @@ cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, in
                                cudaStream_t s);
 
 // Lanczos (FP64 or complex FP64, all systems in lockstep, CSR per system in global rows)
-// A: t = H v1; v0 = t - sqrt(nrm_prev[s]) v0; alpha[s] += Re(conj(t) v1)
-// B: v0 -= alpha[s] v1; nrm[s] += |v0|^2
+// A: t = H v1; v0 = t - sqrt(nrm_prev[s]) v0; alpha[s] = sum Re(conj(t) v1)
+// B: v0 -= alpha[s] v1; nrm[s] = sum |v0|^2
 // C: v0 *= 1/sqrt(nrm[s])
+// The sums of A and B go through per-tile partials (`part`, num_tiles doubles) reduced per
+// system in a fixed order (tiles sys_tiles[s] .. sys_tiles[s + 1] - 1): bit-reproducible.
 cudaError_t launch_lanczos_a(bool cplx, int32_t const* ip, int32_t const* ix, void const* v,
                              void const* v1, void* v0, Tile const* tiles, int num_tiles,
-                             double const* nrm_prev, double* alpha, cudaStream_t s);
+                             double const* nrm_prev, double* part, int32_t const* sys_tiles, int nsys,
+                             double* alpha, cudaStream_t s);
 cudaError_t launch_lanczos_b(bool cplx, void const* v1, void* v0, Tile const* tiles, int num_tiles,
-                             double const* alpha, double* nrm, cudaStream_t s);
+                             double const* alpha, double* part, int32_t const* sys_tiles, int nsys, double* nrm,
+                             cudaStream_t s);
 cudaError_t launch_lanczos_c(bool cplx, void* v0, Tile const* tiles, int num_tiles, double const* nrm,
                              cudaStream_t s);
 

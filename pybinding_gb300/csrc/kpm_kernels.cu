@@ -14,12 +14,16 @@
 // ([batch][row][K]) and one launch covers every batch and every system of a
 // ragged batch through a tile list (rows of one system x one batch).
 //
-// Moment sums: each thread accumulates its rows in the vector precision
-// (FP32 for FP32 vectors), the block reduces them (shuffles + shared memory,
-// still FP32), and one FP64 atomic add per (block, vector, sum) lands in a
+// Moment sums: each thread accumulates the rows it visits for one (system,
+// batch) in the vector precision (FP32 for FP32 vectors: at most a few tiles,
+// ~8-64 rows per thread), the two row slots of a warp are added once, and from
+// there on everything is FP64: the block sums the per-thread partials in FP64
+// shared memory and adds one FP64 atomic per (block, vector, sum) into a
 // per-step FP64 accumulator. Per-element FP64 work is avoided on purpose:
-// GB300's FP64 rate is ~1/300 of its FP32 rate.
-#include "kpm_async.cuh"
+// GB300's FP64 rate is ~1/300 of its FP32 rate, and the FP32 partials over a
+// bounded number of rows do not add measurable error (moments of a 400k-site
+// flake agree to 2.30e-7 of the FP64 recursion with 16-row and with 1024-row
+// tiles; the error is the FP32 arithmetic of the recursion itself).
 #include "kpm_internal.h"
 
 #include <cuda.h>
@@ -244,11 +248,13 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
 // the end.
 template<class V, int E, int LPR>
 __device__ __forceinline__ void diag_flush(typename Tr<V>::R (&m2)[E], typename Tr<V>::R (&m3r)[E],
-                                           typename Tr<V>::R (&m3i)[E], typename Tr<V>::R* red, double* a) {
+                                           typename Tr<V>::R (&m3i)[E], double* red, double* a) {
     using R = typename Tr<V>::R;
     constexpr bool CPLX = Tr<V>::C;
     constexpr int K = E * LPR;
     constexpr int NV = CPLX ? 3 : 2;
+    // the row slots of a warp hold partials of the same vectors: pairwise in the partials'
+    // precision (one add for the 32 / LPR = 2 slots of a 16-lane row), then FP64 from here on
 #pragma unroll
     for (int off = LPR; off < 32; off <<= 1) {
 #pragma unroll
@@ -264,18 +270,18 @@ __device__ __forceinline__ void diag_flush(typename Tr<V>::R (&m2)[E], typename 
     if (wl < LPR) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            R* rw = red + (warp * K + wl * E + e) * NV;
-            rw[0] = m2[e];
-            rw[1] = m3r[e];
-            if (CPLX) rw[NV - 1] = m3i[e];
+            double* rw = red + (warp * K + wl * E + e) * NV;
+            rw[0] = static_cast<double>(m2[e]);
+            rw[1] = static_cast<double>(m3r[e]);
+            if (CPLX) rw[NV - 1] = static_cast<double>(m3i[e]);
         }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < K * NV; i += BLOCK) {
-        R sum = R(0);
+        double sum = 0.0;
 #pragma unroll
         for (int w = 0; w < WARPS; ++w) sum += red[w * K * NV + i];
-        atomicAdd(a + i, static_cast<double>(sum));
+        atomicAdd(a + i, sum);
     }
 #pragma unroll
     for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
@@ -292,7 +298,7 @@ diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, in
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;  // rows per pass of the block
     constexpr int NV = CPLX ? 3 : 2;
-    __shared__ R red[WARPS * K * NV];
+    __shared__ double red[WARPS * K * NV];
 
     int const lane = threadIdx.x % LPR;
     int const slot = threadIdx.x / LPR;
@@ -330,482 +336,155 @@ diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, in
         diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
 }
 
-// ------------------------------------------------------------------ many steps per launch
-// For recursions whose vectors stay in L2, every step in one cooperative launch: the blocks
-// sweep their tiles (the same tiles every step), add their moment partials to the step's
-// accumulator, and meet at a grid barrier before the next step, which saves the launch
-// gap and ramp of each step. The gathers of a step read rows other blocks wrote in the
-// step before, so x and y_old are read through L2 (the XCOH form of the row loop). The
-// barrier is a generation count: the last block to
-// arrive resets the arrival count and releases the next generation; the others poll it
-// with a bounded number of sleeps and, when it runs out, set *err and leave.
-__device__ __forceinline__ unsigned ld_acquire_u(unsigned const* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
+// ------------------------------------------------------------------ diagonal step, prefetched entries
+// The step of diag_step_kernel with the ELL entries copied into shared memory ahead of use.
+// Each warp works through chunks of PF_ROWS consecutive rows of a tile (chunks warp,
+// warp + WARPS, ... of every tile the block takes) and, while it computes one chunk, the
+// column indices and values of its next chunk are in flight as cp.async copies (no registers
+// held). A row then costs one memory round trip -- x[r], y_old[r] and every gather issued
+// together, the indices coming from shared memory -- instead of two (indices, then gathers),
+// and a warp fetches its entries in a few coalesced copies per chunk rather than one small
+// dependent load per row. cp.async completion waits are hardware waits on the warp's own
+// copies; nothing here waits on another block.
+constexpr int PF_ROWS = 16;  // rows per warp chunk (at least one pass of the warp: 32 / LPR rows)
+template<int LPR> __host__ __device__ constexpr int pf_rows() { return (32 / LPR) > PF_ROWS ? (32 / LPR) : PF_ROWS; }
 
-// bar[0] = arrivals of the current generation, bar[1] = generation
-__device__ bool grid_barrier(unsigned* bar, int* err, int spin_limit) {
-    __shared__ int ok_s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        unsigned const g = ld_acquire_u(bar + 1);
-        __threadfence();
-        if (atomicAdd(bar, 1u) + 1 == gridDim.x) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            st_release_u(bar + 1, g + 1);
-        } else {
-            int polls = 0;
-            while (ld_acquire_u(bar + 1) == g) {
-                if (++polls > spin_limit || *reinterpret_cast<int volatile*>(err) != 0) {
-                    atomicExch(err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        ok_s = ok;
-    }
-    __syncthreads();
-    return ok_s != 0;
+__device__ __forceinline__ uint32_t smem_addr(void const* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-
-template<class V, int E, int LPR, class MV = V>
-__global__ void __launch_bounds__(BLOCK)
-diag_multi_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W, V* r0, V* r1,
-                  int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles, int nbatch,
-                  double* __restrict__ acc_base, int64_t step_acc, int64_t n0, int64_t n1, unsigned* bar,
-                  int* err, int spin_limit) {
-    using R = typename Tr<V>::R;
-    constexpr bool CPLX = Tr<V>::C;
-    constexpr int K = E * LPR;
-    constexpr int RPP = BLOCK / LPR;
-    constexpr int NV = CPLX ? 3 : 2;
-    __shared__ R red[WARPS * K * NV];
-    int const lane = threadIdx.x % LPR;
-    int const slot = threadIdx.x / LPR;
-    int const G = gridDim.x;
-    for (int64_t n = n0; n <= n1; ++n) {
-        V const* x_all = r1;  // T_{n-1}
-        V* y_all = r0;        // T_{n-2} -> T_n
-        double* acc = acc_base + step_acc * (n - 1);
-        R m2[E], m3r[E], m3i[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
-        int cur_sys = -1, cur_batch = -1;
-        for (int ti = blockIdx.x; ti < num_tiles; ti += G) {
-            Tile const t = tiles[ti];
-            if (t.system != cur_sys || t.batch != cur_batch) {
-                if (cur_sys >= 0)
-                    diag_flush<V, E, LPR>(m2, m3r, m3i, red,
-                                          acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
-                cur_sys = t.system;
-                cur_batch = t.batch;
-            }
-            V const* __restrict__ x = x_all + t.batch * batch_stride;
-            V* __restrict__ y = y_all + t.batch * batch_stride;
-            for (int r = t.row_begin + slot; r < t.row_end; r += RPP) {
-                int rr[1] = {r};
-                bool live[1] = {true};
-                diag_rows<V, E, LPR, false, 1, true, MV>(col, val, W, x, y, rr, live, lane, m2, m3r, m3i);
-            }
-        }
-        if (cur_sys >= 0)
-            diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
-        V* const tmp = r0;
-        r0 = r1;
-        r1 = tmp;
-        if (n < n1 && !grid_barrier(bar, err, spin_limit)) return;
-    }
-}
-
-// ------------------------------------------------------------------ diagonal step, cp.async pipeline
-// Per-thread asynchronous copies (cp.async, global -> shared) of the next row's x[r], y_old[r]
-// and gathered x[col] while the current row is computed from shared memory: each thread keeps
-// two rows in flight without holding their data in registers. The next row's column indices
-// and matrix values are prefetched into registers one row further ahead. Rows of at most 4
-// entries, 16-byte lanes.
-__device__ __forceinline__ void cp_async16_ca(void* smem, void const* gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
-                 "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async16_cg(void* smem, void const* gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
-                 "l"(gmem)
-                 : "memory");
+__device__ __forceinline__ void cp_async4(void* dst, void const* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-constexpr int ASYNC_ITEMS = 6;  // x[r], y_old[r], 4 gathers
-
-template<class V, int E, int LPR>
-size_t diag_async_smem() {
-    using R = typename Tr<V>::R;
-    constexpr int NV = Tr<V>::C ? 3 : 2;
-    return static_cast<size_t>(2) * BLOCK * ASYNC_ITEMS * 16 + sizeof(R) * WARPS * E * LPR * NV;
+// Shared memory of one block: per warp two buffers of one chunk of entries, each buffer
+// holding the column indices (padded to 16 bytes) followed by the values.
+template<class MV, int LPR>
+__host__ __device__ constexpr int pf_col_words(int W) { return ((pf_rows<LPR>() * W + 3) / 4) * 4; }
+template<class MV, int LPR>
+__host__ __device__ constexpr int pf_buf_words(int W) {
+    return pf_col_words<MV, LPR>(W) + pf_rows<LPR>() * W * Tr<MV>::VS * static_cast<int>(sizeof(MV) / 4);
 }
+template<class MV, int LPR>
+size_t pf_smem_bytes(int W) { return static_cast<size_t>(WARPS) * 2 * pf_buf_words<MV, LPR>(W) * 4; }
+constexpr size_t PF_SMEM_MAX = 160 * 1024;  // wider rows use the per-row-load step
 
-template<class V, int E, int LPR, bool INIT>
-__global__ void __launch_bounds__(BLOCK)
-diag_async_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x_all,
-                  V* __restrict__ y_all, int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles,
-                  int nbatch, double* __restrict__ acc) {
+template<class V, int E, int LPR, bool INIT, int MINB, class MV = V>
+__global__ void __launch_bounds__(BLOCK, MINB)
+diag_pf_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
+               V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+               Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
+               double* __restrict__ acc) {
     using R = typename Tr<V>::R;
     using P = Pack<V, E>;
-    static_assert(sizeof(P) == 16, "16-byte lanes");
     constexpr bool CPLX = Tr<V>::C;
     constexpr int K = E * LPR;
-    constexpr int VS = Tr<V>::VS;
-    constexpr int RPP = BLOCK / LPR;
+    constexpr int RPW = 32 / LPR;  // rows of a warp per pass
     constexpr int NV = CPLX ? 3 : 2;
-    extern __shared__ __align__(16) unsigned char async_smem[];
-    P* stage = reinterpret_cast<P*>(async_smem);  // [2][BLOCK][ASYNC_ITEMS]
-    R* red = reinterpret_cast<R*>(async_smem + static_cast<size_t>(2) * BLOCK * ASYNC_ITEMS * 16);
-    int const lane = threadIdx.x % LPR;
-    int const slot = threadIdx.x / LPR;
+    constexpr int VS = Tr<MV>::VS;
+    constexpr int MW = static_cast<int>(sizeof(MV) / 4);  // 4-byte words per matrix value
+    constexpr int CR = pf_rows<LPR>();                     // rows per warp chunk
+    __shared__ double red[WARPS * K * NV];
+    extern __shared__ __align__(16) uint32_t pf_words[];
+
+    int const warp = threadIdx.x / 32;
+    int const wl = threadIdx.x % 32;
+    int const lane = wl % LPR;
+    int const sub = wl / LPR;
     int const G = gridDim.x;
+    int const col_words = pf_col_words<MV, LPR>(W);
+    int const buf_words = pf_buf_words<MV, LPR>(W);
+    uint32_t* const wbuf = pf_words + static_cast<size_t>(warp) * 2 * buf_words;
+
+    // the warp's next chunk at or after (ti, c): skips tiles without a chunk for this warp
+    auto next_chunk = [&](int& ti, int& c) {
+        while (ti < num_tiles) {
+            Tile const t = tiles[ti];
+            if (t.row_begin + c * CR < min(t.row_end, row_limit)) return;
+            ti += G;
+            c = warp;
+        }
+    };
+    // copies of the entries of chunk (ti, c) into buffer b
+    auto issue = [&](int ti, int c, int b) {
+        Tile const t = tiles[ti];
+        int const cb = t.row_begin + c * CR;
+        int const ce = min(cb + CR, min(t.row_end, row_limit));
+        int const ncol = (ce - cb) * W;
+        uint32_t* const dst = wbuf + b * buf_words;
+        int32_t const* src_c = col + static_cast<int64_t>(cb) * W;
+        for (int i = wl; i < ncol; i += 32) cp_async4(dst + i, src_c + i);
+        uint32_t const* src_v = reinterpret_cast<uint32_t const*>(val + static_cast<int64_t>(cb) * W * VS);
+        int const nval = ncol * VS * MW;
+        for (int i = wl; i < nval; i += 32) cp_async4(dst + col_words + i, src_v + i);
+    };
+
     R m2[E], m3r[E], m3i[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
     int cur_sys = -1, cur_batch = -1;
-    auto slot_of = [&](int st, int item) -> P* { return stage + (st * BLOCK + threadIdx.x) * ASYNC_ITEMS + item; };
+
+    int pti = blockIdx.x, pc = warp;  // the chunk whose entries are in flight or landed
+    next_chunk(pti, pc);
+    if (pti < num_tiles) issue(pti, pc, 0);
+    cp_async_commit();
+    int buf = 0;
 
     for (int ti = blockIdx.x; ti < num_tiles; ti += G) {
         Tile const t = tiles[ti];
         if (t.system != cur_sys || t.batch != cur_batch) {
             if (cur_sys >= 0)
-                diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+                diag_flush<V, E, LPR>(m2, m3r, m3i, red,
+                                      acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
             cur_sys = t.system;
             cur_batch = t.batch;
         }
         V const* __restrict__ x = x_all + t.batch * batch_stride;
         V* __restrict__ y = y_all + t.batch * batch_stride;
-        int const row_end = t.row_end;
-        // prefetched indices and values of the next row to issue
-        int32_t cn[4];
-        V vn[4 * VS];
-        auto fetch_meta = [&](int r) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                cn[q] = q < W ? __ldg(col + static_cast<int64_t>(r) * W + q) : 0;
-#pragma unroll
-                for (int v = 0; v < VS; ++v) {
-                    vzero(vn[q * VS + v]);
-                    if (q < W) vn[q * VS + v] = val[(static_cast<int64_t>(r) * W + q) * VS + v];
-                }
-            }
-        };
-        auto issue = [&](int r, int st) {
-            P const* xr = reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane;
-            cp_async16_ca(slot_of(st, 0), xr);
-            if (!INIT) cp_async16_cg(slot_of(st, 1), reinterpret_cast<P const*>(y + static_cast<int64_t>(r) * K) + lane);
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (q < W) cp_async16_ca(slot_of(st, 2 + q), reinterpret_cast<P const*>(x + static_cast<int64_t>(cn[q]) * K) + lane);
-        };
-        int r = t.row_begin + slot;
-        int32_t cc[4];
-        V vc[4 * VS];
-        if (r < row_end) {
-            fetch_meta(r);
-            issue(r, 0);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) cc[q] = cn[q];
-#pragma unroll
-            for (int i = 0; i < 4 * VS; ++i) vc[i] = vn[i];
-        }
-        cp_async_commit();
-        if (r + RPP < row_end) fetch_meta(r + RPP);
-        for (int k = 0; r < row_end; ++k, r += RPP) {
-            int const st = k & 1;
-            int const rn = r + RPP;
-            int32_t cnn[4];
-            V vnn[4 * VS];
-            if (rn < row_end) {
-                issue(rn, st ^ 1);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) cnn[q] = cn[q];
-#pragma unroll
-                for (int i = 0; i < 4 * VS; ++i) vnn[i] = vn[i];
-            }
+        int const row_end = min(t.row_end, row_limit);
+        for (int c = warp; t.row_begin + c * CR < row_end; c += WARPS) {
+            // (ti, c) is the chunk (pti, pc) prefetched last: start the copies of the next one
+            int nti = pti, nc = pc + WARPS;
+            next_chunk(nti, nc);
+            if (nti < num_tiles) issue(nti, nc, buf ^ 1);
             cp_async_commit();
-            if (rn + RPP < row_end) fetch_meta(rn + RPP);
-            cp_async_wait1();  // this row's copies have landed (only the newest group may be pending)
-            P const xr = *slot_of(st, 0);
-            P yo;
-            if (!INIT) yo = *slot_of(st, 1);
-            V sum[E], lo[E];
-#pragma unroll
-            for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(lo[e]); }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (q >= W) continue;
-                P const xv = *slot_of(st, 2 + q);
-#pragma unroll
-                for (int e = 0; e < E; ++e) vfma(sum[e], vc[q * VS], xv.v[e]);
-                if (VS == 2) {
-#pragma unroll
-                    for (int e = 0; e < E; ++e) vfma(lo[e], vc[q * VS + 1], xv.v[e]);
-                }
-            }
-            P yn;
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
-                yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
-                m2[e] += vsq(xr.v[e]);
-                m3r[e] += vdre(yn.v[e], xr.v[e]);
-                if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
-            }
-            st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) cc[q] = cnn[q];
-#pragma unroll
-            for (int i = 0; i < 4 * VS; ++i) vc[i] = vnn[i];
-        }
-        asm volatile("cp.async.wait_all;" ::: "memory");
-    }
-    if (cur_sys >= 0)
-        diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
-}
-
-template<class V, int E, int LPR>
-cudaError_t diag_async_launch(DiagStep const& a, cudaStream_t s) {
-    if (a.num_tiles == 0) return cudaSuccess;
-    if (a.W > 4) return cudaErrorInvalidValue;
-    size_t const smem = diag_async_smem<V, E, LPR>();
-    auto fn = a.init ? diag_async_kernel<V, E, LPR, true> : diag_async_kernel<V, E, LPR, false>;
-    static void const* done[16];
-    static int ndone = 0;
-    std::lock_guard<std::mutex> lock(g_launch_cache_mutex);
-    bool set = false;
-    for (int i = 0; i < ndone; ++i) set = set || done[i] == reinterpret_cast<void const*>(fn);
-    if (!set) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-        if (ndone < 16) done[ndone++] = reinterpret_cast<void const*>(fn);
-    }
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, BLOCK, smem) != cudaSuccess || occ < 1) {
-        cudaGetLastError();
-        return cudaErrorInvalidConfiguration;
-    }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int const g = std::max(1, std::min(a.num_tiles, sms * occ));
-    fn<<<g, BLOCK, smem, s>>>(a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x), static_cast<V*>(a.y),
-                              a.batch_stride, a.tiles, a.num_tiles, a.nbatch, a.acc);
-    return cudaGetLastError();
-}
-
-// ------------------------------------------------------------------ diagonal step, TMA-staged
-// The contiguous operands of a tile (its y_old rows, its own x rows for the moment dots,
-// and its ELL indices and values) are prefetched into shared memory by bulk copies, up to
-// TMA_STAGES tiles ahead of the consumers (one producer warp, a ring of stages, full/empty
-// mbarriers). The consumer warps only gather the neighbour x rows from global memory (L2)
-// and stream y_new out. Bulk copies keep far more bytes in flight per SM than register
-// loads, which is what this latency-bound step lacks. Starts of the index and value
-// copies are aligned down to 16 bytes (the consumer skips the lead-in), sizes rounded up
-// (the matrix arrays carry tail padding for that).
-constexpr int TMA_THREADS = 512;
-constexpr int TMA_CONSUMERS = TMA_THREADS - 32;
-constexpr int TMA_STAGES = 3;
-
-struct TmaLayout {
-    uint32_t y, x, col, val, stage;
-};
-__host__ __device__ inline TmaLayout tma_layout(int TR, int K, int vb, int W, int VS) {
-    auto up = [](uint32_t v) { return (v + 127u) & ~127u; };
-    TmaLayout L;
-    L.y = 0;
-    L.x = up(static_cast<uint32_t>(TR * K * vb));
-    L.col = L.x + up(static_cast<uint32_t>(TR * K * vb));
-    L.val = L.col + up(static_cast<uint32_t>(TR * W * 4 + 32));
-    L.stage = L.val + up(static_cast<uint32_t>(TR * W * VS * vb + 32));
-    return L;
-}
-
-template<class V, int E, int LPR>
-size_t diag_tma_smem(int TR, int W) {
-    using R = typename Tr<V>::R;
-    constexpr int NV = Tr<V>::C ? 3 : 2;
-    TmaLayout const L = tma_layout(TR, E * LPR, sizeof(V), W, Tr<V>::VS);
-    return static_cast<size_t>(TMA_STAGES) * L.stage + 2 * TMA_STAGES * sizeof(uint64_t) +
-           sizeof(R) * (TMA_CONSUMERS / 32) * E * LPR * NV + 128;
-}
-
-template<class V, int E, int LPR>
-__device__ __forceinline__ void tma_flush(typename Tr<V>::R (&m2)[E], typename Tr<V>::R (&m3r)[E],
-                                          typename Tr<V>::R (&m3i)[E], typename Tr<V>::R* red, double* a, bool live) {
-    using R = typename Tr<V>::R;
-    constexpr bool CPLX = Tr<V>::C;
-    constexpr int K = E * LPR;
-    constexpr int NV = CPLX ? 3 : 2;
-    constexpr int CW = TMA_CONSUMERS / 32;
-#pragma unroll
-    for (int off = LPR; off < 32; off <<= 1) {
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            m2[e] += __shfl_xor_sync(0xffffffffu, m2[e], off);
-            m3r[e] += __shfl_xor_sync(0xffffffffu, m3r[e], off);
-            if (CPLX) m3i[e] += __shfl_xor_sync(0xffffffffu, m3i[e], off);
-        }
-    }
-    int const ct = threadIdx.x - 32;
-    int const cw = ct / 32, wl = ct % 32;
-    asm volatile("bar.sync 1, %0;" ::"n"(TMA_CONSUMERS) : "memory");  // the previous flush has read `red`
-    if (wl < LPR) {
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            R* rw = red + (cw * K + wl * E + e) * NV;
-            rw[0] = m2[e];
-            rw[1] = m3r[e];
-            if (CPLX) rw[NV - 1] = m3i[e];
-        }
-    }
-    asm volatile("bar.sync 1, %0;" ::"n"(TMA_CONSUMERS) : "memory");
-    if (live)
-        for (int i = ct; i < K * NV; i += TMA_CONSUMERS) {
-            R sum = R(0);
-#pragma unroll
-            for (int w = 0; w < CW; ++w) sum += red[w * K * NV + i];
-            atomicAdd(a + i, static_cast<double>(sum));
-        }
-#pragma unroll
-    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
-}
-
-template<class V, int E, int LPR, bool INIT>
-__global__ void __launch_bounds__(TMA_THREADS, 2)
-diag_tma_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x_all,
-                V* __restrict__ y_all, int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles, int nbatch,
-                double* __restrict__ acc, int TR, int* __restrict__ err) {
-    using R = typename Tr<V>::R;
-    using P = Pack<V, E>;
-    constexpr bool CPLX = Tr<V>::C;
-    constexpr int K = E * LPR;
-    constexpr int VS = Tr<V>::VS;
-    constexpr int NV = CPLX ? 3 : 2;
-    constexpr int RPP = TMA_CONSUMERS / LPR;
-    extern __shared__ unsigned char smem_raw[];
-    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t{127});
-    TmaLayout const L = tma_layout(TR, K, sizeof(V), W, VS);
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + TMA_STAGES * L.stage);
-    uint64_t* empty = full + TMA_STAGES;
-    R* red = reinterpret_cast<R*>(empty + TMA_STAGES);
-    int const G = gridDim.x;
-    int const my_tiles = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + G - 1) / G : 0;
-    int const warp = threadIdx.x / 32;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < TMA_STAGES; ++s) {
-            async::mbar_init(full + s, 1);
-            async::mbar_init(empty + s, TMA_CONSUMERS / 32);
-        }
-        async::mbar_init_fence();
-    }
-    __syncthreads();
-
-    if (warp == 0) {
-        if (threadIdx.x == 0) {  // producer
-            int issued = 0;
-            for (int i = 0; i < my_tiles; ++i) {
-                int const s = i % TMA_STAGES, use = i / TMA_STAGES;
-                if (use > 0 && !async::mbar_wait(empty + s, (use - 1) & 1, err)) break;
-                Tile const t = tiles[blockIdx.x + i * G];
-                int const rows = t.row_end - t.row_begin;
-                unsigned char* st = sm + s * L.stage;
-                uint32_t const vbytes = static_cast<uint32_t>(rows) * K * sizeof(V);
-                auto const* cb = reinterpret_cast<unsigned char const*>(col + static_cast<int64_t>(t.row_begin) * W);
-                auto const* ce = reinterpret_cast<unsigned char const*>(col + static_cast<int64_t>(t.row_end) * W);
-                auto const* c0 = reinterpret_cast<unsigned char const*>(reinterpret_cast<uintptr_t>(cb) & ~uintptr_t{15});
-                uint32_t const cbytes = static_cast<uint32_t>(((ce - c0) + 15) & ~15);
-                auto const* vb = reinterpret_cast<unsigned char const*>(val + static_cast<int64_t>(t.row_begin) * W * VS);
-                auto const* ve = reinterpret_cast<unsigned char const*>(val + static_cast<int64_t>(t.row_end) * W * VS);
-                auto const* v0 = reinterpret_cast<unsigned char const*>(reinterpret_cast<uintptr_t>(vb) & ~uintptr_t{15});
-                uint32_t const valbytes = static_cast<uint32_t>(((ve - v0) + 15) & ~15);
-                int64_t const vo = t.batch * batch_stride + static_cast<int64_t>(t.row_begin) * K;
-                async::mbar_expect_tx(full + s, (INIT ? 0u : vbytes) + vbytes + cbytes + valbytes);
-                if (!INIT) async::bulk_load(st + L.y, y_all + vo, vbytes, full + s);
-                async::bulk_load(st + L.x, x_all + vo, vbytes, full + s);
-                async::bulk_load(st + L.col, c0, cbytes, full + s);
-                async::bulk_load(st + L.val, v0, valbytes, full + s);
-                issued = i + 1;
-            }
-            // copies still in flight land before the block exits (already true without an error)
-            for (int i = issued - TMA_STAGES < 0 ? 0 : issued - TMA_STAGES; i < issued; ++i)
-                async::mbar_drain(full + i % TMA_STAGES, (i / TMA_STAGES) & 1, err);
-        }
-        return;
-    }
-
-    // consumers: every one of them runs the same sequence of flushes (named barriers), also
-    // after an error, in which case the rows are skipped
-    int const ct = threadIdx.x - 32;
-    int const lane = ct % LPR;
-    int const slot = ct / LPR;
-    R m2[E], m3r[E], m3i[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
-    int cur_sys = -1, cur_batch = -1;
-    bool ok = true;
-    for (int i = 0; i < my_tiles; ++i) {
-        int const s = i % TMA_STAGES, use = i / TMA_STAGES;
-        Tile const t = tiles[blockIdx.x + i * G];
-        if (t.system != cur_sys || t.batch != cur_batch) {
-            if (cur_sys >= 0)
-                tma_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV, ok);
-            cur_sys = t.system;
-            cur_batch = t.batch;
-        }
-        ok = ok && async::mbar_wait_warp(full + s, use & 1, err);
-        if (ok) {
-            unsigned char const* st = sm + s * L.stage;
-            V const* ys = reinterpret_cast<V const*>(st + L.y);
-            V const* xs = reinterpret_cast<V const*>(st + L.x);
-            uintptr_t const cb = reinterpret_cast<uintptr_t>(col + static_cast<int64_t>(t.row_begin) * W);
-            int32_t const* cs = reinterpret_cast<int32_t const*>(st + L.col + (cb & 15));
-            uintptr_t const vb = reinterpret_cast<uintptr_t>(val + static_cast<int64_t>(t.row_begin) * W * VS);
-            V const* vs = reinterpret_cast<V const*>(st + L.val + (vb & 15));
-            V const* __restrict__ x = x_all + t.batch * batch_stride;
-            V* __restrict__ y = y_all + t.batch * batch_stride;
-            int const rows = t.row_end - t.row_begin;
-            for (int lr = slot; lr < rows; lr += RPP) {
-                P const xr = reinterpret_cast<P const*>(xs + static_cast<int64_t>(lr) * K)[lane];
+            cp_async_wait_prior();  // every group but the newest is complete: this chunk's entries
+            __syncwarp();
+            int32_t const* const scol = reinterpret_cast<int32_t const*>(wbuf + buf * buf_words);
+            MV const* const sval = reinterpret_cast<MV const*>(wbuf + buf * buf_words + col_words);
+            int const cb = t.row_begin + c * CR;
+            int const ce = min(cb + CR, row_end);
+#pragma unroll 1
+            for (int lr0 = 0; lr0 < CR; lr0 += RPW) {
+                int const lr = lr0 + sub;
+                int const r = cb + lr;
+                if (r >= ce) continue;
+                P const* xp = reinterpret_cast<P const*>(x + static_cast<int64_t>(r) * K) + lane;
+                P const xr = ld_ro(xp);
                 P yo;
-                if (!INIT) yo = reinterpret_cast<P const*>(ys + static_cast<int64_t>(lr) * K)[lane];
+                if (!INIT) yo = ld_stream(reinterpret_cast<P const*>(y + static_cast<int64_t>(r) * K) + lane);
                 V sum[E], lo[E];
 #pragma unroll
                 for (int e = 0; e < E; ++e) { vzero(sum[e]); vzero(lo[e]); }
+                int32_t const* crow = scol + lr * W;
+                MV const* vrow = sval + lr * W * VS;
                 for (int j0 = 0; j0 < W; j0 += 4) {
-                    int32_t c[4];
                     P xv[4];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) c[q] = j0 + q < W ? cs[lr * W + j0 + q] : 0;
-#pragma unroll
                     for (int q = 0; q < 4; ++q)
-                        if (j0 + q < W) xv[q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[q]) * K) + lane);
+                        if (j0 + q < W)
+                            xv[q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(crow[j0 + q]) * K) + lane);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         if (j0 + q >= W) continue;
-                        V const* vp = vs + (lr * W + j0 + q) * VS;
-                        V const a = vp[0];
+                        MV const a = vrow[(j0 + q) * VS];
 #pragma unroll
                         for (int e = 0; e < E; ++e) vfma(sum[e], a, xv[q].v[e]);
                         if (VS == 2) {
-                            V const b = vp[1];
+                            MV const bl = vrow[(j0 + q) * VS + 1];
 #pragma unroll
-                            for (int e = 0; e < E; ++e) vfma(lo[e], b, xv[q].v[e]);
+                            for (int e = 0; e < E; ++e) vfma(lo[e], bl, xv[q].v[e]);
                         }
                     }
                 }
@@ -814,301 +493,25 @@ diag_tma_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
                 for (int e = 0; e < E; ++e) {
                     V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
                     yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
+                }
+                st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
                     m2[e] += vsq(xr.v[e]);
                     m3r[e] += vdre(yn.v[e], xr.v[e]);
                     if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
                 }
-                st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(t.row_begin + lr) * K) + lane, yn);
             }
+            __syncwarp();  // the buffer is refilled two chunks later
+            pti = nti;
+            pc = nc;
+            buf ^= 1;
         }
-        __syncwarp();
-        if ((ct % 32) == 0) async::mbar_arrive(empty + s);
     }
+    cp_async_commit();
+    asm volatile("cp.async.wait_group 0;" ::: "memory");  // nothing may land after the block exits
     if (cur_sys >= 0)
-        tma_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV, ok);
-}
-
-template<class V, int E, int LPR>
-cudaError_t diag_tma_launch(DiagStep const& a, cudaStream_t s) {
-    if (a.num_tiles == 0) return cudaSuccess;
-    if (a.error == nullptr || a.tma_rows < 1 || (E * LPR * sizeof(V)) % 16 != 0) return cudaErrorInvalidValue;
-    size_t const smem = diag_tma_smem<V, E, LPR>(a.tma_rows, a.W);
-    auto fn = a.init ? diag_tma_kernel<V, E, LPR, true> : diag_tma_kernel<V, E, LPR, false>;
-    // one attribute set and occupancy query per (kernel, shared size)
-    static void const* done_fn[32];
-    static size_t done_smem[32];
-    static int done_occ[32];
-    static int ndone = 0;
-    std::unique_lock<std::mutex> lock(g_launch_cache_mutex);
-    int occ = 0;
-    for (int i = 0; i < ndone; ++i)
-        if (done_fn[i] == reinterpret_cast<void const*>(fn) && done_smem[i] == smem) occ = done_occ[i];
-    if (occ == 0) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, TMA_THREADS, smem) != cudaSuccess || occ < 1) {
-            cudaGetLastError();
-            return cudaErrorInvalidConfiguration;
-        }
-        if (ndone < 32) {
-            done_fn[ndone] = reinterpret_cast<void const*>(fn);
-            done_smem[ndone] = smem;
-            done_occ[ndone] = occ;
-            ++ndone;
-        }
-    }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int const g = std::max(1, std::min(a.num_tiles, sms * occ));
-    fn<<<g, TMA_THREADS, smem, s>>>(a.col, static_cast<V const*>(a.val), a.W, static_cast<V const*>(a.x),
-                                    static_cast<V*>(a.y), a.batch_stride, a.tiles, a.num_tiles, a.nbatch, a.acc,
-                                    a.tma_rows, a.error);
-    return cudaGetLastError();
-}
-
-// ------------------------------------------------------------------ diagonal step, TMA gathers
-// The TMA-staged step with the neighbour rows gathered by the tensor memory accelerator
-// too: for each row the producer warp reads the row's column indices and issues one
-// cp.async.bulk.tensor tile::gather4 per four entries, which copies those four x rows
-// (K FP32 values each) into shared memory. The consumer warps then read every operand of a
-// row from shared memory and only store y_new to global memory, so a row costs no
-// dependent global round trip on the consumers, and the copies in flight per SM are bounded
-// by the stages, not by registers. FP32 recursions (E = 4, K = 4 LPR <= 256), full rows.
-// Measured on the 32-flake FP32 workload: 4.19 ms per step against 1.32 ms for register
-// loads, and the same with the next tile's indices prefetched: one gather4 per row takes
-// ~160 SM cycles of TMA issue. So it is not among the options timed on a first call;
-// staging = 4 selects it.
-constexpr int GTH_STAGES = 3;
-
-struct GatherLayout {
-    uint32_t y, x, g, val, stage;
-};
-__host__ __device__ inline GatherLayout gather_layout(int TR, int K, int W) {
-    auto up = [](uint32_t v) { return (v + 127u) & ~127u; };
-    int const NG = (W + 3) / 4;
-    GatherLayout L;
-    L.y = 0;
-    L.x = up(static_cast<uint32_t>(TR * K * 4));
-    L.g = L.x + up(static_cast<uint32_t>(TR * K * 4));
-    L.val = L.g + up(static_cast<uint32_t>(TR * NG * 4 * K * 4));
-    L.stage = L.val + up(static_cast<uint32_t>(TR * W * 2 * 4 + 32));
-    return L;
-}
-
-size_t diag_gather_smem(int TR, int K, int W) {
-    GatherLayout const L = gather_layout(TR, K, W);
-    return static_cast<size_t>(GTH_STAGES) * L.stage + 2 * GTH_STAGES * sizeof(uint64_t) +
-           sizeof(float) * (TMA_CONSUMERS / 32) * K * 2 + 128;
-}
-
-// Four rows y0..y3 (box {K, 1} of a 2D map [rows][K]) from column x into dst, in that order.
-__device__ __forceinline__ void tma_gather4(void* dst, CUtensorMap const* map, uint64_t* bar, int x, int y0, int y1,
-                                            int y2, int y3) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%3, %4, %5, %6, %7}], [%2];"
-        ::"r"(async::smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(async::smem_u32(bar)), "r"(x),
-          "r"(y0), "r"(y1), "r"(y2), "r"(y3)
-        : "memory");
-}
-
-template<int E, int LPR, bool INIT>
-__global__ void __launch_bounds__(TMA_THREADS, 1)
-diag_gather_kernel(const __grid_constant__ CUtensorMap xmap, int32_t const* __restrict__ col,
-                   float const* __restrict__ val, int W, float const* __restrict__ x_all, float* __restrict__ y_all,
-                   int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles, int nbatch,
-                   double* __restrict__ acc, int TR, int* __restrict__ err) {
-    using V = float;
-    using R = float;
-    using P = Pack<V, E>;
-    constexpr int K = E * LPR;
-    constexpr int NV = 2;
-    constexpr int RPP = TMA_CONSUMERS / LPR;
-    extern __shared__ unsigned char smem_raw[];
-    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t{127});
-    GatherLayout const L = gather_layout(TR, K, W);
-    int const NG = (W + 3) / 4;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + GTH_STAGES * L.stage);
-    uint64_t* empty = full + GTH_STAGES;
-    R* red = reinterpret_cast<R*>(empty + GTH_STAGES);
-    int const G = gridDim.x;
-    int const my_tiles = blockIdx.x < num_tiles ? (num_tiles - blockIdx.x + G - 1) / G : 0;
-    int const warp = threadIdx.x / 32;
-    int64_t const rows_total = batch_stride / K;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < GTH_STAGES; ++s) {
-            async::mbar_init(full + s, 1);
-            async::mbar_init(empty + s, TMA_CONSUMERS / 32);
-        }
-        async::mbar_init_fence();
-    }
-    __syncthreads();
-
-    if (warp == 0) {  // producer warp: lane 0 the contiguous copies, every lane gathers rows
-        int const ln = threadIdx.x;
-        int issued = 0;
-        for (int i = 0; i < my_tiles; ++i) {
-            int const s = i % GTH_STAGES, use = i / GTH_STAGES;
-            if (use > 0 && !async::mbar_wait_warp(empty + s, (use - 1) & 1, err)) break;
-            Tile const t = tiles[blockIdx.x + i * G];
-            int const rows = t.row_end - t.row_begin;
-            unsigned char* st = sm + s * L.stage;
-            uint32_t const vbytes = static_cast<uint32_t>(rows) * K * 4;
-            uint32_t const gbytes = static_cast<uint32_t>(rows) * NG * 4 * K * 4;
-            auto const* vb = reinterpret_cast<unsigned char const*>(val + static_cast<int64_t>(t.row_begin) * W * 2);
-            auto const* ve = reinterpret_cast<unsigned char const*>(val + static_cast<int64_t>(t.row_end) * W * 2);
-            auto const* v0 = reinterpret_cast<unsigned char const*>(reinterpret_cast<uintptr_t>(vb) & ~uintptr_t{15});
-            uint32_t const valbytes = static_cast<uint32_t>(((ve - v0) + 15) & ~15);
-            int64_t const vo = t.batch * batch_stride + static_cast<int64_t>(t.row_begin) * K;
-            if (ln == 0) {
-                async::mbar_expect_tx(full + s, (INIT ? 0u : vbytes) + vbytes + gbytes + valbytes);
-                if (!INIT) async::bulk_load(st + L.y, y_all + vo, vbytes, full + s);
-                async::bulk_load(st + L.x, x_all + vo, vbytes, full + s);
-                async::bulk_load(st + L.val, v0, valbytes, full + s);
-            }
-            __syncwarp();
-            int const ybase = static_cast<int>(t.batch * rows_total);
-            for (int lr = ln; lr < rows; lr += 32) {
-                int const r = t.row_begin + lr;
-                int32_t const* cr = col + static_cast<int64_t>(r) * W;
-                for (int gi = 0; gi < NG; ++gi) {
-                    int c[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) c[q] = gi * 4 + q < W ? __ldg(cr + gi * 4 + q) : r;
-                    tma_gather4(st + L.g + static_cast<uint32_t>((lr * NG + gi) * 4 * K * 4), &xmap, full + s, 0,
-                                ybase + c[0], ybase + c[1], ybase + c[2], ybase + c[3]);
-                }
-            }
-            issued = i + 1;
-        }
-        // copies still in flight land before the block exits
-        if (ln == 0)
-            for (int i = issued - GTH_STAGES < 0 ? 0 : issued - GTH_STAGES; i < issued; ++i)
-                async::mbar_drain(full + i % GTH_STAGES, (i / GTH_STAGES) & 1, err);
-        return;
-    }
-
-    int const ct = threadIdx.x - 32;
-    int const lane = ct % LPR;
-    int const slot = ct / LPR;
-    R m2[E], m3r[E], m3i[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
-    int cur_sys = -1, cur_batch = -1;
-    bool ok = true;
-    for (int i = 0; i < my_tiles; ++i) {
-        int const s = i % GTH_STAGES, use = i / GTH_STAGES;
-        Tile const t = tiles[blockIdx.x + i * G];
-        if (t.system != cur_sys || t.batch != cur_batch) {
-            if (cur_sys >= 0)
-                tma_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV, ok);
-            cur_sys = t.system;
-            cur_batch = t.batch;
-        }
-        ok = ok && async::mbar_wait_warp(full + s, use & 1, err);
-        if (ok) {
-            unsigned char const* st = sm + s * L.stage;
-            P const* ys = reinterpret_cast<P const*>(st + L.y);
-            P const* xs = reinterpret_cast<P const*>(st + L.x);
-            P const* gs = reinterpret_cast<P const*>(st + L.g);
-            uintptr_t const vb = reinterpret_cast<uintptr_t>(val + static_cast<int64_t>(t.row_begin) * W * 2);
-            float const* vs = reinterpret_cast<float const*>(st + L.val + (vb & 15));
-            float* __restrict__ y = y_all + t.batch * batch_stride;
-            int const rows = t.row_end - t.row_begin;
-            for (int lr = slot; lr < rows; lr += RPP) {
-                P const xr = xs[lr * LPR + lane];
-                P yo;
-                if (!INIT) yo = ys[lr * LPR + lane];
-                V sum[E], lo[E];
-#pragma unroll
-                for (int e = 0; e < E; ++e) { sum[e] = 0.f; lo[e] = 0.f; }
-                for (int j = 0; j < W; ++j) {
-                    P const xv = gs[(lr * NG * 4 + j) * LPR + lane];
-                    float const a = vs[(lr * W + j) * 2];
-                    float const b = vs[(lr * W + j) * 2 + 1];
-#pragma unroll
-                    for (int e = 0; e < E; ++e) {
-                        vfma(sum[e], a, xv.v[e]);
-                        vfma(lo[e], b, xv.v[e]);
-                    }
-                }
-                P yn;
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    V const sv = vadd(sum[e], lo[e]);
-                    yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
-                    m2[e] += vsq(xr.v[e]);
-                    m3r[e] += vdre(yn.v[e], xr.v[e]);
-                }
-                st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(t.row_begin + lr) * K) + lane, yn);
-            }
-        }
-        __syncwarp();
-        if ((ct % 32) == 0) async::mbar_arrive(empty + s);
-    }
-    if (cur_sys >= 0)
-        tma_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV, ok);
-}
-
-PFN_cuTensorMapEncodeTiled_v12000 rows_encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 const fn = [] {  // thread-safe one-time lookup
-        cudaDriverEntryPointQueryResult q;
-        void* p = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
-    }();
-    return fn;
-}
-
-template<int E, int LPR>
-cudaError_t diag_gather_launch(DiagStep const& a, cudaStream_t s) {
-    constexpr int K = E * LPR;
-    if (a.num_tiles == 0) return cudaSuccess;
-    if (a.error == nullptr || a.gather_rows < 1 || K > 256 || a.W < 1) return cudaErrorInvalidValue;
-    int64_t const rows_total = a.batch_stride / K;
-    int64_t const all_rows = rows_total * a.nbatch;
-    if (all_rows > (int64_t{1} << 31) - 1 || (reinterpret_cast<uintptr_t>(a.x) & 15) != 0) return cudaErrorInvalidValue;
-    auto enc = rows_encode_fn();
-    if (!enc) return cudaErrorInvalidValue;
-    CUtensorMap map;
-    cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(all_rows)};
-    cuuint64_t strides[1] = {static_cast<cuuint64_t>(K) * sizeof(float)};
-    cuuint32_t box[2] = {static_cast<cuuint32_t>(K), 1};  // gather4: one row per coordinate
-    cuuint32_t estr[2] = {1, 1};
-    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(a.x), dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return cudaErrorInvalidValue;
-    size_t const smem = diag_gather_smem(a.gather_rows, K, a.W);
-    auto fn = a.init ? diag_gather_kernel<E, LPR, true> : diag_gather_kernel<E, LPR, false>;
-    // the shared-memory limit is raised once per kernel to the largest size asked for
-    static void const* set_fn[16];
-    static size_t set_smem[16];
-    static int nset = 0;
-    std::unique_lock<std::mutex> lock(g_launch_cache_mutex);
-    int k = 0;
-    while (k < nset && set_fn[k] != reinterpret_cast<void const*>(fn)) ++k;
-    if (k == nset || set_smem[k] < smem) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-        if (k == nset && nset < 16) ++nset;
-        if (k < 16) {
-            set_fn[k] = reinterpret_cast<void const*>(fn);
-            set_smem[k] = smem;
-        }
-    }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int const g = std::max(1, std::min(a.num_tiles, sms));
-    fn<<<g, TMA_THREADS, smem, s>>>(map, a.col, static_cast<float const*>(a.val), a.W, static_cast<float const*>(a.x),
-                                    static_cast<float*>(a.y), a.batch_stride, a.tiles, a.num_tiles, a.nbatch, a.acc,
-                                    a.gather_rows, a.error);
-    return cudaGetLastError();
+        diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
 }
 
 // ------------------------------------------------------------------ off-diagonal step
@@ -1196,7 +599,7 @@ off_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 }
 
 // ------------------------------------------------------------------ dense collection step
-int persistent_grid(void const* fn, int num_tiles);
+int persistent_grid(void const* fn, int num_tiles, size_t smem = 0);
 
 // One row of y <- H~ x - y (or H~ x / 2) for this lane's E vectors and the collected vector
 // of the row: x[r] (left side) or V x at row r (right side, V = val2 on the pattern of H~).
@@ -1311,14 +714,17 @@ cudaError_t dense_launch(DenseStep const& a, cudaStream_t s) {
 //   gt[r][j] += sum over the K vectors of x[col_j] * g[r]
 // (the gradient of the recursion with respect to the transposed entry S[col_j][r]; the
 // pattern of S is symmetric) and gd[r] += sum_k x[r][k] * g[r][k] (the diagonal, also where
-// S stores none). The row loop is uniform over the block so that the lanes of a row can
-// reduce with warp shuffles.
+// S stores none). The per-step sum over the K vectors of a row is taken in the vectors'
+// precision; gt and gd accumulate those over the steps in FP64 (one add per entry and step:
+// an FP32 running sum over M/2 steps of terms of both signs lost ~1e-4 of the largest
+// gradient). The row loop is uniform over the block so that the lanes of a row can reduce
+// with warp shuffles.
 template<class V, int E, int LPR>
 __global__ void __launch_bounds__(BLOCK)
 adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x,
                 V const* yprev, V* out, int half, V const* __restrict__ v0, V const* __restrict__ vm,
-                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, V* __restrict__ gt,
-                V* __restrict__ gd, Tile const* __restrict__ tiles, int num_tiles) {
+                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, double* __restrict__ gt,
+                double* __restrict__ gd, Tile const* __restrict__ tiles, int num_tiles) {
     static_assert(!Tr<V>::C, "the adjoint step is real");
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;
@@ -1327,9 +733,9 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
     int const lane = threadIdx.x % LPR;
     int const slot = threadIdx.x / LPR;
     bool const grad = gt != nullptr;
-    // gradient sums (the recursion's precision): with fewer entries per row than lanes, lane j
-    // owns slot j and lane W the diagonal; their old values are loaded with the row's other
-    // loads, so no dependent read-modify-write ends the row
+    // gradient sums (FP64): with fewer entries per row than lanes, lane j owns slot j and lane W
+    // the diagonal; their old values are loaded with the row's other loads, so no dependent
+    // read-modify-write ends the row
     bool const spread = grad && W < LPR;
     for (int ti = blockIdx.x; ti < num_tiles; ti += gridDim.x) {  // uniform over the block
         Tile const t = tiles[ti];
@@ -1339,7 +745,7 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
             int const rs = live ? r : t.row_begin;  // dead lanes follow a valid row without storing
             int64_t const off = static_cast<int64_t>(rs) * K;
             P gv, yo, q0;
-            V gpre = V(0), gsum = V(0);
+            double gpre = 0.0, gsum = 0.0;
             if (spread && live) {
                 if (lane < W) gpre = gt[static_cast<int64_t>(r) * W + lane];
                 else if (lane == W) gpre = gd[r];
@@ -1355,9 +761,9 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 #pragma unroll
                 for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
                 if (spread) {
-                    if (lane == W) gsum += p;
+                    if (lane == W) gsum += static_cast<double>(p);
                 } else if (live && lane == 0) {
-                    gd[r] += p;
+                    gd[r] += static_cast<double>(p);
                 }
             }
             V sum[E], lo[E];
@@ -1390,9 +796,9 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 #pragma unroll
                         for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
                         if (spread) {
-                            if (lane == j0 + q) gsum += p;
+                            if (lane == j0 + q) gsum += static_cast<double>(p);
                         } else if (live && lane == 0) {
-                            gt[static_cast<int64_t>(r) * W + j0 + q] += p;
+                            gt[static_cast<int64_t>(r) * W + j0 + q] += static_cast<double>(p);
                         }
                     }
                 }
@@ -1435,7 +841,7 @@ cudaError_t adj_launch(AdjStep const& a, cudaStream_t s) {
                               static_cast<V const*>(a.yprev), static_cast<V*>(a.out), a.half ? 1 : 0,
                               static_cast<V const*>(a.v0), static_cast<V const*>(a.vm), static_cast<V const*>(a.vp),
                               static_cast<V>(a.a0), static_cast<V>(a.am), static_cast<V>(a.ap),
-                              static_cast<V const*>(a.g), static_cast<V*>(a.gt), static_cast<V*>(a.gd), a.tiles,
+                              static_cast<V const*>(a.g), static_cast<double*>(a.gt), static_cast<double*>(a.gd), a.tiles,
                               a.num_tiles);
     return cudaGetLastError();
 }
@@ -1593,7 +999,7 @@ __global__ void kubo_integrate_kernel(double const* __restrict__ sum_nm, double 
     out[2 * j + 1] = prefix * coeff * ti;
 }
 
-int persistent_grid(void const* fn, int num_tiles) {
+int persistent_grid(void const* fn, int num_tiles, size_t smem) {
     constexpr int kMaxDevices = 64;
     static int sms_of[kMaxDevices] = {};
     int dev = 0;
@@ -1606,19 +1012,48 @@ int persistent_grid(void const* fn, int num_tiles) {
     }
     // occupancy per kernel, queried once (the recursion launches the same kernels thousands of times)
     static void const* fns[64];
+    static size_t smems[64];
     static int occ[64];
     static int nfns = 0;
     int per_sm = 0;
     for (int i = 0; i < nfns; ++i)
-        if (fns[i] == fn) per_sm = occ[i];
+        if (fns[i] == fn && smems[i] == smem) per_sm = occ[i];
     if (per_sm == 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BLOCK, 0) != cudaSuccess || per_sm < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BLOCK, smem) != cudaSuccess || per_sm < 1) {
             cudaGetLastError();
             per_sm = 1;
         }
-        if (nfns < 64) { fns[nfns] = fn; occ[nfns] = per_sm; ++nfns; }
+        if (nfns < 64) { fns[nfns] = fn; smems[nfns] = smem; occ[nfns] = per_sm; ++nfns; }
     }
     return std::max(1, std::min(num_tiles, sms * per_sm));
+}
+
+template<class V, int E, int LPR, class MV = V>
+cudaError_t diag_launch_pf(DiagStep const& a, cudaStream_t s) {
+    auto const* val = static_cast<MV const*>(a.val);
+    auto const* x = static_cast<V const*>(a.x);
+    auto* y = static_cast<V*>(a.y);
+    size_t const smem = pf_smem_bytes<MV, LPR>(a.W);
+    if (smem > PF_SMEM_MAX) return cudaErrorInvalidValue;
+    auto run = [&](auto fn) {
+        if (smem > 48 * 1024) {
+            cudaError_t const e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
+        int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles, smem);
+        fn<<<g, BLOCK, smem, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit,
+                                  a.nbatch, a.acc);
+        return cudaGetLastError();
+    };
+    // MINB: blocks per SM the register allocation is held to (3, or 4 with a few spilled words
+    // of loop state for the FP32 64-vector shape), timed by the autotuner
+    if (a.prefetch >= 4) {
+        if (a.init) return run(diag_pf_kernel<V, E, LPR, true, 4, MV>);
+        return run(diag_pf_kernel<V, E, LPR, false, 4, MV>);
+    }
+    if (a.init) return run(diag_pf_kernel<V, E, LPR, true, 3, MV>);
+    return run(diag_pf_kernel<V, E, LPR, false, 3, MV>);
 }
 
 template<class V, int E, int LPR, int U, class MV = V>
@@ -1671,7 +1106,7 @@ diag_pair_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;
     constexpr int NV = CPLX ? 3 : 2;
-    __shared__ R red[WARPS * K * NV];
+    __shared__ double red[WARPS * K * NV];
     // per-thread moment partials of both phases live in shared memory (own slot, no sync); only
     // the current item's partials are in registers, which keeps the kernel within 64 registers
     __shared__ R part[2][NV][E][BLOCK];
@@ -1792,35 +1227,17 @@ cudaError_t pair_launch(DiagPair const& a, cudaStream_t s) {
 template<class V, int E, int LPR>
 cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
     if (a.num_tiles == 0) return cudaSuccess;
-    if (a.async_copy) {
-        if (a.real_matrix || a.W > 4) return cudaErrorInvalidValue;
-        if constexpr (E * sizeof(V) == 16)
-            return diag_async_launch<V, E, LPR>(a, s);
-        else
-            return cudaErrorInvalidValue;
-    }
-    if (a.gather_rows > 0) {
-        if constexpr (std::is_same_v<V, float> && E == 4)
-            return diag_gather_launch<E, LPR>(a, s);
-        else
-            return cudaErrorInvalidValue;
-    }
-    if (a.tma_rows > 0) {
-        if (a.real_matrix) return cudaErrorInvalidValue;
-        if constexpr (E * sizeof(V) == 16 && LPR > 1)  // multi-vector rows of 16-byte lanes
-            return diag_tma_launch<V, E, LPR>(a, s);
-        else
-            return cudaErrorInvalidValue;
-    }
     if (a.real_matrix) {  // complex vectors, real H~ values: two FMAs per entry instead of four
         if constexpr (Tr<V>::C) {
             using MR = typename Tr<V>::R;
+            if (a.prefetch) return diag_launch_pf<V, E, LPR, MR>(a, s);
             if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2, MR>(a, s);
             return diag_launch_u<V, E, LPR, 1, MR>(a, s);
         } else {
             return cudaErrorInvalidValue;
         }
     }
+    if (a.prefetch) return diag_launch_pf<V, E, LPR>(a, s);
     if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2>(a, s);
     return diag_launch_u<V, E, LPR, 1>(a, s);
 }
@@ -1983,7 +1400,7 @@ template<class V>
 __global__ void __launch_bounds__(BLOCK)
 lanczos_a_kernel(int32_t const* __restrict__ ip, int32_t const* __restrict__ ix, V const* __restrict__ hv,
                  V const* __restrict__ v1, V* __restrict__ v0, Tile const* __restrict__ tiles,
-                 double const* __restrict__ nrm_prev, double* __restrict__ alpha) {
+                 double const* __restrict__ nrm_prev, double* __restrict__ part) {
     __shared__ double sh[WARPS];
     Tile const t = tiles[blockIdx.x];
     double const bp = sqrt(nrm_prev[t.system]);  // beta of the previous iteration (0 at the start)
@@ -1998,13 +1415,13 @@ lanczos_a_kernel(int32_t const* __restrict__ ip, int32_t const* __restrict__ ix,
         a += vdre(sum, v1[r]);
     }
     double const s = block_sum<V>(a, sh);
-    if (threadIdx.x == 0) atomicAdd(alpha + t.system, s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
 template<class V>
 __global__ void __launch_bounds__(BLOCK)
 lanczos_b_kernel(V const* __restrict__ v1, V* __restrict__ v0, Tile const* __restrict__ tiles,
-                 double const* __restrict__ alpha, double* __restrict__ nrm) {
+                 double const* __restrict__ alpha, double* __restrict__ part) {
     __shared__ double sh[WARPS];
     Tile const t = tiles[blockIdx.x];
     double const a = alpha[t.system];
@@ -2018,7 +1435,22 @@ lanczos_b_kernel(V const* __restrict__ v1, V* __restrict__ v0, Tile const* __res
         n2 += vsq(l);
     }
     double const s = block_sum<V>(n2, sh);
-    if (threadIdx.x == 0) atomicAdd(nrm + t.system, s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// Per-system sums of the per-tile partials of lanczos_a/b in a fixed order (a strided sum
+// per thread, then a fixed tree), so that the Lanczos coefficients, and with them the
+// spectral bounds, are the same bits on every run: the moments at high n are sensitive to
+// the bounds, and two runs must not differ by the order in which blocks finished.
+__global__ void __launch_bounds__(BLOCK)
+lanczos_reduce_kernel(double const* __restrict__ part, int32_t const* __restrict__ sys_tiles,
+                      double* __restrict__ out) {
+    __shared__ double sh[WARPS];
+    int const s = blockIdx.x;
+    double v = 0.0;
+    for (int i = sys_tiles[s] + threadIdx.x; i < sys_tiles[s + 1]; i += BLOCK) v += part[i];
+    double const tot = block_sum<double>(v, sh);
+    if (threadIdx.x == 0) out[s] = tot;
 }
 
 template<class V>
@@ -2118,6 +1550,13 @@ bool diag_shape_supported(int vtype, int E, int LPR) {
     return false;
 }
 
+bool diag_pf_supported(int vtype, int W, int LPR) {
+    int const cr = std::max(PF_ROWS, 32 / std::max(LPR, 1));
+    int const val_words = (vtype == V_C64 || vtype == V_C128) ? 4 : 2;  // per entry (hi/lo pairs for FP32)
+    size_t const buf = static_cast<size_t>((cr * W + 3) / 4) * 4 + static_cast<size_t>(cr) * W * val_words;
+    return static_cast<size_t>(WARPS) * 2 * buf * 4 <= PF_SMEM_MAX;
+}
+
 bool diag_step_supported(int vtype, int E, int LPR) {
 #define KPM_CHECK(V, e, l) if (vtype == vcode<V>() && E == e && LPR == l) return true;
     KPM_SHAPES_F32(KPM_CHECK) KPM_SHAPES_F64(KPM_CHECK) KPM_SHAPES_C64(KPM_CHECK) KPM_SHAPES_C128(KPM_CHECK)
@@ -2135,49 +1574,6 @@ cudaError_t launch_diag_pair(DiagPair const& a, cudaStream_t s) {
 
 cudaError_t launch_diag_step(DiagStep const& a, cudaStream_t s) {
 #define KPM_DISPATCH(V, e, l) if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) return diag_launch<V, e, l>(a, s);
-    KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
-    KPM_DIAG_ALT_F32(KPM_DISPATCH) KPM_DIAG_ALT_F64(KPM_DISPATCH) KPM_DIAG_ALT_C64(KPM_DISPATCH)
-#undef KPM_DISPATCH
-    return cudaErrorInvalidValue;
-}
-
-template<class V, int E, int LPR>
-cudaError_t diag_multi_launch(DiagStep const& a, void* r0, void* r1, int64_t n0, int64_t n1, double* acc_base,
-                              int64_t step_acc, unsigned* bar, int spin_limit, cudaStream_t s) {
-    if (a.num_tiles == 0 || n1 < n0) return cudaSuccess;
-    if (a.error == nullptr || bar == nullptr) return cudaErrorInvalidValue;
-    auto run = [&](auto fn, auto const* val) {
-        // every block must be resident at once: at most SMs x occupancy blocks
-        int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
-        int32_t const* col = a.col;
-        int W = a.W;
-        V* p0 = static_cast<V*>(r0);
-        V* p1 = static_cast<V*>(r1);
-        int64_t bstride = a.batch_stride;
-        Tile const* tiles = a.tiles;
-        int num_tiles = a.num_tiles, nbatch = a.nbatch;
-        int* err = a.error;
-        int spin = spin_limit;
-        void* args[] = {&col, &val, &W, &p0, &p1, &bstride, &tiles, &num_tiles, &nbatch, &acc_base, &step_acc,
-                        &n0, &n1, &bar, &err, &spin};
-        return cudaLaunchCooperativeKernel(reinterpret_cast<void const*>(fn), dim3(g), dim3(BLOCK), args, 0, s);
-    };
-    if (a.real_matrix) {
-        if constexpr (Tr<V>::C) {
-            using MR = typename Tr<V>::R;
-            return run(diag_multi_kernel<V, E, LPR, MR>, static_cast<MR const*>(a.val));
-        } else {
-            return cudaErrorInvalidValue;
-        }
-    }
-    return run(diag_multi_kernel<V, E, LPR, V>, static_cast<V const*>(a.val));
-}
-
-cudaError_t launch_diag_multi(DiagStep const& a, void* r0, void* r1, int64_t n0, int64_t n1, double* acc_base,
-                              int64_t step_acc, unsigned* bar, int spin_limit, cudaStream_t s) {
-#define KPM_DISPATCH(V, e, l) \
-    if (a.vtype == vcode<V>() && a.E == e && a.LPR == l) \
-        return diag_multi_launch<V, e, l>(a, r0, r1, n0, n1, acc_base, step_acc, bar, spin_limit, s);
     KPM_SHAPES_F32(KPM_DISPATCH) KPM_SHAPES_F64(KPM_DISPATCH) KPM_SHAPES_C64(KPM_DISPATCH) KPM_SHAPES_C128(KPM_DISPATCH)
     KPM_DIAG_ALT_F32(KPM_DISPATCH) KPM_DIAG_ALT_F64(KPM_DISPATCH) KPM_DIAG_ALT_C64(KPM_DISPATCH)
 #undef KPM_DISPATCH
@@ -2340,26 +1736,30 @@ cudaError_t launch_gather_rows(int vtype, void const* y, int32_t const* dest, in
 }
 
 cudaError_t launch_lanczos_a(bool cplx, int32_t const* ip, int32_t const* ix, void const* v, void const* v1, void* v0,
-                             Tile const* tiles, int num_tiles, double const* nrm_prev, double* alpha, cudaStream_t s) {
+                             Tile const* tiles, int num_tiles, double const* nrm_prev, double* part,
+                             int32_t const* sys_tiles, int nsys, double* alpha, cudaStream_t s) {
     if (cplx)
         lanczos_a_kernel<double2><<<num_tiles, BLOCK, 0, s>>>(ip, ix, static_cast<double2 const*>(v),
                                                               static_cast<double2 const*>(v1),
-                                                              static_cast<double2*>(v0), tiles, nrm_prev, alpha);
+                                                              static_cast<double2*>(v0), tiles, nrm_prev, part);
     else
         lanczos_a_kernel<double><<<num_tiles, BLOCK, 0, s>>>(ip, ix, static_cast<double const*>(v),
                                                              static_cast<double const*>(v1), static_cast<double*>(v0),
-                                                             tiles, nrm_prev, alpha);
+                                                             tiles, nrm_prev, part);
+    lanczos_reduce_kernel<<<nsys, BLOCK, 0, s>>>(part, sys_tiles, alpha);
     return cudaGetLastError();
 }
 
 cudaError_t launch_lanczos_b(bool cplx, void const* v1, void* v0, Tile const* tiles, int num_tiles,
-                             double const* alpha, double* nrm, cudaStream_t s) {
+                             double const* alpha, double* part, int32_t const* sys_tiles, int nsys, double* nrm,
+                             cudaStream_t s) {
     if (cplx)
         lanczos_b_kernel<double2><<<num_tiles, BLOCK, 0, s>>>(static_cast<double2 const*>(v1),
-                                                              static_cast<double2*>(v0), tiles, alpha, nrm);
+                                                              static_cast<double2*>(v0), tiles, alpha, part);
     else
         lanczos_b_kernel<double><<<num_tiles, BLOCK, 0, s>>>(static_cast<double const*>(v1), static_cast<double*>(v0),
-                                                             tiles, alpha, nrm);
+                                                             tiles, alpha, part);
+    lanczos_reduce_kernel<<<nsys, BLOCK, 0, s>>>(part, sys_tiles, nrm);
     return cudaGetLastError();
 }
 

@@ -98,10 +98,19 @@ extern "C" int kpm_moments_diag_noalloc(int32_t vector_type, int64_t rows, int32
                       tile_bytes + sum_bytes, tile_bytes, sum_bytes, kScratchBytes);
         return fail(KPM_ERR_VALUE, msg);
     }
+    auto s = static_cast<cudaStream_t>(stream);
+    if (s != nullptr) {  // the scratch address below is the current device's: the stream must be on it
+        int sdev = -1, cur = -1;
+        cudaError_t const e1 = cudaStreamGetDevice(s, &sdev);
+        cudaError_t const e2 = cudaGetDevice(&cur);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            return fail(KPM_ERR_CUDA, std::string("cannot read the stream's device: ") +
+                                          cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        if (sdev != cur) return fail(KPM_ERR_VALUE, "the stream belongs to another device than the current one");
+    }
     void* base = nullptr;
     int rc = scratch_address(&base);
     if (rc != KPM_OK) return rc;
-    auto s = static_cast<cudaStream_t>(stream);
     auto* tiles = static_cast<kpm::Tile*>(base);
     auto* sums = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + tile_bytes);
 

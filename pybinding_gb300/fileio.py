@@ -1,9 +1,11 @@
 """``pb.save`` / ``pb.load``: results in pybinding's ``.pbz`` files.
 
-A ``.pbz`` file is a gzip-compressed pickle (protocol 4); names without an extension
-get ``.pbz`` appended on save and are found with it on load
-(``pybinding/support/pickle.py:39-74``). Result classes pickle their state as
-``{"version": v, "dict": __dict__}`` (``pybinding/support/pickle.py:77-106``).
+The format: a ``.pbz`` file is one pickle (protocol 4) inside a gzip stream. A file
+name given without any extension is stored with ``.pbz`` appended, and loading a name
+that does not exist falls back to the same name with ``.pbz`` appended
+(``pybinding/support/pickle.py:39-74`` defines this behaviour). Result classes
+pickle their state as the mapping ``{"version": v, "dict": attributes}``
+(``pybinding/support/pickle.py:77-106``).
 
 Files written by pybinding load here as well: numpy arrays and plain Python data as
 they are, and pybinding's ``results.Series``, ``Sweep`` and ``NDSweep`` as this
@@ -14,54 +16,83 @@ from __future__ import annotations
 
 import gzip
 import os
-import pathlib
 import pickle
 
 __all__ = ["save", "load"]
 
-
-def _normalize(file):
-    if isinstance(file, pathlib.PurePath):
-        return str(file)
-    return file
+SUFFIX = ".pbz"
+PICKLE_PROTOCOL = 4
 
 
-def _add_extension(file):
-    if not isinstance(file, str):
-        return file
-    path = pathlib.Path(file)
-    return str(path.with_suffix(".pbz")) if not path.suffix else file
+class Versioned:
+    """Pickled state ``{"version": 0, "dict": attributes}``, the layout of pybinding's result
+    classes, so that a result saved by either package carries the same state."""
+
+    STATE_VERSION = 0
+
+    def __getstate__(self):
+        return {"version": self.STATE_VERSION, "dict": self.__dict__}
+
+    def __setstate__(self, state):
+        if "version" not in state:  # a plain attribute dictionary
+            self.__dict__.update(state)
+            return
+        if state["version"] != self.STATE_VERSION:
+            raise RuntimeError("%s pickles state version %d; this file holds version %s" % (
+                type(self).__name__, self.STATE_VERSION, state["version"]))
+        self.__dict__.update(state["dict"])
+
+
+def _is_stream(file):
+    return hasattr(file, "read") or hasattr(file, "write")
+
+
+def _target(file):
+    """The path to write: ``file`` itself, or ``file + '.pbz'`` when it has no extension."""
+    name = os.fspath(file)
+    return name if os.path.splitext(name)[1] else name + SUFFIX
+
+
+def _source(file):
+    """The path to read: ``file`` if it exists, else the ``.pbz`` name that saving it would use."""
+    name = os.fspath(file)
+    if os.path.exists(name):
+        return name
+    alt = _target(name)
+    return alt if os.path.exists(alt) else name
 
 
 def save(obj, file):
-    """Save ``obj`` to a gzip-compressed pickle; ``.pbz`` is added to a name without extension."""
-    file = _add_extension(_normalize(file))
-    with gzip.open(file, "wb") as f:
-        pickle.dump(obj, f, protocol=4)
+    """Write ``obj`` as a gzip-compressed pickle (a path or a binary file object)."""
+    if _is_stream(file):
+        with gzip.GzipFile(fileobj=file, mode="wb") as z:
+            pickle.dump(obj, z, protocol=PICKLE_PROTOCOL)
+        return
+    with gzip.GzipFile(_target(file), mode="wb") as z:
+        pickle.dump(obj, z, protocol=PICKLE_PROTOCOL)
 
 
-def _pybinding_classes():
-    from .chebyshev import Series
-    from .parallel import NDSweep, Sweep
-    return {("pybinding.results", "Series"): Series, ("pybinding.results", "Sweep"): Sweep,
-            ("pybinding.results", "NDSweep"): NDSweep}
+# pybinding's result classes, by their pickled (module, name), and this package's equivalents
+_PYBINDING_RESULTS = {"Series": ("chebyshev", "Series"), "Sweep": ("parallel", "Sweep"),
+                      "NDSweep": ("parallel", "NDSweep")}
 
 
-class _Unpickler(pickle.Unpickler):
+class _ResultUnpickler(pickle.Unpickler):
     def find_class(self, module, name):
-        if module.split(".")[0] in ("pybinding", "_pybinding"):
-            cls = _pybinding_classes().get((module, name))
-            if cls is None:
-                raise pickle.UnpicklingError("%s.%s has no counterpart in pybinding_gb300" % (module, name))
-            return cls
-        return super().find_class(module, name)
+        top = module.partition(".")[0]
+        if top not in ("pybinding", "_pybinding"):
+            return super().find_class(module, name)
+        if module == "pybinding.results" and name in _PYBINDING_RESULTS:
+            import importlib
+            sub, cls = _PYBINDING_RESULTS[name]
+            return getattr(importlib.import_module("." + sub, __package__), cls)
+        raise pickle.UnpicklingError("%s.%s has no counterpart in pybinding_gb300" % (module, name))
 
 
 def load(file):
-    """Load an object saved by :func:`save` or by pybinding's ``pb.save``."""
-    file = _normalize(file)
-    file_ext = _add_extension(file)
-    if isinstance(file, str) and not os.path.exists(file) and os.path.exists(file_ext):
-        file = file_ext
-    with gzip.open(file, "rb") as f:
-        return _Unpickler(f).load()
+    """Read an object written by :func:`save` or by pybinding's ``pb.save``."""
+    if _is_stream(file):
+        with gzip.GzipFile(fileobj=file, mode="rb") as z:
+            return _ResultUnpickler(z).load()
+    with gzip.GzipFile(_source(file), mode="rb") as z:
+        return _ResultUnpickler(z).load()

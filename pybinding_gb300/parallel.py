@@ -17,8 +17,9 @@ from copy import copy
 
 import numpy as np
 
-from . import _native
+from . import _binding
 from .chebyshev import DeferredLDOS
+from .fileio import Versioned
 
 __all__ = ["parallelize", "parallel_for", "sweep", "ndsweep", "Sweep", "NDSweep", "Factory"]
 
@@ -99,7 +100,7 @@ def _run_ldos_batch(chunk):
     first = chunk[0].impl
     t0 = time.perf_counter()
     # the jobs' own engines already hold their checked matrices: concatenate those
-    engine = _native.Engine.from_engines([d.impl.engine for d in chunk], _native.make_config(**first._cfg_args))
+    engine = _binding.engine_batch([d.impl.engine for d in chunk], first._cfg_args)
     t1 = time.perf_counter()
     try:
         out = engine.calc_ldos_batch(sites, chunk[0].energy, chunk[0].broadening)
@@ -121,24 +122,7 @@ def parallel_for(factory, make_result=None):
     return make_result(data) if make_result else data
 
 
-class _Pickleable:
-    """Pickled state in the layout of pybinding's ``@pickleable`` result classes
-    (``pybinding/support/pickle.py:77-106``), so ``.pbz`` files carry the same state either way."""
-
-    def __getstate__(self):
-        return dict(version=0, dict=self.__dict__)
-
-    def __setstate__(self, state):
-        if "version" not in state:
-            self.__dict__.update(state)
-            return
-        if state["version"] != 0:
-            raise RuntimeError("Can't create class {} v0 from incompatible data v{}".format(
-                type(self), state["version"]))
-        self.__dict__.update(state["dict"])
-
-
-class Sweep(_Pickleable):
+class Sweep(Versioned):
     """2D parameter sweep result (``pybinding/results.py:772-800``): ``data[i, j]`` at
     ``x[i]``, ``y[j]``."""
 
@@ -150,7 +134,7 @@ class Sweep(_Pickleable):
         self.tags = tags
 
 
-class NDSweep(_Pickleable):
+class NDSweep(Versioned):
     """N-dimensional sweep result (``pybinding/results.py:1027-1052``)."""
 
     def __init__(self, variables, data, labels=None, tags=None):

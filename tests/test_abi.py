@@ -174,13 +174,67 @@ def test_optimized_hamiltonian_disconnected_bit_exact(oracle):
 def test_config_fields_are_checked_on_create():
     """kpm_create rejects launch options outside their ranges before touching the GPU."""
     h = _small_h()
-    for field, bad, msg in (("staging", 5, "staging must be"), ("fuse_steps", 4, "fuse_steps must be"),
+    for field, bad, msg in (("staging", 3, "staging must be"), ("fuse_steps", 3, "fuse_steps must be"),
                             ("precision", 7, "unknown precision mode")):
         cfg = _native.make_config()
         setattr(cfg, field, bad)
         with pytest.raises(ValueError, match=msg):
             _native.Engine(h, cfg)
-    for staging in ("auto", "registers", "tma", "async", "gather"):
+    for staging in ("auto", "registers", "prefetch"):
         _native.Engine(h, _native.make_config(staging=staging)).close()
     with pytest.raises(ValueError, match="Invalid energy range"):
         _native.Engine(h, _native.make_config(energy_range=(1.0, -1.0)))
+
+
+def test_spatial_ldos_refuses_multi_orbital_models():
+    """KPM.cpp:69-71: calc_spatial_ldos raises for multi-orbital models (here a duck-typed model
+    with two Hamiltonian rows per site), before any device work."""
+    import types
+    from pybinding_gb300 import kpm
+    h = _small_h()
+    n = h.shape[0]
+    system = types.SimpleNamespace(x=np.zeros(n // 2, np.float32), y=np.zeros(n // 2, np.float32),
+                                   z=np.zeros(n // 2, np.float32), num_sites=n // 2, hamiltonian_size=n)
+    system.positions = (system.x, system.y, system.z)
+    model = types.SimpleNamespace(hamiltonian=h, system=system)
+    k = kpm(model, energy_range=(-1, 1))
+    with pytest.raises(RuntimeError, match="doesn't currently support multi-orbital models"):
+        k.calc_spatial_ldos(np.linspace(-0.5, 0.5, 3), 0.1, lambda x, y, z: np.ones(x.size, bool))
+
+
+def test_cpp_host_caller_builds_against_the_c_abi():
+    """tests/cpp/host_caller.cpp (a C++ program that calls kpm_create / kpm_moments_diag /
+    kpm_destroy through include/kpm_gb300.h) compiles and links against the library; its
+    GPU-free first check (the reference's error for min > max) passes before any device use."""
+    import subprocess
+    from pybinding_gb300 import build
+    from tests.conftest import ROOT
+    exe = build.build_host_program(os.path.join(ROOT, "tests", "cpp", "host_caller.cpp"))
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.stdout.startswith("ok: kpm_create rejects min > max"), r.stdout
+
+
+def test_pybind_module_raises_the_reference_exception_types():
+    """The pybind11 module (csrc/pykpm.cpp) over the C ABI: std::invalid_argument-like errors
+    come out as ValueError, others as RuntimeError (cppmodule/src/kpm.cpp semantics), unknown
+    configuration keys as TypeError; the host-side calls need no GPU."""
+    from pybinding_gb300 import _binding
+    h = _small_h()
+    with pytest.raises(ValueError, match="Invalid energy range"):
+        _binding.Engine(h, dict(energy_range=(1.0, -1.0)))
+    with pytest.raises(TypeError, match="unknown KPM configuration key"):
+        _binding.Engine(h, dict(colour="red"))
+    bad = h.copy()
+    bad.data[0] = np.nan
+    with pytest.raises(RuntimeError, match="invalid values: NaN or INF"):
+        _binding.Engine(bad)
+    e = _binding.Engine(h, dict(energy_range=(-2.0, 2.0), num_threads=2))
+    assert e.rows == 10 and e.num_systems == 1 and e.dtype == np.float32
+    a, b = e.scaling_factors()
+    assert a == pytest.approx(2.02, rel=1e-6) and b == 0
+    np.testing.assert_array_equal(_binding.damping_coefficients("jackson", 4.0, 7),
+                                  _native.damping_coefficients("jackson", 4.0, 7))
+    assert _binding.round_num_moments(2048) == 2050
+    e.close()
+    with pytest.raises(RuntimeError, match="closed"):
+        e.scaling_factors()

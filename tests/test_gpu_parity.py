@@ -372,41 +372,6 @@ def test_first_call_gives_the_moments_of_later_calls(dtype, nvec):
     assert err < 1e-12
 
 
-@pytest.mark.parametrize("dtype,nvec,tol", [(np.float32, 64, 1e-5), (np.float64, 16, 1e-10),
-                                            (np.complex64, 32, 1e-5), (np.complex128, 8, 1e-10)])
-def test_tma_staged_step_matches_register_step_and_oracle(oracle, dtype, nvec, tol):
-    """The TMA-staged diagonal step (bulk copies of y_old, own x rows and the ELL entries into
-    shared memory) and the cp.async-pipelined step against the register-load step and the FP64
-    oracle, on a ragged batch of three flakes whose row offsets are not multiples of 4
-    (unaligned index and value copies)."""
-    hs = [_disordered_flake(n, s, np.float64) for n, s in ((9001, 1), (4003, 2), (12007, 3))]
-    if np.iscomplexobj(np.zeros(1, dtype)):
-        hs = [(h + 1j * sp.triu(h, 1) * 0.1 - 1j * sp.tril(h, -1) * 0.1).tocsr() for h in hs]
-    hs = [h.astype(dtype) for h in hs]
-    rng = (-9.5, 9.5)
-    M = 130
-    a, b = oracle.scale(*rng)
-    starters = [oracle.random_starters(h.shape[0], nvec, dtype) for h in hs]
-    flat = np.concatenate([st.ravel() for st in starters])
-    out = {}
-    for staging in ("tma", "async", "registers"):
-        batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, staging=staging)
-        out[staging] = batch.engine.moments_diag(M, flat)
-        st = batch.engine.stats()
-        assert (st.staged_rows > 0) == (staging == "tma"), st.staged_rows
-        assert (st.staged_rows < 0) == (staging == "async"), st.staged_rows
-        out[staging + "2"] = batch.engine.moments_diag(M, flat)  # replayed recursion graph
-    for s, h in enumerate(hs):
-        h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
-        r = oracle.optimize(h64, [0], [0], a, b)
-        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(h64.dtype), r["reorder_map"]), M,
-                                  slices=r["slices"])
-        for k in ("tma", "tma2", "async", "async2", "registers", "registers2"):
-            err = rel_err(out[k][s], ref)
-            print("%s %s system %d: %.3e" % (np.dtype(dtype).name, k, s, err))
-            assert err <= tol
-
-
 @pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
 def test_complex_vectors_with_real_valued_hamiltonian(oracle, dtype, tol):
     """A real lattice stored as complex (so that random-phase starters apply, as the 60k-site
@@ -513,36 +478,6 @@ def test_conductivity_in_two_parts(oracle, gemm_mode):
         assert rel_err(parts, ref) < 1e-9
 
 
-@pytest.mark.parametrize("nvec", [64, 16, 128])
-def test_tma_gather_step_matches_register_step_and_oracle(oracle, nvec):
-    """The TMA gather step (neighbour rows copied into shared memory by tile::gather4) against
-    the register-load step and the FP64 oracle, FP32 vectors, on a ragged batch with row offsets
-    that are not multiples of 4. The vectors are computed in the same order as the register
-    step; only the per-tile FP32 moment partials differ."""
-    hs = [_disordered_flake(n, s, np.float64).astype(np.float32) for n, s in ((9001, 5), (4003, 6), (12007, 7))]
-    rng = (-9.5, 9.5)
-    M = 130
-    a, b = oracle.scale(*rng)
-    starters = [oracle.random_starters(h.shape[0], nvec, np.float32) for h in hs]
-    flat = np.concatenate([st.ravel() for st in starters])
-    out = {}
-    for staging in ("gather", "registers"):
-        batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, staging=staging)
-        out[staging] = batch.engine.moments_diag(M, flat)
-        assert (batch.engine.stats().gather_rows > 0) == (staging == "gather")
-        out[staging + "2"] = batch.engine.moments_diag(M, flat)  # replayed recursion graph
-        batch.close()
-    assert rel_err(out["gather"], out["registers"]) < 1e-6
-    for s, h in enumerate(hs):
-        r = oracle.optimize(h.astype(np.float64), [0], [0], a, b)
-        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(np.float64), r["reorder_map"]), M,
-                                  slices=r["slices"])
-        for k in ("gather", "gather2", "registers"):
-            err = rel_err(out[k][s], ref)
-            print("gather test %s system %d (K=%d): %.3e" % (k, s, nvec, err))
-            assert err <= 1e-5
-
-
 def test_engines_on_two_host_threads_agree_with_one_thread():
     """ctypes releases the GIL around engine calls: two engines driven from two host threads at
     once (shared launch caches, process-wide tuning cache) give the moments of one-by-one calls."""
@@ -572,36 +507,3 @@ def test_engines_on_two_host_threads_agree_with_one_thread():
     assert not errors, errors
     for i in range(2):
         assert rel_err(out[i], ref[i]) < 1e-12
-
-
-@pytest.mark.parametrize("dtype,nvec,tol", [(np.float64, 8, 1e-10), (np.float32, 64, 1e-5), (np.complex128, 8, 1e-10),
-                                            (np.complex64, 16, 1e-5)])
-def test_all_steps_in_one_launch_match_single_steps_and_oracle(oracle, dtype, nvec, tol):
-    """fuse_steps = 3: every step of the recursion in one cooperative launch with a grid barrier
-    between steps (systems that fit in L2), against one launch per step and the FP64 oracle, on
-    a ragged batch; the complex128 case has a real H stored complex (the real-value path)."""
-    hs = [_disordered_flake(n, 50 + i, np.float64) for i, n in enumerate((3001, 1502, 2203))]
-    hs = [h.astype(dtype) for h in hs]
-    rng = (-9.5, 9.5)
-    M = 258
-    a, b = oracle.scale(*rng)
-    starters = [oracle.random_starters(h.shape[0], nvec, dtype) for h in hs]
-    flat = np.concatenate([st.ravel() for st in starters])
-    out = {}
-    for fuse in (3, 1):
-        batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, fuse_steps=fuse)
-        out[fuse] = batch.engine.moments_diag(M, flat)
-        spl = batch.engine.stats().steps_per_launch
-        assert (spl == M // 2 - 1) == (fuse == 3), spl
-        out[fuse * 10] = batch.engine.moments_diag(M, flat)  # the second call of the same shape
-        batch.close()
-    assert rel_err(out[3], out[1]) < (1e-12 if tol < 1e-9 else 1e-6)
-    for s, h in enumerate(hs):
-        h64 = h.astype(np.complex128 if np.iscomplexobj(h.data) else np.float64)
-        r = oracle.optimize(h64, [0], [0], a, b)
-        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(h64.dtype), r["reorder_map"]), M,
-                                  slices=r["slices"])
-        for k in (3, 30, 1):
-            err = rel_err(out[k][s], ref)
-            print("one-launch test %s fuse %d system %d: %.3e" % (np.dtype(dtype).name, k, s, err))
-            assert err <= tol

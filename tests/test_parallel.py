@@ -118,17 +118,16 @@ def test_sweep_of_deferred_ldos_runs_as_one_batch(monkeypatch):
 
 
 def test_batch_engine_from_engines_checks_its_members():
-    from pybinding_gb300 import _native
-    cfg = _native.make_config()
-    a = _native.Engine(_flake(300, 1).hamiltonian, cfg)
-    b = _native.Engine(_flake(400, 2, double=True).hamiltonian, cfg)
+    from pybinding_gb300 import _binding
+    a = _binding.Engine(_flake(300, 1).hamiltonian)
+    b = _binding.Engine(_flake(400, 2, double=True).hamiltonian)
     with pytest.raises(ValueError, match="share the scalar type"):
-        _native.Engine.from_engines([a, b], cfg)
+        _binding.engine_batch([a, b])
     two = pbg.kpm_batch([_flake(300, 3), _flake(200, 4)]).engine
     with pytest.raises(ValueError, match="one system each"):
-        _native.Engine.from_engines([a, two], cfg)
-    c = _native.Engine(_flake(500, 5).hamiltonian, cfg)
-    batch = _native.Engine.from_engines([a, c], cfg)
+        _binding.engine_batch([a, two])
+    c = _binding.Engine(_flake(500, 5).hamiltonian)
+    batch = _binding.engine_batch([a, c])
     assert batch.num_systems == 2 and batch.rows == a.rows + c.rows
     np.testing.assert_array_equal(batch.system_offsets, [0, a.rows, a.rows + c.rows])
     batch.close()
@@ -136,12 +135,11 @@ def test_batch_engine_from_engines_checks_its_members():
 
 @pytest.mark.gpu
 def test_batch_engine_from_engines_matches_block_diagonal_batch():
-    from pybinding_gb300 import _native
+    from pybinding_gb300 import _binding
     models = [_flake(n, 40 + i, double=True) for i, n in enumerate((2000, 3100, 700))]
-    cfg = _native.make_config()
-    members = [_native.Engine(m.hamiltonian, cfg) for m in models]
+    members = [_binding.Engine(m.hamiltonian) for m in models]
     members[1].scaling_factors()  # bounds found by a member are kept by the batch
-    joined = _native.Engine.from_engines(members, cfg)
+    joined = _binding.engine_batch(members)
     ref = pbg.kpm_batch(models).engine
     e = np.linspace(-8, 8, 51)
     for s in range(3):
