@@ -46,6 +46,8 @@ extern "C" {
 #define KPM_PREC_AUTO 0   /* f32/c64 H: FP32 vectors + FP64 moment sums; f64/c128 H: FP64 */
 #define KPM_PREC_FP64 1   /* FP64 (f64 or c128) vectors, values and sums */
 #define KPM_PREC_FP32 2   /* FP32 (f32 or c64) vectors and values, FP64 moment sums */
+#define KPM_PREC_FP32X 3  /* as KPM_PREC_FP32, and for real H each row sum of H~ x compensated
+                             (error-free products and sums) and rounded once */
 
 /* matrix formats accepted for API compatibility (kpm/Config.hpp:7) */
 #define KPM_FORMAT_CSR 0
@@ -248,6 +250,22 @@ int kpm_kubo_bastin(kpm_engine* engine, const double* moments, int64_t num_momen
 int kpm_adjoint_diag(kpm_engine* engine, int64_t num_moments, int64_t num_vectors, const void* starters,
                      const double* dl_dmu, int64_t checkpoint, double* out_grad_values, double* out_grad_onsite,
                      int64_t* num_moments_out);
+
+/* Reverse-mode gradient of the Kubo-Bastin moments matrix (system 0; real Hamiltonians, FP64
+ * recursion). No reference counterpart: pybinding has no gradients; the forward algorithm
+ * differentiated is Core::conductivity's (cppcore/src/kpm/Core.cpp:119-145: DenseMatrixMoments
+ * of both sides and MomentMultiplication, kpm/Moments.cpp:92-155) for caller-supplied starters
+ * ([num_vectors][rows], H's scalar type, site order):
+ *   mu[m][n] = (1/R) sum_r <L_m, R_n>, L_m = T_m(H~) V_l r, R_n = V_r T_n(H~) r (row/column 0 halved),
+ * V = H o (x_i - x_j) from left/right coordinates. out_mu (nullable): mu, row-major [m][n], undamped.
+ * With dl_dmu (row-major [m][n], nullable together with out_grad_values): the gradient of
+ * L = sum_mn dl_dmu[m][n] mu[m][n] with respect to every stored entry of the input CSR
+ * (out_grad_values, nnz; through the recursion and through both velocity operators) and the
+ * onsite energies (out_grad_onsite, rows, nullable). The scaling (a, b) is held fixed. Keeps both
+ * Chebyshev chains on the device (5 x num_moments x rows x vectors doubles). */
+int kpm_adjoint_conductivity(kpm_engine* engine, const float* left_coords, const float* right_coords,
+                             int64_t num_moments, int64_t num_vectors, const void* starters, const double* dl_dmu,
+                             double* out_mu, double* out_grad_values, double* out_grad_onsite);
 
 /* Stats of the last calculation (kpm/Stats.cpp:31-65; KPMStats, cppmodule/src/kpm.cpp:50-66). */
 int kpm_get_stats(kpm_engine* engine, kpm_stats* out);

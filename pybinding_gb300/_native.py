@@ -21,7 +21,7 @@ KPM_OK, KPM_ERR_RUNTIME, KPM_ERR_VALUE, KPM_ERR_CUDA, KPM_ERR_TIMEOUT = 0, 1, 2,
 SCALAR_CODE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1,
                np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
 KERNEL_CODE = {"jackson": 0, "lorentz": 1, "dirichlet": 2}
-PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2}
+PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2, "fp32x": 3}
 STAGING_CODE = {"auto": 0, "registers": 1, "prefetch": 2}
 
 
@@ -75,6 +75,7 @@ SIGNATURES = {
     "kpm_moments": (_I32, [_P, _I64, _P, _I64, _P, _I64, _I64, _P, _P, _P, _P]),
     "kpm_calc_conductivity": (_I32, [_P, _P, _P, _P, _I64, _D, _D, _I64, _I64, _I32, _P]),
     "kpm_adjoint_diag": (_I32, [_P, _I64, _I64, _P, _P, _I64, _P, _P, _P]),
+    "kpm_adjoint_conductivity": (_I32, [_P, _P, _P, _I64, _I64, _P, _P, _P, _P, _P]),
     "kpm_conductivity_moments": (_I32, [_P, _P, _P, _I64, _I64, _I32, _P]),
     "kpm_kubo_bastin": (_I32, [_P, _P, _I64, _P, _I64, _D, _I64, _P]),
     "kpm_get_stats": (_I32, [_P, _P]),
@@ -377,6 +378,28 @@ class Engine:
         fn = PROGRESS_FN(lambda delta, total, user: callback(int(delta), int(total)))
         self._progress = fn  # kept alive as long as the engine may call it
         check(lib().kpm_set_progress_callback(self._h, fn, None))
+
+    def adjoint_conductivity(self, left, right, num_moments, starters, dl_dmu=None):
+        """Kubo-Bastin moments matrix mu[m, n] (undamped, real) of ``starters`` [vector][site]
+        and, with ``dl_dmu`` (M, M), the gradient of sum(dl_dmu * mu) with respect to the stored
+        entries of H and the onsite energies: (mu, grad_values, grad_onsite)."""
+        l_ = np.ascontiguousarray(left, np.float32)
+        r_ = np.ascontiguousarray(right, np.float32)
+        keep = np.ascontiguousarray(starters, dtype=self.dtype)
+        if keep.size == 0 or keep.size % self.rows:
+            raise ValueError("starters must hold num_vectors * %d elements" % self.rows)
+        M = int(num_moments)
+        mu = np.empty((M, M), np.float64)
+        gv = go = w = None
+        if dl_dmu is not None:
+            w = np.ascontiguousarray(dl_dmu, np.float64)
+            if w.shape != (M, M):
+                raise ValueError("dl_dmu must have shape (%d, %d)" % (M, M))
+            gv = np.empty(self._nnz, np.float64)
+            go = np.empty(self.rows, np.float64)
+        check(lib().kpm_adjoint_conductivity(self._h, ptr(l_), ptr(r_), M, keep.size // self.rows, ptr(keep), ptr(w),
+                                             ptr(mu), ptr(gv), ptr(go)))
+        return mu, gv, go
 
     def stream(self):
         """The engine's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""

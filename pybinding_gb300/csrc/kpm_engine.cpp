@@ -968,19 +968,22 @@ struct kpm_engine {
         int vtype, E, LPR, nbatch;
         int64_t rows, nnz;
         int W, staging, device;
-        bool full_rows, real;
+        bool full_rows, real, comp;
         bool operator==(TuneKey const& o) const {
             return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows &&
                    nnz == o.nnz && W == o.W && staging == o.staging && device == o.device &&
-                   full_rows == o.full_rows && real == o.real;
+                   full_rows == o.full_rows && real == o.real && comp == o.comp;
         }
     };
     TuneKey tune_key(Shape const& sh, bool full_rows) const {
         int dev = 0;
         cudaGetDevice(&dev);
-        return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, full_rows, real_values};
+        return TuneKey{vtype, sh.E, sh.LPR, sh.nbatch, rows, opt_nnz, W, cfg.staging, dev, full_rows, real_values,
+                       compensated()};
     }
     struct Tuned { int rows_per_tile, unroll, E, LPR, prefetch = 0; };
+    // FP32 real recursions with compensated row sums (KPM_PREC_FP32X)
+    bool compensated() const { return vtype == kpm::V_F32 && cfg.precision == KPM_PREC_FP32X; }
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
     template<class T>
@@ -1027,7 +1030,7 @@ struct kpm_engine {
             for (auto const& mp : maps)
                 for (int unroll : {1, 2})
                     for (int rpt : {1, 2, 4, 8, 16, 32, 64}) {
-                        if (rpt < 2 * unroll || cfg.staging == 2) continue;
+                        if (rpt < 2 * unroll || cfg.staging == 2 || (compensated() && unroll != 1)) continue;
                         Shape t = sh;
                         t.E = mp.first;
                         t.LPR = mp.second;
@@ -1055,7 +1058,7 @@ struct kpm_engine {
             base.LPR = sh.LPR;
             for (int pf : {3, 4})
                 for (int chunks : {1, 2, 4, 8}) {
-                    if (cfg.staging == 1) break;
+                    if (cfg.staging == 1 || compensated()) break;
                     Shape t = sh;
                     t.rows_per_tile = 128 * chunks;
                     base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
@@ -1270,6 +1273,7 @@ struct kpm_engine {
         a.y = d_x1.p;
         a.acc = d_acc.as<double>();
         bool alt_map = false;  // a thinner lane mapping: single-step launches only
+        a.compensated = compensated();
         d_pair_error.ensure(sizeof(int));
         KPM_CUDA(cudaMemsetAsync(d_pair_error.p, 0, sizeof(int), stream));
         if (cfg.tile_rows > 0) {
@@ -1365,7 +1369,7 @@ struct kpm_engine {
             n += 2;
         };
         int const rpp = 256 / sh.LPR;
-        bool const can_pair = !opt_rows && cfg.fuse_steps != 1 && !alt_map;
+        bool const can_pair = !opt_rows && cfg.fuse_steps != 1 && !alt_map && !a.compensated;
         FuseChoice choice{1, 0};
         TuneKey const fkey = tune_key(sh, full_rows);
         bool have_choice = fuse_tuned().find(fkey, choice);
@@ -1610,7 +1614,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
             fail(KPM_ERR_VALUE, "KPM: Invalid energy range specified (min > max).");
         if (e->cfg.kernel == KPM_KERNEL_LORENTZ && e->cfg.kernel_param <= 0)
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
-        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
+        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32X)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
         if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
@@ -1643,7 +1647,7 @@ int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_
             fail(KPM_ERR_VALUE, "KPM: Invalid energy range specified (min > max).");
         if (e->cfg.kernel == KPM_KERNEL_LORENTZ && e->cfg.kernel_param <= 0)
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
-        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32)
+        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32X)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
         if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
@@ -2649,6 +2653,291 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         e->finish_stats();
         e->calc_time = now_s() - t0;
         if (num_moments_out) *num_moments_out = M;
+    });
+}
+
+// Reverse-mode gradient of a loss of the Kubo-Bastin moments matrix (real Hamiltonians, FP64
+// recursion). With t^l_m = T_m(H~) V_l r, t^r_n = T_n(H~) r and u_n = V_r t^r_n (row and column
+// 0 halved as the collectors store them, kpm/default/collectors.cpp:82-107),
+//   mu_mn = (1/R) sum_r h_m h_n <t^l_m, u_n>,   L = sum_mn dl_dmu[m][n] mu_mn,
+// the cotangents of the stored vectors are A_m = sum_n C_mn u_n and B_n = sum_m C_mn t^l_m with
+// C_mn = dl_dmu[m][n] h_m h_n / R (two FP64 combinations on the GPU). Each side then runs the
+// adjoint of its Chebyshev chain (t_0 = s, t_1 = S s / 2, t_{m+1} = S t_m - t_{m-1}, S = 2 H~):
+//   lam_m = a_m + S lam_{m+1} - lam_{m+2},  lam_0 = a_0 + S lam_1 / 2 - lam_2,
+//   dL/dS += sum_{m>=1} lam_{m+1} t_m^T + lam_1 t_0^T / 2,
+// with sources a_m = A_m on the left and a_n = V_r^T B_n = -V_r B_n on the right (V is
+// antisymmetric for a real H). The velocity operators V = H o (x_i - x_j) depend on H too:
+// dL/dV_l = lam^l_0 r^T and dL/dV_r = sum_n B_n (t^r_n)^T on the pattern of H. Everything stays on
+// the device (every vector of both chains is kept: 5 M x rows x K doubles).
+int kpm_adjoint_conductivity(kpm_engine* e, const float* left, const float* right, int64_t num_moments,
+                             int64_t num_vectors, const void* starters, const double* dl_dmu, double* out_mu,
+                             double* out_grad_values, double* out_grad_onsite) {
+    return guarded([&] {
+        if (!e) fail(KPM_ERR_VALUE, "null engine");
+        HostThreads host_threads(e->cfg.num_threads);
+        if (!left || !right || !starters) fail(KPM_ERR_VALUE, "null argument");
+        if ((dl_dmu == nullptr) != (out_grad_values == nullptr))
+            fail(KPM_ERR_VALUE, "dl_dmu and out_grad_values go together");
+        if (e->nsys != 1) fail(KPM_ERR_VALUE, "conductivity gradients need a single-system engine");
+        if (e->stype == KPM_C64 || e->stype == KPM_C128 || e->vtype != kpm::V_F64)
+            fail(KPM_ERR_VALUE, "conductivity gradients need a real Hamiltonian and the FP64 recursion "
+                                "(float64 H, or precision fp64)");
+        if (num_vectors < 1) fail(KPM_ERR_VALUE, "num_vectors must be >= 1");
+        int64_t const M = num_moments;
+        if (M < 3) fail(KPM_ERR_VALUE, "num_moments must be >= 3");
+        double const t0 = now_s();
+        e->optimize({0}, {0});
+        auto const sc = e->scale(0);
+        int64_t const n = e->rows;
+        int const vt = kpm::V_F64;
+        int const W = e->W;
+        kpm_engine::Shape sh = e->pick_shape(num_vectors);
+        int64_t const K = sh.K;
+        int64_t const I = n * K;
+        size_t const vec = sizeof(double) * static_cast<size_t>(I);
+        {
+            size_t free_b = 0, total_b = 0;
+            KPM_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            if (static_cast<double>(5 * M + 8) * vec > 0.8 * static_cast<double>(free_b))
+                fail(KPM_ERR_RUNTIME, "not enough device memory to keep both Chebyshev chains (5 x num_moments x rows "
+                                      "x vectors doubles)");
+        }
+        // velocity operators V = H o (x_i - x_j) on the reordered ELL pattern of S (kpm/Moments.cpp:132-155;
+        // float coordinate differences, KPM.cpp:140-145)
+        std::vector<int32_t> const& hcol = e->h_col;
+        std::vector<double> vl_ell(static_cast<size_t>(n) * W, 0.0), vr_ell(static_cast<size_t>(n) * W, 0.0);
+        with_scalar(e->stype, [&](auto zi) {
+            using T = decltype(zi);
+            auto const* hv = reinterpret_cast<T const*>(e->values.data());
+            for (int64_t r = 0; r < n; ++r)
+                for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) {
+                    int32_t const c = e->indices[k];
+                    int32_t const nr = e->map[r], nc = e->map[c];
+                    int j = 0;
+                    while (j < W && hcol[static_cast<size_t>(nr) * W + j] != nc) ++j;
+                    if (j == W) fail(KPM_ERR_RUNTIME, "internal: entry outside the S pattern");
+                    size_t const q = static_cast<size_t>(nr) * W + j;
+                    double const h = to_cd(hv[k]).real();
+                    vl_ell[q] = h * static_cast<double>(left[r] - left[c]);
+                    vr_ell[q] = h * static_cast<double>(right[r] - right[c]);
+                }
+        });
+        DBuf d_vl, d_vr, d_tl, d_tr, d_u, d_a, d_b, d_lam, d_tmp, d_r0, d_gs, d_gsd, d_gvl, d_gvr, d_gvd, d_c, d_mu;
+        d_vl.ensure(sizeof(double) * vl_ell.size());
+        d_vr.ensure(sizeof(double) * vr_ell.size());
+        e->upload_host(d_vl.p, vl_ell.data(), sizeof(double) * vl_ell.size());
+        e->upload_host(d_vr.p, vr_ell.data(), sizeof(double) * vr_ell.size());
+        d_tl.ensure(vec * M);
+        d_tr.ensure(vec * M);
+        d_u.ensure(vec * M);
+        bool const grad = dl_dmu != nullptr;
+        if (grad) {
+            d_a.ensure(vec * M);
+            d_b.ensure(vec * M);
+        }
+        d_lam.ensure(vec * 3);
+        d_tmp.ensure(vec);
+        d_r0.ensure(vec);
+        size_t const gs_bytes = sizeof(double) * static_cast<size_t>(n) * W;
+        for (DBuf* b : {&d_gs, &d_gvl, &d_gvr}) {
+            b->ensure(gs_bytes);
+            KPM_CUDA(cudaMemsetAsync(b->p, 0, gs_bytes, e->stream));
+        }
+        d_gsd.ensure(sizeof(double) * n);
+        d_gvd.ensure(sizeof(double) * n);  // diagonal of the velocity gradients: unused (V_ii = 0)
+        KPM_CUDA(cudaMemsetAsync(d_gsd.p, 0, sizeof(double) * n, e->stream));
+        KPM_CUDA(cudaMemsetAsync(d_gvd.p, 0, sizeof(double) * n, e->stream));
+        d_mu.ensure(sizeof(double) * 2 * M * M);
+        KPM_CUDA(cudaMemsetAsync(d_mu.p, 0, sizeof(double) * 2 * M * M, e->stream));
+        // C_mn = dl_dmu[m][n] h_m h_n / R, and its transpose
+        double const R = static_cast<double>(num_vectors);
+        std::vector<double> c, ct;
+        if (grad) {
+            c.resize(static_cast<size_t>(M) * M);
+            ct.resize(static_cast<size_t>(M) * M);
+            for (int64_t m = 0; m < M; ++m)
+                for (int64_t q = 0; q < M; ++q) {
+                    double const v = dl_dmu[m * M + q] * (m == 0 ? 0.5 : 1.0) * (q == 0 ? 0.5 : 1.0) / R;
+                    c[m * M + q] = v;
+                    ct[q * M + m] = v;
+                }
+            d_c.ensure(sizeof(double) * 2 * M * M);
+            KPM_CUDA(cudaMemcpyAsync(d_c.p, c.data(), sizeof(double) * M * M, cudaMemcpyHostToDevice, e->stream));
+            KPM_CUDA(cudaMemcpyAsync(d_c.as<double>() + M * M, ct.data(), sizeof(double) * M * M,
+                                     cudaMemcpyHostToDevice, e->stream));
+        }
+        sh.nbatch = 1;
+        int const ntiles = e->build_tiles(sh, true);
+        kpm::AdjStep base{};
+        base.vtype = vt;
+        base.E = sh.E;
+        base.LPR = sh.LPR;
+        base.col = e->d_col.as<int32_t>();
+        base.val = e->d_val.p;
+        base.W = W;
+        base.tiles = e->d_tiles.as<Tile>();
+        base.num_tiles = ntiles;
+        auto* tl = static_cast<unsigned char*>(d_tl.p);
+        auto* tr = static_cast<unsigned char*>(d_tr.p);
+        auto* u = static_cast<unsigned char*>(d_u.p);
+        auto vrow = [&](unsigned char* b, int64_t m) { return b + vec * m; };
+        auto apply_v = [&](void const* vals, void const* x, void* out) {  // out = V x on the pattern of S
+            kpm::AdjStep a = base;
+            a.val = vals;
+            a.x = x;
+            a.out = out;
+            KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+        };
+        auto chain = [&](unsigned char* t, void const* start) {  // t_0 .. t_{M-1}
+            KPM_CUDA(cudaMemcpyAsync(t, start, vec, cudaMemcpyDeviceToDevice, e->stream));
+            kpm::AdjStep a = base;
+            a.x = t;
+            a.out = vrow(t, 1);
+            a.half = true;
+            KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+            for (int64_t m = 1; m + 1 < M; ++m) {
+                a.x = vrow(t, m);
+                a.yprev = vrow(t, m - 1);
+                a.out = vrow(t, m + 1);
+                a.half = false;
+                KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+            }
+        };
+        // the adjoint of a chain with sources a_m (rows of `src` times src_scale), S gradient into
+        // d_gs / d_gsd; returns the buffer holding lam_0
+        unsigned char* lamb = static_cast<unsigned char*>(d_lam.p);
+        auto adjoint = [&](unsigned char* t, unsigned char* src, double src_scale) -> unsigned char* {
+            unsigned char* l1 = nullptr;  // lam_{m+1}
+            unsigned char* l2 = nullptr;  // lam_{m+2}
+            auto fresh = [&]() {
+                for (int q = 0; q < 3; ++q) {
+                    unsigned char* b = lamb + vec * q;
+                    if (b != l1 && b != l2) return b;
+                }
+                return lamb;
+            };
+            for (int64_t m = M - 1; m >= 0; --m) {
+                unsigned char* out = fresh();
+                if (l1 != nullptr) {
+                    kpm::AdjStep a = base;
+                    a.v0 = vrow(src, m);
+                    a.a0 = src_scale;
+                    a.x = l1;
+                    a.yprev = l2;
+                    a.half = (m == 0);
+                    // dL/dS += lam_{m+1} t_m^T (m >= 1); lam_1 t_0^T / 2 at m = 0 (g = t_0 / 2)
+                    if (m >= 1) {
+                        a.g = vrow(t, m);
+                    } else {
+                        KPM_CUDA(kpm::launch_axpby(vt, I, 0.5, vrow(t, 0), 0.0, nullptr, d_tmp.p, e->stream));
+                        a.g = d_tmp.p;
+                    }
+                    a.gt = d_gs.p;
+                    a.gd = d_gsd.p;
+                    a.out = out;
+                    KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+                } else {  // lam_{M-1} = a_{M-1}
+                    KPM_CUDA(kpm::launch_axpby(vt, I, src_scale, vrow(src, m), 0.0, nullptr, out, e->stream));
+                }
+                l2 = l1;
+                l1 = out;
+            }
+            return l1;
+        };
+        auto grad_v = [&](void const* x, void const* g, void* gt) {  // gt[p][j] += x[col_j] . g[p]
+            kpm::AdjStep a = base;
+            a.x = x;
+            a.g = g;
+            a.gt = gt;
+            a.gd = d_gvd.p;
+            KPM_CUDA(kpm::launch_adj_step(a, e->stream));
+        };
+
+        size_t const ssize = static_cast<size_t>(scalar_bytes(e->stype));
+        std::vector<unsigned char> stage(static_cast<size_t>(K) * n * ssize);
+        int64_t const nbatch = (num_vectors + K - 1) / K;
+        KPM_CUDA(cudaEventRecord(e->ev0, e->stream));
+        for (int64_t bt = 0; bt < nbatch; ++bt) {
+            int64_t const v_first = bt * K;
+            int64_t const v_count = std::min<int64_t>(K, num_vectors - v_first);
+            KPM_CUDA(cudaStreamSynchronize(e->stream));  // the previous batch's upload has been consumed
+            std::fill(stage.begin(), stage.end(), 0);
+            std::memcpy(stage.data(), static_cast<unsigned char const*>(starters) + static_cast<size_t>(v_first) * n * ssize,
+                        static_cast<size_t>(v_count) * n * ssize);
+            void const* src = e->device_view(stage.data(), stage.size());
+            KPM_CUDA(cudaMemsetAsync(d_r0.p, 0, vec, e->stream));
+            KPM_CUDA(kpm::launch_scatter_starters(e->stype, vt, src, d_r0.p, e->d_map.as<int32_t>(),
+                                                  e->d_sysoff.as<int64_t>(), 1, K, static_cast<int>(K), 1, n, e->stream));
+            // forward: t^l from V_l r, t^r from r, u_n = V_r t^r_n
+            apply_v(d_vl.p, d_r0.p, d_tmp.p);
+            chain(tl, d_tmp.p);
+            chain(tr, d_r0.p);
+            for (int64_t m = 0; m < M; ++m) apply_v(d_vr.p, vrow(tr, m), vrow(u, m));
+            // mu_mn += sum <t^l_m, u_n> (the halved row / column 0 and 1/R are applied on the host)
+            KPM_CUDA(kpm::launch_mu_gemm_fp64(vt, tl, u, M, I, d_mu.as<double>(), e->stream));
+            if (!grad) continue;
+            auto* A = static_cast<unsigned char*>(d_a.p);
+            auto* B = static_cast<unsigned char*>(d_b.p);
+            // A_m = sum_n C_mn u_n ; B_n = sum_m C_mn t^l_m
+            KPM_CUDA(kpm::launch_dense_combine(d_c.as<double>(), reinterpret_cast<double const*>(u),
+                                               reinterpret_cast<double*>(A), static_cast<int>(M), I, e->stream));
+            KPM_CUDA(kpm::launch_dense_combine(d_c.as<double>() + M * M, reinterpret_cast<double const*>(tl),
+                                               reinterpret_cast<double*>(B), static_cast<int>(M), I, e->stream));
+            // left adjoint first: A is then free to hold the right side's sources V_r B_n
+            unsigned char* lam0 = adjoint(tl, A, 1.0);
+            grad_v(lam0, d_r0.p, d_gvl.p);  // dL/dV_l = lam^l_0 r^T
+            for (int64_t q = 0; q < M; ++q) {
+                grad_v(vrow(B, q), vrow(tr, q), d_gvr.p);  // dL/dV_r += B_q (t^r_q)^T
+                apply_v(d_vr.p, vrow(B, q), vrow(A, q));   // A_q <- V_r B_q (sources, scaled by -1)
+            }
+            adjoint(tr, A, -1.0);
+        }
+        KPM_CUDA(cudaEventRecord(e->ev1, e->stream));
+        std::vector<double> mu(static_cast<size_t>(2) * M * M);
+        KPM_CUDA(cudaMemcpyAsync(mu.data(), d_mu.p, sizeof(double) * mu.size(), cudaMemcpyDeviceToHost, e->stream));
+        std::vector<double> gs(static_cast<size_t>(n) * W), gsd(n), gvl(static_cast<size_t>(n) * W),
+            gvr(static_cast<size_t>(n) * W);
+        if (grad) {
+            KPM_CUDA(cudaMemcpyAsync(gs.data(), d_gs.p, gs_bytes, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaMemcpyAsync(gsd.data(), d_gsd.p, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaMemcpyAsync(gvl.data(), d_gvl.p, gs_bytes, cudaMemcpyDeviceToHost, e->stream));
+            KPM_CUDA(cudaMemcpyAsync(gvr.data(), d_gvr.p, gs_bytes, cudaMemcpyDeviceToHost, e->stream));
+        }
+        KPM_CUDA(cudaStreamSynchronize(e->stream));
+        float ms = 0;
+        KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        if (out_mu)  // mu[m][n] (real part: zero imaginary part for a real H and real starters)
+            for (int64_t m = 0; m < M; ++m)
+                for (int64_t q = 0; q < M; ++q)
+                    out_mu[m * M + q] = mu[2 * (q * M + m)] * (m == 0 ? 0.5 : 1.0) * (q == 0 ? 0.5 : 1.0) / R;
+        if (grad) {
+            // gt[p][t] holds the gradient of the transposed entry (col(p, t), p): the stored entry
+            // (i, j) is found at slot (map[j], t) with col = map[i]
+            double const f = 2.0 / sc.a;
+            for (int64_t r = 0; r < n; ++r)
+                for (int32_t k = e->indptr[r]; k < e->indptr[r + 1]; ++k) {
+                    int32_t const c = e->indices[k];
+                    int32_t const ni = e->map[r], nj = e->map[c];
+                    if (c == r) {
+                        out_grad_values[k] = f * gsd[ni];
+                        continue;
+                    }
+                    int t = 0;
+                    while (t < W && hcol[static_cast<size_t>(nj) * W + t] != ni) ++t;
+                    if (t == W) fail(KPM_ERR_RUNTIME, "internal: adjoint entry outside the S pattern");
+                    size_t const q = static_cast<size_t>(nj) * W + t;
+                    // V = H o (x_i - x_j): dL/dH_ij += (x_i - x_j) dL/dV_ij on either side
+                    double const dl = static_cast<double>(left[r] - left[c]);
+                    double const dr = static_cast<double>(right[r] - right[c]);
+                    out_grad_values[k] = f * gs[q] + dl * gvl[q] + dr * gvr[q];
+                }
+            if (out_grad_onsite)
+                for (int64_t i = 0; i < n; ++i) out_grad_onsite[i] = f * gsd[e->map[i]];
+        }
+        e->reset_stats(M, false, false, static_cast<double>(num_vectors), 0);
+        e->st.moments_time = ms * 1e-3;
+        e->finish_stats();
+        e->calc_time = now_s() - t0;
     });
 }
 

@@ -45,6 +45,8 @@ struct DiagStep {
     int prefetch = 0;         // > 0: ELL entries copied to shared memory a chunk ahead (diag_pf_kernel),
                               // register allocation for 3 or 4 resident blocks per SM (3 or 4);
                               // chosen by the autotuner; unroll is then 1
+    bool compensated = false; // FP32 real vectors: each row sum of H~ x compensated (error-free
+                              // products and TwoSum), rounded once; one row per thread
     bool real_matrix = false; // complex vectors with real H~ values: val holds [rows][W][vs] of the
                               // real type (vs of that type: hi/lo pairs for FP32)
 };
@@ -174,6 +176,8 @@ cudaError_t launch_adj_step(AdjStep const& a, cudaStream_t s);
 // dst[0..bytes) = src[0..bytes), both 16-byte aligned; src may be host memory that the GPU
 // reads through the host page tables (a copy at the link's rate, no staging)
 cudaError_t launch_copy(void* dst, void const* src, size_t bytes, cudaStream_t s);
+// Y[m][i] = sum_n C[m][n] X[n][i] in FP64 (C: M x M row-major; X, Y: M rows of I doubles)
+cudaError_t launch_dense_combine(double const* C, double const* X, double* Y, int M, int64_t I, cudaStream_t s);
 cudaError_t launch_axpby(int vtype, int64_t n, double a, void const* x, double b, void const* y, void* out,
                          cudaStream_t s);
 bool diag_shape_supported(int vtype, int E, int LPR);

@@ -69,7 +69,8 @@ kpm_config make_config(py::dict kw) {
             if (p == "auto") c.precision = KPM_PREC_AUTO;
             else if (p == "fp64") c.precision = KPM_PREC_FP64;
             else if (p == "fp32") c.precision = KPM_PREC_FP32;
-            else throw py::value_error("precision must be 'auto', 'fp64' or 'fp32'");
+            else if (p == "fp32x") c.precision = KPM_PREC_FP32X;
+            else throw py::value_error("precision must be 'auto', 'fp64', 'fp32' or 'fp32x'");
         } else if (key == "batch_width") {
             c.batch_width = v.cast<int32_t>();
         } else if (key == "tile_rows") {
@@ -336,6 +337,37 @@ public:
         return py::make_tuple(gv, go);
     }
 
+    // Kubo-Bastin moments matrix of explicit starters and, with dl_dmu, its gradient
+    py::tuple adjoint_conductivity(carr<float> left, carr<float> right, int64_t num_moments, py::object starters,
+                                   py::object dl_dmu) {
+        py::array keep = contiguous(starters);
+        if (keep.size() == 0 || keep.size() % rows_)
+            throw py::value_error("starters must hold num_vectors * " + std::to_string(rows_) + " elements");
+        int64_t const M = num_moments;
+        auto mu = carr<double>({M, M});
+        carr<double> w;
+        py::object gv = py::none(), go = py::none();
+        double* gvp = nullptr;
+        double* gop = nullptr;
+        if (!dl_dmu.is_none()) {
+            w = carr<double>(dl_dmu);
+            if (w.ndim() != 2 || w.shape(0) != M || w.shape(1) != M)
+                throw py::value_error("dl_dmu must have shape (num_moments, num_moments)");
+            auto a = carr<double>(static_cast<py::ssize_t>(nnz_));
+            auto b = carr<double>(static_cast<py::ssize_t>(rows_));
+            gvp = a.mutable_data();
+            gop = b.mutable_data();
+            gv = a;
+            go = b;
+        }
+        {
+            py::gil_scoped_release nogil;
+            check(kpm_adjoint_conductivity(handle(), left.data(), right.data(), M, keep.size() / rows_, keep.data(),
+                                           gvp ? w.data() : nullptr, mu.mutable_data(), gvp, gop));
+        }
+        return py::make_tuple(mu, gv, go);
+    }
+
     void set_progress_callback(py::object fn) {
         progress_ = fn;
         if (fn.is_none()) check(kpm_set_progress_callback(handle(), nullptr, nullptr));
@@ -449,6 +481,8 @@ PYBIND11_MODULE(_kpm_gb300, m) {
              py::arg("num_points"), py::arg("gemm_mode") = 0)
         .def("adjoint_diag", &Engine::adjoint_diag, py::arg("num_moments"), py::arg("starters"), py::arg("dl_dmu"),
              py::arg("checkpoint") = 0)
+        .def("adjoint_conductivity", &Engine::adjoint_conductivity, py::arg("left"), py::arg("right"),
+             py::arg("num_moments"), py::arg("starters"), py::arg("dl_dmu") = py::none())
         .def("set_progress_callback", &Engine::set_progress_callback, py::arg("callback"))
         .def("stats", &Engine::stats)
         .def("report", &Engine::report, py::arg("shortform") = false)

@@ -45,11 +45,13 @@ PHI0 = 2 * math.pi * HBAR
 
 @dataclass
 class System:
-    """Site positions and sublattice layout of a built system (single orbital)."""
+    """Site positions and sublattice layout of a built system; ``orbitals`` per site (one
+    sublattice kind per system here, so every site has the same number)."""
     x: np.ndarray
     y: np.ndarray
     z: np.ndarray
     sub_ranges: dict = field(default_factory=dict)  # name -> (start, end)
+    orbitals: int = 1
 
     @property
     def positions(self):
@@ -61,7 +63,7 @@ class System:
 
     @property
     def hamiltonian_size(self):
-        return self.num_sites
+        return self.num_sites * self.orbitals
 
     def sublattice_range(self, sublattice=""):
         """cppcore/src/system/System.cpp:50-66"""
@@ -87,8 +89,10 @@ class System:
         return int(start + np.argmin(d))
 
     def to_hamiltonian_indices(self, system_index):
-        """Single-orbital systems map site ``i`` to Hamiltonian row ``i`` (System.cpp:33-48)."""
-        return np.array([int(system_index)], dtype=np.int32)
+        """The Hamiltonian rows of site ``i``: ``i * orbitals + k`` for its orbitals k
+        (System.cpp:33-48, one sublattice kind)."""
+        first = int(system_index) * self.orbitals
+        return np.arange(first, first + self.orbitals, dtype=np.int32)
 
     def contains_mask(self, contains):
         return np.asarray(contains(self.x, self.y, self.z), dtype=bool)
@@ -105,7 +109,7 @@ class Model:
 
     @property
     def is_multiorbital(self):
-        return False
+        return self.system is not None and self.system.orbitals > 1
 
 
 # --------------------------------------------------------------------------- shapes
@@ -509,3 +513,101 @@ def simple_cubic_periodic(L, t=-1.0, onsite=None, dtype=np.float32, device=None)
     h = _csr_sorted(rows, cols, vals, n, dtype)
     system = System(xi.astype(f32), yi.astype(f32), zi.astype(f32), {"A": (0, n)})
     return Model(h, system, name="cubic")
+
+
+# --------------------------------------------------------------------------- 3-band TMD monolayers
+# Nearest-neighbour three-band model of group-6 transition-metal dichalcogenides (metal d_z2,
+# d_xy, d_x2-y2 orbitals on a triangular lattice; Liu et al., Phys. Rev. B 88, 085433 (2013),
+# the parameters pybinding/repository/group6_tmd.py:7-14 uses):
+#            a (nm), eps1,  eps2,   t0,     t1,    t2,    t11,   t12,   t22
+TMD_3BAND = {
+    "MoS2": (0.3190, 1.046, 2.104, -0.184, 0.401, 0.507, 0.218, 0.338, 0.057),
+    "WS2": (0.3191, 1.130, 2.275, -0.206, 0.567, 0.536, 0.286, 0.384, -0.061),
+    "MoSe2": (0.3326, 0.919, 2.065, -0.188, 0.317, 0.456, 0.211, 0.290, 0.130),
+    "WSe2": (0.3325, 0.943, 2.179, -0.207, 0.457, 0.486, 0.263, 0.329, 0.034),
+    "MoTe2": (0.3557, 0.605, 1.972, -0.169, 0.228, 0.390, 0.207, 0.239, 0.252),
+    "WTe2": (0.3560, 0.606, 2.102, -0.175, 0.342, 0.410, 0.233, 0.270, 0.190),
+}
+
+
+def _tmd_hopping_blocks(t0, t1, t2, t11, t12, t22):
+    """The 3 x 3 hopping matrices of the bonds a1, -a2 and a1 - a2 (the three a metal site owns).
+    The bond along a1 (angle 0) has E(R1) below; a bond at angle phi is the C3-related matrix
+    U(phi) E(R1) U(phi)^T, where U rotates (d_z2, d_xy, d_x2-y2) by phi (the d_xy / d_x2-y2 pair
+    turns by 2 phi), and reversing a bond transposes its matrix: -a2 points at 240 degrees and
+    a1 - a2 at 300 degrees, the reverse of the bond at 120 degrees."""
+    e1 = np.array([[t0, -t1, t2], [t1, t11, -t12], [t2, t12, t22]])
+
+    def rotate(deg):
+        c, s = math.cos(math.radians(2 * deg)), math.sin(math.radians(2 * deg))
+        u = np.array([[1.0, 0, 0], [0, c, s], [0, -s, c]])
+        return u @ e1 @ u.T
+    return [((1, 0), e1), ((0, -1), rotate(240)), ((1, -1), rotate(120).T)]
+
+
+def build_tmd_3band(vertices, material="MoS2", min_neighbors=1, is_double=False, name=None):
+    """A group-6 TMD monolayer (three orbitals per metal site) cut by the polygon ``vertices``, in
+    pybinding's site and Hamiltonian order: sites of the triangular lattice a1 = (a, 0),
+    a2 = (a/2, a sqrt(3)/2) inside the polygon (foundation and float32 positions as for the
+    honeycomb builder), dangling sites removed down to ``min_neighbors`` (the lattice default 1),
+    Hamiltonian row 3 i + k for orbital k of site i (``System.cpp:33-48``), onsite
+    diag(eps1, eps2, eps2), each bond's 3 x 3 block stored for the owning site and its transpose
+    for the other (``Hamiltonian.hpp:74-100``). Real; float32 unless ``is_double``."""
+    f32 = np.float32
+    a, eps1, eps2, t0, t1, t2, t11, t12, t22 = TMD_3BAND[material]
+    v0 = np.array([a, 0, 0], f32)
+    v1 = np.array([a / 2, a / 2 * math.sqrt(3), 0], f32)
+    m = np.array([[v0[0], v1[0]], [v0[1], v1[1]]], dtype=np.float64)
+    coords = np.linalg.solve(m, np.asarray(vertices, np.float64).T).T
+    ic = np.trunc(coords).astype(np.int64)
+    lo = ic.min(axis=0) - 1
+    hi = ic.max(axis=0) + 1
+    s0, s1 = int(hi[0] - lo[0] + 1), int(hi[1] - lo[1] + 1)
+    origin = np.zeros(3, f32) + f32(lo[0]) * v0
+    origin = origin + f32(lo[1]) * v1
+    bb = np.arange(s1)
+    aa = np.arange(s0)
+    pb = np.empty((s1, 3), f32)
+    pb[0] = origin
+    pb[1:] = origin[None, :] + bb[1:, None].astype(f32) * v1[None, :]
+    pa = pb[:, None, :] + aa[None, :, None].astype(f32) * v0[None, None, :]
+    x, y, z = pa[..., 0].ravel(), pa[..., 1].ravel(), pa[..., 2].ravel()
+    total = s0 * s1
+    valid = polygon_contains(np.asarray(vertices, np.float32), x, y)
+    blocks = _tmd_hopping_blocks(t0, t1, t2, t11, t12, t22)
+    a_idx = np.tile(aa, s1)
+    b_idx = np.repeat(bb, s0)
+    offsets = [d for d, _ in blocks] + [(-da, -db) for (da, db), _ in blocks]
+    nbr = np.full((total, len(offsets)), -1, np.int64)
+    for h, (da, db) in enumerate(offsets):
+        na, nb = a_idx + da, b_idx + db
+        ok = (na >= 0) & (na < s0) & (nb >= 0) & (nb < s1)
+        nbr[:, h] = np.where(ok, nb * s0 + na, -1)
+    valid = _k_core(valid, nbr, min_neighbors)
+    final = np.full(total, -1, np.int64)
+    nvalid = int(valid.sum())
+    final[valid] = np.arange(nvalid)
+    dtype = np.float64 if is_double else np.float32
+    sites = np.nonzero(valid)[0]
+    rows, cols, vals = [], [], []
+    for h, (_, e) in enumerate(blocks):
+        tgt = nbr[sites, h]
+        ok = tgt >= 0
+        ok[ok] &= valid[tgt[ok]]
+        i, j = final[sites[ok]], final[tgt[ok]]
+        for p in range(3):
+            for q in range(3):
+                rows += [3 * i + p, 3 * j + q]
+                cols += [3 * j + q, 3 * i + p]
+                vals += [np.full(i.size, e[p, q]), np.full(i.size, e[p, q])]
+    diag = np.array([eps1, eps2, eps2])
+    d = np.arange(3 * nvalid)
+    rows.append(d)
+    cols.append(d)
+    vals.append(np.tile(diag, nvalid))
+    h = _csr_sorted(np.concatenate(rows), np.concatenate(cols), np.concatenate(vals).astype(dtype), 3 * nvalid,
+                    dtype)
+    metal = material[:2] if material[1].islower() else material[:1]
+    system = System(x[valid], y[valid], z[valid], {metal: (0, nvalid)}, orbitals=3)
+    return Model(h, system, is_double=is_double, name=name or material)
+

@@ -238,3 +238,12 @@ def test_pybind_module_raises_the_reference_exception_types():
     e.close()
     with pytest.raises(RuntimeError, match="closed"):
         e.scaling_factors()
+
+
+def test_spatial_ldos_refuses_the_three_band_tmd_model():
+    """The refusal on a real multi-orbital model (three orbitals per MoS2 site)."""
+    from pybinding_gb300 import kpm, lattice as L
+    k = kpm(L.build_tmd_3band(L.rectangle(2), "MoS2"), energy_range=(-3, 6), silent=True)
+    with pytest.raises(RuntimeError, match="doesn't currently support multi-orbital models"):
+        k.calc_spatial_ldos(np.linspace(0, 1, 3), 0.1, lambda x, y, z: np.ones(x.size, bool))
+

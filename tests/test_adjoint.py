@@ -191,9 +191,8 @@ def test_gpu_adjoint_matches_dense_eigh_gradient():
 @pytest.mark.gpu
 def test_gpu_adjoint_fp32_close_to_fp64():
     """FP32 recursion (FP32 vectors, FP64 gradient sums over the steps) against the FP64 one on a
-    64k-site strained flake, 1026 moments, 32 Rademacher vectors: within 1e-5 of the largest
-    entry (with FP32 gradient sums the difference was 1.8e-4: each entry's gradient is a sum
-    over 513 steps of terms of both signs)."""
+    64k-site strained flake (spectrum +-9.11 eV inside the range +-9.5 eV), 1026 moments, 32
+    Rademacher vectors: within 1e-5 of the largest entry."""
     from pybinding_gb300 import _native
     m = _strained_flake(64000)
     h = sp.csr_matrix(m.hamiltonian, dtype=np.float64)
@@ -207,7 +206,7 @@ def test_gpu_adjoint_fp32_close_to_fp64():
     out = {}
     for prec in ("fp64", "fp32"):
         hh = h.astype(np.float64 if prec == "fp64" else np.float32)
-        eng = _native.Engine(hh, _native.make_config(energy_range=(-9.5, 9.0), precision=prec))
+        eng = _native.Engine(hh, _native.make_config(energy_range=(-9.5, 9.5), precision=prec))
         out[prec] = eng.adjoint_diag(M, r0, w)
     scale = np.abs(out["fp64"][0]).max()
     err = np.abs(out["fp32"][0] - out["fp64"][0]).max() / scale
@@ -233,7 +232,7 @@ def test_gpu_adjoint_fp32_at_the_strained_flake_configuration_matches_finite_dif
     Mr = _native.round_num_moments(M)
     w = rng.normal(size=Mr) / np.sqrt(np.arange(1, Mr + 1))
     r0 = rng.choice([-1.0, 1.0], size=(32, n))
-    rng_e = (-9.5, 9.0)
+    rng_e = (-9.5, 9.5)  # the strained flake's spectrum is +-9.11 eV
     e32 = _native.Engine(h.astype(np.float32), _native.make_config(energy_range=rng_e, precision="fp32"))
     gv, go = e32.adjoint_diag(M, r0, w)
     e32.close()
@@ -324,3 +323,138 @@ def test_torch_autograd_dos_loss():
     an = float(values.grad.numpy() @ d.data)
     print("directional derivative: fd %.9e adjoint %.9e" % (fd, an))
     assert abs(fd - an) <= 1e-6 * abs(an)
+
+
+# ---------------------------------------------------------------- conductivity
+def _numpy_conductivity_moments(h, left, right, a, b, r0, M):
+    """mu[m, n] = mean_r h_m h_n <T_m(H~) V_l r, V_r T_n(H~) r> in NumPy FP64 (Core.cpp:119-145,
+    collectors.cpp:82-107; V = H o (x_i - x_j) with float32 coordinate differences)."""
+    s = _scaled(h, a, b)
+    coo = sp.csr_matrix(h, dtype=np.float64).tocoo()
+    dl = (left[coo.row] - left[coo.col]).astype(np.float64)
+    dr = (right[coo.row] - right[coo.col]).astype(np.float64)
+    vl = sp.csr_matrix((coo.data * dl, (coo.row, coo.col)), shape=h.shape)
+    vr = sp.csr_matrix((coo.data * dr, (coo.row, coo.col)), shape=h.shape)
+
+    def chain(start):
+        t = [start, 0.5 * (s @ start)]
+        for _ in range(2, M):
+            t.append(s @ t[-1] - t[-2])
+        return np.array(t)
+
+    mu = np.zeros((M, M))
+    for r in r0:
+        tl = chain(vl @ r)
+        u = np.array([vr @ x for x in chain(r)])
+        mu += tl @ u.T
+    hm = np.ones(M)
+    hm[0] = 0.5
+    return mu * np.outer(hm, hm) / r0.shape[0]
+
+
+@pytest.mark.gpu
+def test_gpu_conductivity_moments_and_kubo_bastin_match_numpy_and_engine():
+    """The conductivity moments matrix of explicit starters (the forward pass of the conductivity
+    gradient) equals a NumPy FP64 evaluation of Core::conductivity's moments, and the
+    differentiable torch Kubo-Bastin equals the engine's reconstruction of the same moments."""
+    torch = pytest.importorskip("torch")
+    from pybinding_gb300 import _native, jackson_kernel
+    from pybinding_gb300.adjoint import ConductivityMoments, kubo_bastin
+    m = _strained_flake(1200, onsite=0.3)
+    h = sp.csr_matrix(m.hamiltonian, dtype=np.float64)
+    h.sort_indices()
+    x = m.system.x
+    y = m.system.y
+    rng = np.random.default_rng(8)
+    r0 = rng.choice([-1.0, 1.0], size=(3, h.shape[0]))
+    M = 40
+    op = ConductivityMoments(h, x, y, M, r0, (-9.5, 9.0))
+    mu = op.moments(h.data)
+    a, b = op.scaling
+    ref = _numpy_conductivity_moments(h, x, y, a, b, r0, M)
+    err = np.abs(mu - ref).max() / np.abs(ref).max()
+    print("conductivity moments vs NumPy: %.3e" % err)
+    assert err < TOL_FP64
+    chem = np.linspace(-1.0, 1.0, 7)
+    kern = jackson_kernel()
+    sig = kubo_bastin(torch.from_numpy(mu), chem, op.scaling, op.energy_bounds, kern, 0.0, 300).numpy()
+    g = kern.damping_coefficients(M)
+    eng = _native.Engine(h, _native.make_config(energy_range=(-9.5, 9.0), precision="fp64"))
+    ref_sig = eng.kubo_bastin(mu * np.outer(g, g), chem, 0.0, 300).real
+    eng.close()
+    serr = np.abs(sig - ref_sig).max() / np.abs(ref_sig).max()
+    print("torch Kubo-Bastin vs the engine's: %.3e" % serr)
+    assert serr < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_conductivity_gradient_matches_finite_differences():
+    """d sigma / d H through the whole conductivity path -- velocity operators, both Chebyshev
+    chains, the moments matrix, damping and Kubo-Bastin -- by the engine's adjoint and torch
+    autograd, against central differences (one Richardson step) of the forward conductivity on
+    sampled bonds and onsite energies of a strained, disordered flake."""
+    torch = pytest.importorskip("torch")
+    from pybinding_gb300 import jackson_kernel
+    from pybinding_gb300.adjoint import ConductivityMoments, kubo_bastin
+    m = _strained_flake(1500, onsite=0.3)
+    h = sp.csr_matrix(m.hamiltonian, dtype=np.float64)
+    h.sort_indices()
+    n = h.shape[0]
+    rng = np.random.default_rng(9)
+    r0 = rng.choice([-1.0, 1.0], size=(2, n))
+    M = 50
+    chem = np.array([-0.8, -0.2, 0.3, 1.1])
+    c = np.array([1.0, -0.5, 2.0, 0.7])
+    kern = jackson_kernel()
+    op = ConductivityMoments(h, m.system.x, m.system.x, M, r0, (-9.5, 9.0))
+    scaling, bounds = op.scaling, op.energy_bounds
+
+    def loss_t(values):
+        return (torch.from_numpy(c) * kubo_bastin(op(values), chem, scaling, bounds, kern, 0.0, 400)).sum()
+
+    values = torch.tensor(h.data, dtype=torch.float64, requires_grad=True)
+    loss_t(values).backward()
+    gv = values.grad.numpy().copy()
+    # the onsite disorder stores every diagonal entry: onsite gradients are those entries
+    diag_pos = np.array([h.indptr[i] + np.searchsorted(h.indices[h.indptr[i]:h.indptr[i + 1]], i) for i in range(n)])
+    assert np.array_equal(h.indices[diag_pos], np.arange(n))
+    _, go = op.gradient(h.data, np.zeros((M, M)))
+    assert go.shape == (n,) and not np.any(go)
+
+    def loss_np(v, o=op):
+        with torch.no_grad():
+            return float((torch.from_numpy(c) * kubo_bastin(torch.from_numpy(o.moments(v)), chem, scaling, bounds,
+                                                              kern, 0.0, 400)).sum())
+
+    def richardson(f, eps):
+        d1 = (f(eps) - f(-eps)) / (2 * eps)
+        d2 = (f(eps / 2) - f(-eps / 2)) / eps
+        return (4 * d2 - d1) / 3
+
+    scale = np.abs(gv).max()
+    coo = h.tocoo()
+    eps = 1e-4
+    worst = 0.0
+    for k in [k for k in rng.permutation(h.nnz) if coo.row[k] < coo.col[k]][:6]:
+        i, j = coo.row[k], coo.col[k]
+        kt = h.indptr[j] + np.searchsorted(h.indices[h.indptr[j]:h.indptr[j + 1]], i)
+
+        def f(d, k=k, kt=kt):
+            v = h.data.copy()
+            v[k] += d
+            v[kt] += d
+            return loss_np(v)
+        fd = richardson(f, eps)
+        an = gv[k] + gv[kt]
+        worst = max(worst, abs(fd - an) / scale)
+        print("bond (%d,%d): fd %.9e adjoint %.9e" % (i, j, fd, an))
+    for i in rng.choice(n, 4, replace=False):
+        def fo(d, i=i):
+            v = h.data.copy()
+            v[diag_pos[i]] += d
+            return loss_np(v)
+        fd = richardson(fo, eps)
+        worst = max(worst, abs(fd - gv[diag_pos[i]]) / scale)
+        print("onsite %d: fd %.9e adjoint %.9e" % (i, fd, gv[diag_pos[i]]))
+    print("largest |fd - adjoint| / max |grad|: %.3e" % worst)
+    assert worst < 1e-6

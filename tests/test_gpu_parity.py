@@ -109,6 +109,25 @@ def test_ldos_matches_reference_golden(baselines, name):
         np.testing.assert_allclose(ldos.data, baselines["ldos[%s]" % name], rtol=1e-3, atol=1e-6)
 
 
+def test_multi_orbital_ldos_matches_reference_golden(baselines):
+    """The ldos[mos2] golden of tests/test_kpm.py:22-47: three-band MoS2 (three orbitals per site),
+    LDOS of the site nearest (0, 0.07), reduce=False gives one column per orbital and reduce=True
+    their sum (KPM.cpp:55-65); Lorentz kernel, rtol 1e-3, atol 1e-6, every configuration."""
+    m = L.build_tmd_3band(L.rectangle(6), "MoS2")
+    energy = np.linspace(0, 2, 25)
+    expected = baselines["ldos[mos2]"]
+    for cfg in [dict(matrix_format="CSR", optimal_size=False, interleaved=False),
+                dict(matrix_format="CSR", optimal_size=True, interleaved=False),
+                dict(matrix_format="CSR", optimal_size=False, interleaved=True),
+                dict(matrix_format="ELL", optimal_size=True, interleaved=True)]:
+        k = kpm(m, kernel=lorentz_kernel(), silent=True, **cfg)
+        ldos = k.calc_ldos(energy, broadening=0.15, position=[0, 0.07], reduce=False)
+        assert ldos.data.shape == (25, 3)
+        np.testing.assert_allclose(ldos.data, expected, rtol=1e-3, atol=1e-6)
+        summed = k.calc_ldos(energy, broadening=0.15, position=[0, 0.07]).data
+        np.testing.assert_allclose(summed, ldos.data.sum(axis=1), rtol=1e-12, atol=0)
+
+
 def test_ldos_equals_oracle_and_multi_index(oracle):
     """Several LDOS columns in one batch; each equals the oracle's Core::ldos."""
     m = TM.graphene("const_potential", 6)

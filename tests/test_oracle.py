@@ -137,6 +137,24 @@ def test_golden_dos(oracle, baselines, name):
         np.testing.assert_allclose(r, baselines["dos[%s]" % name], rtol=1e-3, atol=1e-6)
 
 
+def test_golden_ldos_mos2(oracle, baselines):
+    """tests/test_kpm.py:22-47, the multi-orbital case: the three-band MoS2 model
+    (group6_tmd.monolayer_3band, restated by lattice.build_tmd_3band) in a 6 nm rectangle, LDOS of
+    the three orbitals of the site nearest (0, 0.07) without reduction (rtol 1e-3, atol 1e-6)."""
+    from pybinding_gb300 import lattice as L
+    m = L.build_tmd_3band(L.rectangle(6), "MoS2")
+    assert m.is_multiorbital and m.hamiltonian.shape == (3 * m.system.num_sites,) * 2
+    idx = m.system.to_hamiltonian_indices(m.system.find_nearest([0, 0.07]))
+    assert idx.size == 3
+    energy = np.linspace(0, 2, 25)
+    for cfg in [dict(matrix_format="CSR", optimal_size=False, interleaved=False),
+                dict(matrix_format="CSR", optimal_size=True, interleaved=False),
+                dict(matrix_format="CSR", optimal_size=False, interleaved=True),
+                dict(matrix_format="ELL", optimal_size=True, interleaved=True)]:
+        r = oracle.core_ldos(m.hamiltonian, idx, energy, 0.15, kernel="lorentz", **cfg)
+        np.testing.assert_allclose(r, baselines["ldos[mos2]"], rtol=1e-3, atol=1e-6)
+
+
 @pytest.mark.parametrize("name", list(TM.COND_MODELS))
 def test_golden_conductivity(oracle, baselines, name):
     """tests/test_kpm.py:176-197 (rtol 1e-2, atol 1e-5)"""
