@@ -78,6 +78,8 @@ def parse():
     p.add_argument("--ldos-sites", type=int, default=4096, help="LDOS sites of the 3D Anderson workload (0: none)")
     p.add_argument("--staging", default="auto", choices=["auto", "registers", "prefetch"],
                    help="diagonal step's matrix entries: per-row loads or staged a chunk ahead (auto = by timing)")
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "fp32x"],
+                   help="FP32 recursion: plain (fp32 = auto) or with compensated row sums (fp32x)")
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2],
                    help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
@@ -268,7 +270,9 @@ def workload_config(args, hs):
             "flakes": args.flakes, "sites": int(sum(h.shape[0] for h in hs)),
             "nnz": int(sum(h.nnz for h in hs)), "vectors_per_flake": args.vectors,
             "moments": int(args.moments + ((4 - (args.moments - 2) % 4) % 4)),
-            "recursion": "fp32 vectors, fp64 moment sums", "bounds": "fp64 Lanczos per flake",
+            "recursion": "fp32 vectors, %sfp64 moment sums" % (
+                "compensated fp32 row sums, " if getattr(args, "precision", "auto") == "fp32x" else ""),
+            "bounds": "fp64 Lanczos per flake",
             "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if args.gpus > 1 else "single"}
 
 
@@ -298,7 +302,7 @@ def run_gpu(args, rank, world, local_rank):
             starters[pos:pos + n] = rademacher(rng, n)
             pos += n
     # Lanczos bounds, Jackson, auto precision (fp32 vectors for an f32 H)
-    cfg = _native.make_config(staging=args.staging, fuse_steps=args.fuse)
+    cfg = _native.make_config(staging=args.staging, fuse_steps=args.fuse, precision=args.precision)
     eng = _native.Engine(h, cfg, system_offsets=offsets)
     for s in range(nsys):
         eng.scaling_factors(s)

@@ -28,17 +28,19 @@ def _rademacher(n, count, seed):
     return np.where(rng.integers(0, 2, size=(count, n)) == 0, -1.0, 1.0).astype(np.float32)
 
 
-def test_fp32_moments_of_a_full_size_flake(oracle):
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-6), ("fp32x", 2e-7)])
+def test_fp32_moments_of_a_full_size_flake(oracle, precision, tol):
     """One flake of the batched DOS workload at its largest size (400k sites, onsite disorder
     U[-0.5, 0.5] eV, float32 H), 64 Rademacher vectors, 4098 moments, Lanczos bounds: the FP32
-    recursion against the FP64 recursion of the same engine settings (bit-identical bounds) on
-    every vector, and both against the FP64 oracle on two vectors with the engine's own (a, b)."""
+    recursion (plain FMA row sums, or compensated row sums rounded once) against the FP64
+    recursion of the same engine settings (bit-identical bounds) on every vector, and both
+    against the FP64 oracle on two vectors with the engine's own (a, b)."""
     m = L.graphene_flake(400_000, onsite_modifiers=[L.anderson_disorder(1.0, 11)])
     h = m.hamiltonian.astype(np.float32)
     n = h.shape[0]
     st = _rademacher(n, 64, 5)
     M = 4096
-    e32 = _native.Engine(h, _native.make_config())
+    e32 = _native.Engine(h, _native.make_config(precision=precision))
     e64 = _native.Engine(h, _native.make_config(precision="fp64"))
     assert e32.energy_bounds() == e64.energy_bounds()  # deterministic Lanczos: the same bits
     a, b = e32.scaling_factors()
@@ -48,17 +50,17 @@ def test_fp32_moments_of_a_full_size_flake(oracle):
     e64.close()
     assert m32.shape == (64, 4098)
     err = rel_err(m32, m64)
-    print("full-size flake (%d sites): FP32 vs FP64 per-vector %.3e, vector-averaged %.3e" % (
-        n, err, rel_err(m32.mean(0), m64.mean(0))))
-    assert err <= 1e-6
+    print("full-size flake (%d sites), %s: vs FP64 per-vector %.3e, vector-averaged %.3e" % (
+        n, precision, err, rel_err(m32.mean(0), m64.mean(0))))
+    assert err <= tol
     r = oracle.optimize(h.astype(np.float64), [0], [0], a, b)
     ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(st[:2].astype(np.float64), r["reorder_map"]), 4098,
                               slices=r["slices"])
     e64o = rel_err(m64[:2], ref)
     e32o = rel_err(m32[:2], ref)
-    print("  vs FP64 oracle (2 vectors): FP64 %.3e, FP32 %.3e" % (e64o, e32o))
+    print("  vs FP64 oracle (2 vectors): FP64 %.3e, %s %.3e" % (e64o, precision, e32o))
     assert e64o <= 1e-10
-    assert e32o <= 1e-6
+    assert e32o <= tol
 
 
 def test_dos_configuration_c128_60k_matches_oracle(oracle):
@@ -225,6 +227,30 @@ def test_spatial_ldos_of_a_3d_anderson_cube_matches_oracle(oracle, dtype, tol):
     err = rel_err(got, ref)
     print("3D Anderson LDOS %s (64 sites): %.3e" % (np.dtype(dtype).name, err))
     assert err <= tol
+
+
+@pytest.mark.parametrize("nvec", [64, 16, 1])
+def test_compensated_rows_match_the_oracle_on_a_ragged_batch(oracle, nvec):
+    """precision fp32x: FP32 vectors whose row sums of H~ x are compensated (error-free products,
+    TwoSum) and rounded once, on a ragged batch of three disordered flakes (row offsets not
+    multiples of 16), first call and replayed recursion graph, against the FP64 oracle."""
+    hs = [_flake(n, s).astype(np.float32) for n, s in ((9001, 21), (4003, 22), (12007, 23))]
+    rng = (-9.5, 9.5)
+    M = 258
+    a, b = oracle.scale(*rng)
+    starters = [oracle.random_starters(h.shape[0], nvec, np.float32) for h in hs]
+    flat = np.concatenate([st.ravel() for st in starters])
+    batch = kpm_batch([L.Model(h, None) for h in hs], energy_range=rng, precision="fp32x")
+    got = [batch.engine.moments_diag(M, flat), batch.engine.moments_diag(M, flat)]
+    batch.close()
+    for s, h in enumerate(hs):
+        r = oracle.optimize(h.astype(np.float64), [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(np.float64), r["reorder_map"]), M,
+                                  slices=r["slices"])
+        for k in (0, 1):
+            err = rel_err(got[k][s], ref)
+            print("fp32x K=%d system %d call %d: %.3e" % (nvec, s, k, err))
+            assert err <= 1e-7
 
 
 @pytest.mark.parametrize("dtype,nvec,tol", [(np.float32, 64, 1e-6), (np.float64, 16, 1e-10),
