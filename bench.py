@@ -3,7 +3,8 @@
 Workload (default): 32 Anderson-disordered graphene flakes of uneven size
 (sites drawn uniformly in [50k, 400k], onsite energies uniform in
 [-0.5, 0.5] eV), 64 Rademacher starters per flake, 4096 moments (rounded to
-4098 as the reference does), FP32 recursion vectors with FP64 moment sums,
+4098 as the reference does), FP32 recursion vectors (row sums of exactly split
+products) with FP64 moment sums,
 spectral bounds by FP64 Lanczos. All flakes and vectors advance together:
 every Chebyshev step is one kernel launch over the block-diagonal matrix.
 
@@ -78,8 +79,9 @@ def parse():
     p.add_argument("--ldos-sites", type=int, default=4096, help="LDOS sites of the 3D Anderson workload (0: none)")
     p.add_argument("--staging", default="auto", choices=["auto", "registers", "prefetch"],
                    help="diagonal step's matrix entries: per-row loads or staged a chunk ahead (auto = by timing)")
-    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "fp32x"],
-                   help="FP32 recursion: plain (fp32 = auto) or with compensated row sums (fp32x)")
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "fp32p", "fp32x"],
+                   help="FP32 recursion row sums: chained FMAs (fp32), exactly split products (fp32p = auto) "
+                        "or compensated (fp32x)")
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2],
                    help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
@@ -270,8 +272,9 @@ def workload_config(args, hs):
             "flakes": args.flakes, "sites": int(sum(h.shape[0] for h in hs)),
             "nnz": int(sum(h.nnz for h in hs)), "vectors_per_flake": args.vectors,
             "moments": int(args.moments + ((4 - (args.moments - 2) % 4) % 4)),
-            "recursion": "fp32 vectors, %sfp64 moment sums" % (
-                "compensated fp32 row sums, " if getattr(args, "precision", "auto") == "fp32x" else ""),
+            "recursion": "fp32 vectors, %s, fp64 moment sums" % (
+                {"fp32x": "compensated fp32 row sums", "fp32": "fp32 row sums of chained FMAs"}.get(
+                    getattr(args, "precision", "auto"), "fp32 row sums of exactly split products (auto)")),
             "bounds": "fp64 Lanczos per flake",
             "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if args.gpus > 1 else "single"}
 
@@ -385,53 +388,67 @@ def run_gpu(args, rank, world, local_rank):
         e2e = {"value": rate_e / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(starters.nbytes), "d2h_bytes_per_step": int(nsys * M * 16)}
 
-    # the same workload in the plain FP64 recursion (the other half of the metric): timed on the
-    # device like `value`, then its moments are the error reference of the FP32 ones (the two
-    # engines' Lanczos bounds are the same bits: its sums run in a fixed order)
+    def variant(prec, elem_bytes):
+        """The same workload in another recursion precision, timed on the device like `value`:
+        its line entry, its per-vector moments and whether its Lanczos bounds are the same bits."""
+        e = _native.Engine(h, _native.make_config(precision=prec), system_offsets=offsets)
+        same = all(e.energy_bounds(s) == bounds32[s] for s in range(nsys))
+        sv = torch.cuda.ExternalStream(e.stream())
+
+        def run():
+            return e.moments_diag(args.moments, None, average=False, on_device_ptr=d_st.data_ptr(), num_vectors=R)
+
+        mu = run()  # warm (tuning) + the moments
+        nv = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(sv)
+        recs = []
+        for _ in range(nv):
+            run()
+            recs.append(e.stats().moments_time)
+        g1.record(sv)
+        torch.cuda.synchronize()
+        tv = g0.elapsed_time(g1) * 1e-3 / nv
+        sv_st = e.stats()
+        fz = int(sv_st.steps_per_launch)
+        nl = 1 + (M // 2 - 1) // fz
+        alg_v = nnz * (8 + 4) + 4 * (nrows + 1) + (3 if fz == 1 else 4) * nrows * R * elem_bytes
+        avg_v = float(np.median(recs)) / nl
+        out = {"value": work / tv / 1e9, "unit": UNIT, "ms_per_step": tv * 1e3, "timed_steps": nv,
+               "kernel": "%s<%s,%d,%d>" % ("diag_step_kernel" if fz == 1 else "diag_pair_kernel",
+                                           "double" if elem_bytes == 8 else "float", int(sv_st.elems_per_lane),
+                                           int(sv_st.lanes_per_row)),
+               "roofline": {"bound": "hbm", "achieved": alg_v / avg_v / 1e9, "peak": peak, "unit": "GB/s",
+                            "frac": alg_v / avg_v / 1e9 / peak, "alg_bytes_per_launch": alg_v,
+                            "avg_launch_ms": avg_v * 1e3}}
+        e.close()
+        return out, mu, same
+
+    def errors(m, ref):
+        # per-vector moments, and the stochastic-trace moments (average over the vectors of a
+        # flake, as the reference's BatchAccumulator returns them), each relative to its max |mu|
+        return {"per_vector_max": float(np.max(np.abs(m - ref)) / np.max(np.abs(ref))),
+                "vector_averaged_max": float(np.max(np.abs(m.mean(1) - ref.mean(1))) / np.max(np.abs(ref.mean(1))))}
+
+    # the plain FP64 recursion of the same workload (the other half of the metric), whose moments
+    # are the error reference of the FP32 ones (the engines' Lanczos bounds are the same bits:
+    # their sums run in a fixed order), and the FP32 recursion with chained-FMA row sums
     err = None
     fp64 = None
+    fp32_fma = None
     if not args.no_error:
         m32 = eng.moments_diag(args.moments, None, average=False, on_device_ptr=d_st.data_ptr(), num_vectors=R)
         bounds32 = [eng.energy_bounds(s) for s in range(nsys)]
         scales = [eng.scaling_factors(s) for s in range(nsys)]
         eng.close()
-        e64 = _native.Engine(h, _native.make_config(precision="fp64"), system_offsets=offsets)
-        same_bounds = all(e64.energy_bounds(s) == bounds32[s] for s in range(nsys))
-        s64 = torch.cuda.ExternalStream(e64.stream())
-
-        def step64():
-            return e64.moments_diag(args.moments, None, average=False, on_device_ptr=d_st.data_ptr(), num_vectors=R)
-
-        m64 = step64()  # warm (tuning) + the reference moments
-        n64 = max(1, min(args.steps, 3))
-        torch.cuda.synchronize()
-        g0 = torch.cuda.Event(enable_timing=True)
-        g1 = torch.cuda.Event(enable_timing=True)
-        g0.record(s64)
-        rec64 = []
-        for _ in range(n64):
-            step64()
-            rec64.append(e64.stats().moments_time)
-        g1.record(s64)
-        torch.cuda.synchronize()
-        t64 = g0.elapsed_time(g1) * 1e-3 / n64
-        st64 = e64.stats()
-        fuse64 = int(st64.steps_per_launch)
-        launches64 = 1 + (M // 2 - 1) // fuse64
-        alg64 = nnz * (8 + 4) + 4 * (nrows + 1) + (3 if fuse64 == 1 else 4) * nrows * R * 8
-        avg64 = float(np.median(rec64)) / launches64
-        fp64 = {"value": work / t64 / 1e9, "unit": UNIT, "ms_per_step": t64 * 1e3, "timed_steps": n64,
-                "kernel": "%s<double,%d,%d>" % ("diag_step_kernel" if fuse64 == 1 else "diag_pair_kernel",
-                                                 int(st64.elems_per_lane), int(st64.lanes_per_row)),
-                "roofline": {"bound": "hbm", "achieved": alg64 / avg64 / 1e9, "peak": peak, "unit": "GB/s",
-                             "frac": alg64 / avg64 / 1e9 / peak, "alg_bytes_per_launch": alg64,
-                             "avg_launch_ms": avg64 * 1e3}}
-        e64.close()
-        # per-vector moments, and the stochastic-trace moments (average over the vectors of a
-        # flake, as the reference's BatchAccumulator returns them), each relative to its max |mu|
-        err = {"per_vector_max": float(np.max(np.abs(m32 - m64)) / np.max(np.abs(m64))),
-               "vector_averaged_max": float(np.max(np.abs(m32.mean(1) - m64.mean(1))) / np.max(np.abs(m64.mean(1)))),
-               "reference": "FP64 recursion of the same workload (GPU), identical Lanczos bounds: %s" % same_bounds}
+        fp64, m64, same_bounds = variant("fp64", 8)
+        err = errors(m32, m64)
+        err["reference"] = "FP64 recursion of the same workload (GPU), identical Lanczos bounds: %s" % same_bounds
+        if args.precision != "fp32":
+            fp32_fma, mf, _ = variant("fp32", 4)
+            fp32_fma["moment_error_vs_fp64"] = errors(mf, m64)
     else:
         eng.close()
 
@@ -465,6 +482,7 @@ def run_gpu(args, rank, world, local_rank):
                             "avg_launch_ms": avg_launch * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
                "cpu_baseline": cpu,
                "fp64": fp64,
+               "fp32_chained_fma": fp32_fma,
                "e2e": e2e,
                "clocks": clk,
                "gpu_launches": int(args.steps * (launches + 3))}
@@ -539,10 +557,20 @@ def workload_dos_c128_60k(args, stream_of):
     work = (M / 2) * h.nnz * 8
     rec = st.moments_time
     steps = M // 2
-    spl = max(1, int(st.steps_per_launch))  # all steps after the first in one launch when > 2
+    spl = max(1, int(st.steps_per_launch))  # 1 or 2 steps per launch
     launches = 1 + -(-(steps - 1) // spl)
     alg = h.nnz * 20 + 4 * (h.shape[0] + 1) + 3 * h.shape[0] * 8 * 16  # per step
     achieved = alg / (rec / steps) / 1e9
+    err = None
+    if not args.no_error:  # the reference's 8 random-phase starters: engine moments against the FP64 oracle
+        from oracle import oracle as O
+        st_ref = O.random_starters(h.shape[0], 8, np.complex128)
+        mu = eng.moments_diag(2048, st_ref[None])[0]
+        r = O.optimize(h, [0], [0], a, b)
+        ref = O.moments_diag(r["h2"], O.reorder_vector(st_ref, r["reorder_map"]), mu.shape[1], slices=r["slices"])
+        err = {"per_vector_max_vs_oracle": float(np.max(np.abs(mu - ref)) / np.max(np.abs(ref))),
+               "vectors": 8, "moments": int(mu.shape[1]),
+               "starters": "the reference's random-phase starters (std::mt19937 default seed)"}
     cpu = None
     if args.cpu_seconds > 0:
         from oracle import oracle as O
@@ -568,11 +596,10 @@ def workload_dos_c128_60k(args, stream_of):
           roofline={"bound": "l2 (latency)", "achieved": achieved, "unit": "GB/s",
                     "note": "working set fits in L2; HBM fraction not meaningful",
                     "avg_step_us": rec / steps * 1e6, "alg_bytes_per_step": alg, "steps_per_launch": spl,
-                    "kernel": "diag_multi_kernel (all steps, one cooperative launch)" if spl > 2 else
-                              "diag_step_kernel"},
+                    "kernel": "diag_step_kernel" if spl == 1 else "diag_pair_kernel"},
           e2e={"value": work / (wall / args.steps) / 1e9, "unit": "Gnnz*vec/s", "h2d_bytes_per_step": 8000,
                "d2h_bytes_per_step": 8000},
-          cpu_baseline=cpu, clocks=clk, time_per_dos_ms=t / args.steps * 1e3,
+          moment_error_vs_fp64=err, cpu_baseline=cpu, clocks=clk, time_per_dos_ms=t / args.steps * 1e3,
           gpu_launches=int(args.steps * (launches + 4)))
 
 
@@ -600,6 +627,16 @@ def workload_conductivity(args, stream_of):
         deviation = float(np.max(np.abs(outs[-1].real - s64)) / np.max(np.abs(s64)))
         eng.calc_conductivity(x, x, chem, broadening, 0.0, 16, 1000, gemm_mode=1)  # stats of this engine again
     st = eng.stats()
+    gemm_dev = None
+    if not args.no_error:  # one random vector: tcgen05 split-TF32 mu_mn against the FP64 CUDA-core GEMM
+        s_tc = eng.calc_conductivity(x, x, chem, broadening, 0.0, 1, 1000, gemm_mode=1).real
+        s_64 = eng.calc_conductivity(x, x, chem, broadening, 0.0, 1, 1000, gemm_mode=0).real
+        gemm_dev = {"sigma_rel_deviation_tc_vs_fp64_gemm": float(np.max(np.abs(s_tc - s_64)) / np.max(np.abs(s_64))),
+                    "vectors": 1,
+                    "note": "the recursion is FP64 (complex128) in both; its moments equal the FP64 oracle to "
+                            "<1e-13 on the configuration's graphene flakes (tests)"}
+        eng.calc_conductivity(x, x, chem, broadening, 0.0, 16, 1000, gemm_mode=1)
+        st = eng.stats()
     M = st.num_moments
     n = h.shape[0]
     I = n * 16
@@ -626,7 +663,8 @@ def workload_conductivity(args, stream_of):
                      "reconstruction_and_host_s": t / args.steps - st.moments_time},
           e2e={"value": wall / args.steps, "unit": "s", "h2d_bytes_per_step": int(8 * n + 8 * 31),
                "d2h_bytes_per_step": int(16 * 31)},
-          sigma_sample=[float(v.real) for v in outs[-1][:5]], sigma_rel_deviation_vs_fp64=deviation, clocks=clk,
+          sigma_sample=[float(v.real) for v in outs[-1][:5]], sigma_rel_deviation_vs_fp64=deviation,
+          moment_error_vs_fp64=gemm_dev, clocks=clk,
           gpu_launches=int(args.steps * (2 * (M + 2) + 6)))
 
 
@@ -719,6 +757,31 @@ def workload_anderson3d(args, stream_of):
     alg = h.nnz * 12 + 4 * (n + 1) + vec_bytes
     avg = s.moments_time / launches
     peak = float(_peaks().get("hbm_gbs", 6800.0))
+    err = None
+    if not args.no_error:
+        R8 = min(8, R)
+        st8 = st[:R8]
+        m32 = eng.moments_diag(args.cube_moments, st8[None])[0]
+        e64 = _native.Engine(h, _native.make_config(precision="fp64"))
+        assert e64.energy_bounds() == eng.energy_bounds()
+        m64 = e64.moments_diag(args.cube_moments, st8[None])[0]
+        from oracle import oracle as O
+        a, b = eng.scaling_factors()
+        Mo = 130
+        r = O.optimize(h.astype(np.float64), [0], [0], a, b)
+        ref = O.moments_diag(r["h2"], O.reorder_vector(st8[:1].astype(np.float64), r["reorder_map"]), Mo,
+                             slices=r["slices"])
+        m64o = e64.moments_diag(Mo, st8[None, :1])[0]
+        e64.close()
+        err = {"per_vector_max": float(np.max(np.abs(m32 - m64)) / np.max(np.abs(m64))), "vectors": R8,
+               "moments": int(m32.shape[1]),
+               "vector_averaged": float(np.max(np.abs(m32.mean(0) - m64.mean(0))) / np.max(np.abs(m64.mean(0)))),
+               "fp64_vs_oracle": float(np.max(np.abs(m64o - ref)) / np.max(np.abs(ref))),
+               "fp64_vs_oracle_moments": Mo,
+               "reference": "the engine's FP64 recursion on the same vectors and bounds; that recursion against "
+                            "the FP64 oracle on one vector"}
+        eng.moments_diag(args.cube_moments, None, average=True, on_device_ptr=d_st.data_ptr(), num_vectors=R)
+        s = eng.stats()
     t_ldos = None
     if args.ldos_sites > 0:
         sites = rng.choice(n, args.ldos_sites, replace=False)
@@ -740,7 +803,7 @@ def workload_anderson3d(args, stream_of):
                     "unroll": int(s.unroll),
                     "alg_bytes_per_launch": alg, "avg_launch_ms": avg * 1e3,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-          ldos_sites=args.ldos_sites, ldos_1024_moments_s=t_ldos, clocks=clk,
+          moment_error_vs_fp64=err, ldos_sites=args.ldos_sites, ldos_1024_moments_s=t_ldos, clocks=clk,
           gpu_launches=int(args.steps * (launches + 3)))
 
 

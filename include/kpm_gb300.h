@@ -43,11 +43,14 @@ extern "C" {
 #define KPM_KERNEL_DIRICHLET 2
 
 /* recursion precision */
-#define KPM_PREC_AUTO 0   /* f32/c64 H: FP32 vectors + FP64 moment sums; f64/c128 H: FP64 */
+#define KPM_PREC_AUTO 0   /* f32 H: as KPM_PREC_FP32P; c64 H: as KPM_PREC_FP32; f64/c128 H: FP64 */
 #define KPM_PREC_FP64 1   /* FP64 (f64 or c128) vectors, values and sums */
-#define KPM_PREC_FP32 2   /* FP32 (f32 or c64) vectors and values, FP64 moment sums */
+#define KPM_PREC_FP32 2   /* FP32 (f32 or c64) vectors and values, FP64 moment sums; row sums of
+                             H~ x as chained FMAs */
 #define KPM_PREC_FP32X 3  /* as KPM_PREC_FP32, and for real H each row sum of H~ x compensated
                              (error-free products and sums) and rounded once */
+#define KPM_PREC_FP32P 4  /* as KPM_PREC_FP32, and for real H the products of each row sum of H~ x
+                             exact (FMA split), the rounded products summed in FP32 */
 
 /* matrix formats accepted for API compatibility (kpm/Config.hpp:7) */
 #define KPM_FORMAT_CSR 0

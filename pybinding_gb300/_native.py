@@ -21,7 +21,7 @@ KPM_OK, KPM_ERR_RUNTIME, KPM_ERR_VALUE, KPM_ERR_CUDA, KPM_ERR_TIMEOUT = 0, 1, 2,
 SCALAR_CODE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1,
                np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
 KERNEL_CODE = {"jackson": 0, "lorentz": 1, "dirichlet": 2}
-PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2, "fp32x": 3}
+PRECISION_CODE = {"auto": 0, "fp64": 1, "fp32": 2, "fp32x": 3, "fp32p": 4}
 STAGING_CODE = {"auto": 0, "registers": 1, "prefetch": 2}
 
 

@@ -391,7 +391,9 @@ def kpm(model, energy_range=None, kernel="default", num_threads="auto", silent=F
 
     Extra keyword arguments of ``_cpp.kpm`` are accepted: ``matrix_format``,
     ``optimal_size``, ``interleaved``, ``lanczos_precision``; plus the GPU knobs
-    ``precision`` ("auto", "fp64", "fp32"), ``batch_width`` and ``moments_gemm``
+    ``precision`` ("auto"; "fp64"; FP32 vectors with row sums of chained FMAs "fp32", of exactly
+    split products "fp32p" -- the automatic choice for a float32 H -- or compensated "fp32x"),
+    ``batch_width`` and ``moments_gemm``
     ("fp64": the conductivity's moments matrix on the FP64 CUDA cores; "tensor": on
     the tensor cores from FP32 planes, three-product TF32 split). ``num_threads`` is the
     number of host threads for the engine's setup work (the recursion runs on the GPU).

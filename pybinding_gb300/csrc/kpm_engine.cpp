@@ -968,7 +968,8 @@ struct kpm_engine {
         int vtype, E, LPR, nbatch;
         int64_t rows, nnz;
         int W, staging, device;
-        bool full_rows, real, comp;
+        bool full_rows, real;
+        int comp;
         bool operator==(TuneKey const& o) const {
             return vtype == o.vtype && E == o.E && LPR == o.LPR && nbatch == o.nbatch && rows == o.rows &&
                    nnz == o.nnz && W == o.W && staging == o.staging && device == o.device &&
@@ -982,8 +983,13 @@ struct kpm_engine {
                        compensated()};
     }
     struct Tuned { int rows_per_tile, unroll, E, LPR, prefetch = 0; };
-    // FP32 real recursions with compensated row sums (KPM_PREC_FP32X)
-    bool compensated() const { return vtype == kpm::V_F32 && cfg.precision == KPM_PREC_FP32X; }
+    // FP32 real recursions: row sums with exact products (1: KPM_PREC_FP32P, and the automatic
+    // precision of a float32 H) or compensated (2: KPM_PREC_FP32X); 0 = chained FMAs
+    int compensated() const {
+        if (vtype != kpm::V_F32) return 0;
+        if (cfg.precision == KPM_PREC_FP32X) return 2;
+        return (cfg.precision == KPM_PREC_FP32P || cfg.precision == KPM_PREC_AUTO) ? 1 : 0;
+    }
     // steps per launch chosen by timing the first steps of a recursion: 1, or 2 with a tile height
     struct FuseChoice { int steps, rows_per_tile; };
     template<class T>
@@ -1030,7 +1036,7 @@ struct kpm_engine {
             for (auto const& mp : maps)
                 for (int unroll : {1, 2})
                     for (int rpt : {1, 2, 4, 8, 16, 32, 64}) {
-                        if (rpt < 2 * unroll || cfg.staging == 2 || (compensated() && unroll != 1)) continue;
+                        if (rpt < 2 * unroll || cfg.staging == 2 || (compensated() == 2 && unroll != 1)) continue;
                         Shape t = sh;
                         t.E = mp.first;
                         t.LPR = mp.second;
@@ -1058,7 +1064,7 @@ struct kpm_engine {
             base.LPR = sh.LPR;
             for (int pf : {3, 4})
                 for (int chunks : {1, 2, 4, 8}) {
-                    if (cfg.staging == 1 || compensated()) break;
+                    if (cfg.staging == 1 || compensated() == 2) break;
                     Shape t = sh;
                     t.rows_per_tile = 128 * chunks;
                     base.num_tiles = build_tiles(first_batch(t), sys0, batch_outer);
@@ -1614,7 +1620,7 @@ int kpm_create(int32_t scalar_type, int64_t rows, const int32_t* indptr, const i
             fail(KPM_ERR_VALUE, "KPM: Invalid energy range specified (min > max).");
         if (e->cfg.kernel == KPM_KERNEL_LORENTZ && e->cfg.kernel_param <= 0)
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
-        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32X)
+        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32P)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
         if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");
@@ -1647,7 +1653,7 @@ int kpm_create_batch(kpm_engine* const* engines, int32_t num_engines, const kpm_
             fail(KPM_ERR_VALUE, "KPM: Invalid energy range specified (min > max).");
         if (e->cfg.kernel == KPM_KERNEL_LORENTZ && e->cfg.kernel_param <= 0)
             fail(KPM_ERR_VALUE, "Lorentz kernel: lambda must be positive.");
-        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32X)
+        if (e->cfg.precision < KPM_PREC_AUTO || e->cfg.precision > KPM_PREC_FP32P)
             fail(KPM_ERR_VALUE, "unknown precision mode");
         if (e->cfg.fuse_steps < 0 || e->cfg.fuse_steps > 2) fail(KPM_ERR_VALUE, "fuse_steps must be 0, 1 or 2");
         if (e->cfg.staging < 0 || e->cfg.staging > 2) fail(KPM_ERR_VALUE, "staging must be 0, 1 or 2");

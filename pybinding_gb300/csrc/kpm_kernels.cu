@@ -183,7 +183,103 @@ __device__ __forceinline__ void two_sum_term(float& sum, float& lo, float h, flo
     lo = fmaf(hl, x, __fadd_rn(lo, __fadd_rn(err, pe)));
 }
 
-template<class V, int E, int LPR, bool INIT, int U, bool XCOH = false, class MV = V, bool CR = false>
+// Row sum of H~ x with exact products (CR = 1): each product h x is split exactly into
+// fl(h x) + e by an FMA; the rounded products are summed in FP32 and the parts e, with the
+// low halves of the matrix values, in a second FP32 word. The rounding of the products --
+// large against a row sum that cancels, as the rows of high Chebyshev vectors do -- is then
+// gone; what remains is the rounding of the running sum. Measured (NumPy emulation of these
+// operations, 395k-site flake, 4098 moments): 3.8e-7 of max |mu| per vector against 1.4e-6
+// with chained FMAs and 4.5e-8 with the row sum rounded once.
+__device__ __forceinline__ void exact_product_term(float& sum, float& lo, float h, float hl, float x) {
+    float const p = __fmul_rn(h, x);
+    float const pe = fmaf(h, x, -p);  // h x - fl(h x), exact
+    sum = __fadd_rn(sum, p);
+    lo = fmaf(hl, x, __fadd_rn(lo, pe));
+}
+
+// The FP32 row arithmetic two vectors at a time: sm_100 and later issue FP32 add, multiply and
+// FMA on pairs (__fadd2_rn, __fmul2_rn, __ffma2_rn), one instruction for two of a lane's E
+// vectors. Each element rounds as its scalar operation does, so the results are the same bits.
+// CR: 0 chained FMAs, 1 exact products (exact_product_term), 2 compensated (two_sum_term).
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+template<int E, int CR>
+__device__ __forceinline__ void row_terms_f32(float (&sum)[E], float (&lo)[E], float h, float hl,
+                                              Pack<float, E> const& x) {
+    if constexpr (E % 2 != 0) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            if constexpr (CR == 2) two_sum_term(sum[e], lo[e], h, hl, x.v[e]);
+            else if constexpr (CR == 1) exact_product_term(sum[e], lo[e], h, hl, x.v[e]);
+            else { sum[e] = fmaf(h, x.v[e], sum[e]); lo[e] = fmaf(hl, x.v[e], lo[e]); }
+        }
+    } else {
+        float2 const h2 = make_float2(h, h);
+        float2 const hl2 = make_float2(hl, hl);
+#pragma unroll
+        for (int k = 0; k < E; k += 2) {
+            float2 const xv = make_float2(x.v[k], x.v[k + 1]);
+            float2 s = make_float2(sum[k], sum[k + 1]);
+            float2 l = make_float2(lo[k], lo[k + 1]);
+            if constexpr (CR == 0) {
+                s = __ffma2_rn(h2, xv, s);
+                l = __ffma2_rn(hl2, xv, l);
+            } else {
+                float2 const p = __fmul2_rn(h2, xv);
+                float2 const pe = __ffma2_rn(h2, xv, neg2(p));  // h x - fl(h x), exact
+                if constexpr (CR == 1) {
+                    s = __fadd2_rn(s, p);
+                    l = __ffma2_rn(hl2, xv, __fadd2_rn(l, pe));
+                } else {  // Knuth's TwoSum of s + p
+                    float2 const s1 = __fadd2_rn(s, p);
+                    float2 const bb = __fadd2_rn(s1, neg2(s));
+                    float2 const err = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(s1, neg2(bb)))), __fadd2_rn(p, neg2(bb)));
+                    s = s1;
+                    l = __ffma2_rn(hl2, xv, __fadd2_rn(l, __fadd2_rn(err, pe)));
+                }
+            }
+            sum[k] = s.x;
+            sum[k + 1] = s.y;
+            lo[k] = l.x;
+            lo[k + 1] = l.y;
+        }
+    }
+}
+
+// y_new = (sum + lo) - y_old (or (sum + lo) / 2 for the first step), and the moment sums
+// m2 += x_r^2, m3 += y_new x_r, two vectors at a time
+template<int E, bool INIT>
+__device__ __forceinline__ void row_finish_f32(float const (&sum)[E], float const (&lo)[E], Pack<float, E> const& yo,
+                                               Pack<float, E> const& xr, Pack<float, E>& yn, float (&m2)[E],
+                                               float (&m3)[E]) {
+    if constexpr (E % 2 != 0) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            float const sv = sum[e] + lo[e];
+            yn.v[e] = INIT ? 0.5f * sv : sv - yo.v[e];
+            m2[e] = fmaf(xr.v[e], xr.v[e], m2[e]);
+            m3[e] = fmaf(yn.v[e], xr.v[e], m3[e]);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < E; k += 2) {
+            float2 const sv = __fadd2_rn(make_float2(sum[k], sum[k + 1]), make_float2(lo[k], lo[k + 1]));
+            float2 const y = INIT ? __fmul2_rn(sv, make_float2(0.5f, 0.5f))
+                                  : __fadd2_rn(sv, neg2(make_float2(yo.v[k], yo.v[k + 1])));
+            yn.v[k] = y.x;
+            yn.v[k + 1] = y.y;
+            float2 const xv = make_float2(xr.v[k], xr.v[k + 1]);
+            float2 const a = __ffma2_rn(xv, xv, make_float2(m2[k], m2[k + 1]));
+            float2 const b = __ffma2_rn(y, xv, make_float2(m3[k], m3[k + 1]));
+            m2[k] = a.x;
+            m2[k + 1] = a.y;
+            m3[k] = b.x;
+            m3[k + 1] = b.y;
+        }
+    }
+}
+
+template<class V, int E, int LPR, bool INIT, int U, bool XCOH = false, class MV = V, int CR = 0>
 __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
                                           V const* __restrict__ x, V* __restrict__ y, int const (&rr)[U],
                                           bool const (&live)[U], int lane, typename Tr<V>::R (&m2)[E],
@@ -229,12 +325,10 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
                 if (!(live[u] && j0 + q < W)) continue;
                 MV const* vp = val + (static_cast<int64_t>(rr[u]) * W + j0 + q) * VS;
                 MV const a = vp[0];
-                if constexpr (CR) {
-                    static_assert(std::is_same_v<V, float> && std::is_same_v<MV, float>, "compensated rows are FP32");
-                    MV const b = vp[1];
-#pragma unroll
-                    for (int e = 0; e < E; ++e) two_sum_term(sum[u][e], lo[u][e], a, b, xv[u][q].v[e]);
+                if constexpr (std::is_same_v<V, float> && std::is_same_v<MV, float>) {  // (hi, lo) values
+                    row_terms_f32<E, CR>(sum[u], lo[u], a, vp[1], xv[u][q]);
                 } else {
+                    static_assert(CR == 0, "compensated rows are FP32");
 #pragma unroll
                     for (int e = 0; e < E; ++e) vfma(sum[u][e], a, xv[u][q].v[e]);
                     if (VS == 2) {
@@ -249,18 +343,22 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
     for (int u = 0; u < U; ++u) {
         if (!live[u]) continue;
         P yn;
+        if constexpr (std::is_same_v<V, float>) {
+            row_finish_f32<E, INIT>(sum[u], lo[u], yo[u], xr[u], yn, m2, m3r);
+        } else {
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            V const s = (VS == 2) ? vadd(sum[u][e], lo[u][e]) : sum[u][e];
-            yn.v[e] = INIT ? vhalf(s) : vsub(s, yo[u].v[e]);
+            for (int e = 0; e < E; ++e) {
+                V const s = (VS == 2) ? vadd(sum[u][e], lo[u][e]) : sum[u][e];
+                yn.v[e] = INIT ? vhalf(s) : vsub(s, yo[u].v[e]);
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                m2[e] += vsq(xr[u].v[e]);
+                m3r[e] += vdre(yn.v[e], xr[u].v[e]);
+                if (CPLX) m3i[e] += vdim(yn.v[e], xr[u].v[e]);
+            }
         }
         st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(rr[u]) * K) + lane, yn);
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            m2[e] += vsq(xr[u].v[e]);
-            m3r[e] += vdre(yn.v[e], xr[u].v[e]);
-            if (CPLX) m3i[e] += vdim(yn.v[e], xr[u].v[e]);
-        }
     }
 }
 
@@ -311,9 +409,9 @@ __device__ __forceinline__ void diag_flush(typename Tr<V>::R (&m2)[E], typename 
     for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
 }
 
-// CR kernels are held to 4 resident blocks per SM (64 registers, no spills; 77 otherwise)
-template<class V, int E, int LPR, bool INIT, int U, class MV = V, bool CR = false>
-__global__ void __launch_bounds__(BLOCK, CR ? 4 : 1)
+// kernels with exact-product or compensated rows are held to 4 resident blocks per SM (64 registers)
+template<class V, int E, int LPR, bool INIT, int U, class MV = V, int CR = 0>
+__global__ void __launch_bounds__(BLOCK, CR != 0 ? 4 : 1)
 diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
                  V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
                  Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
@@ -395,7 +493,7 @@ template<class MV, int LPR>
 size_t pf_smem_bytes(int W) { return static_cast<size_t>(WARPS) * 2 * pf_buf_words<MV, LPR>(W) * 4; }
 constexpr size_t PF_SMEM_MAX = 160 * 1024;  // wider rows use the per-row-load step
 
-template<class V, int E, int LPR, bool INIT, int MINB, class MV = V>
+template<class V, int E, int LPR, bool INIT, int MINB, class MV = V, int RS = 0>
 __global__ void __launch_bounds__(BLOCK, MINB)
 diag_pf_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
                V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
@@ -504,28 +602,36 @@ diag_pf_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int 
                     for (int q = 0; q < 4; ++q) {
                         if (j0 + q >= W) continue;
                         MV const a = vrow[(j0 + q) * VS];
+                        if constexpr (std::is_same_v<V, float> && std::is_same_v<MV, float>) {
+                            row_terms_f32<E, RS>(sum, lo, a, vrow[(j0 + q) * VS + 1], xv[q]);
+                        } else {
 #pragma unroll
-                        for (int e = 0; e < E; ++e) vfma(sum[e], a, xv[q].v[e]);
-                        if (VS == 2) {
-                            MV const bl = vrow[(j0 + q) * VS + 1];
+                            for (int e = 0; e < E; ++e) vfma(sum[e], a, xv[q].v[e]);
+                            if (VS == 2) {
+                                MV const bl = vrow[(j0 + q) * VS + 1];
 #pragma unroll
-                            for (int e = 0; e < E; ++e) vfma(lo[e], bl, xv[q].v[e]);
+                                for (int e = 0; e < E; ++e) vfma(lo[e], bl, xv[q].v[e]);
+                            }
                         }
                     }
                 }
                 P yn;
+                if constexpr (std::is_same_v<V, float>) {
+                    row_finish_f32<E, INIT>(sum, lo, yo, xr, yn, m2, m3r);
+                } else {
 #pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
-                    yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
+                    for (int e = 0; e < E; ++e) {
+                        V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
+                        yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
+                    }
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                        m2[e] += vsq(xr.v[e]);
+                        m3r[e] += vdre(yn.v[e], xr.v[e]);
+                        if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
+                    }
                 }
                 st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    m2[e] += vsq(xr.v[e]);
-                    m3r[e] += vdre(yn.v[e], xr.v[e]);
-                    if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
-                }
             }
             __syncwarp();  // the buffer is refilled two chunks later
             pti = nti;
@@ -1088,7 +1194,7 @@ int persistent_grid(void const* fn, int num_tiles, size_t smem) {
     return std::max(1, std::min(num_tiles, sms * per_sm));
 }
 
-template<class V, int E, int LPR, class MV = V>
+template<class V, int E, int LPR, class MV = V, int CR = 0>
 cudaError_t diag_launch_pf(DiagStep const& a, cudaStream_t s) {
     auto const* val = static_cast<MV const*>(a.val);
     auto const* x = static_cast<V const*>(a.x);
@@ -1109,14 +1215,14 @@ cudaError_t diag_launch_pf(DiagStep const& a, cudaStream_t s) {
     // MINB: blocks per SM the register allocation is held to (3, or 4 with a few spilled words
     // of loop state for the FP32 64-vector shape), timed by the autotuner
     if (a.prefetch >= 4) {
-        if (a.init) return run(diag_pf_kernel<V, E, LPR, true, 4, MV>);
-        return run(diag_pf_kernel<V, E, LPR, false, 4, MV>);
+        if (a.init) return run(diag_pf_kernel<V, E, LPR, true, 4, MV, CR>);
+        return run(diag_pf_kernel<V, E, LPR, false, 4, MV, CR>);
     }
-    if (a.init) return run(diag_pf_kernel<V, E, LPR, true, 3, MV>);
-    return run(diag_pf_kernel<V, E, LPR, false, 3, MV>);
+    if (a.init) return run(diag_pf_kernel<V, E, LPR, true, 3, MV, CR>);
+    return run(diag_pf_kernel<V, E, LPR, false, 3, MV, CR>);
 }
 
-template<class V, int E, int LPR, int U, class MV = V, bool CR = false>
+template<class V, int E, int LPR, int U, class MV = V, int CR = 0>
 cudaError_t diag_launch_u(DiagStep const& a, cudaStream_t s) {
     auto const* val = static_cast<MV const*>(a.val);
     auto const* x = static_cast<V const*>(a.x);
@@ -1297,11 +1403,15 @@ cudaError_t diag_launch(DiagStep const& a, cudaStream_t s) {
             return cudaErrorInvalidValue;
         }
     }
-    if (a.compensated) {  // FP32 real vectors only, one row per thread
-        if constexpr (std::is_same_v<V, float>)
-            return diag_launch_u<V, E, LPR, 1, V, true>(a, s);
-        else
+    if (a.compensated) {  // FP32 real vectors only
+        if constexpr (std::is_same_v<V, float>) {
+            if (a.compensated == 2) return diag_launch_u<V, E, LPR, 1, V, 2>(a, s);  // one row per thread
+            if (a.prefetch) return diag_launch_pf<V, E, LPR, V, 1>(a, s);
+            if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2, V, 1>(a, s);
+            return diag_launch_u<V, E, LPR, 1, V, 1>(a, s);
+        } else {
             return cudaErrorInvalidValue;
+        }
     }
     if (a.prefetch) return diag_launch_pf<V, E, LPR>(a, s);
     if (a.unroll == 2) return diag_launch_u<V, E, LPR, 2>(a, s);

@@ -70,7 +70,8 @@ kpm_config make_config(py::dict kw) {
             else if (p == "fp64") c.precision = KPM_PREC_FP64;
             else if (p == "fp32") c.precision = KPM_PREC_FP32;
             else if (p == "fp32x") c.precision = KPM_PREC_FP32X;
-            else throw py::value_error("precision must be 'auto', 'fp64', 'fp32' or 'fp32x'");
+            else if (p == "fp32p") c.precision = KPM_PREC_FP32P;
+            else throw py::value_error("precision must be 'auto', 'fp64', 'fp32', 'fp32p' or 'fp32x'");
         } else if (key == "batch_width") {
             c.batch_width = v.cast<int32_t>();
         } else if (key == "tile_rows") {

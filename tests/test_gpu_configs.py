@@ -28,11 +28,12 @@ def _rademacher(n, count, seed):
     return np.where(rng.integers(0, 2, size=(count, n)) == 0, -1.0, 1.0).astype(np.float32)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp32", 1e-6), ("fp32x", 2e-7)])
+@pytest.mark.parametrize("precision,tol", [("fp32", 2e-6), ("fp32p", 1e-6), ("fp32x", 2e-7)])
 def test_fp32_moments_of_a_full_size_flake(oracle, precision, tol):
     """One flake of the batched DOS workload at its largest size (400k sites, onsite disorder
     U[-0.5, 0.5] eV, float32 H), 64 Rademacher vectors, 4098 moments, Lanczos bounds: the FP32
-    recursion (plain FMA row sums, or compensated row sums rounded once) against the FP64
+    recursion (row sums of chained FMAs, of exactly split products, or compensated and rounded
+    once) against the FP64
     recursion of the same engine settings (bit-identical bounds) on every vector, and both
     against the FP64 oracle on two vectors with the engine's own (a, b)."""
     m = L.graphene_flake(400_000, onsite_modifiers=[L.anderson_disorder(1.0, 11)])
@@ -227,6 +228,29 @@ def test_spatial_ldos_of_a_3d_anderson_cube_matches_oracle(oracle, dtype, tol):
     err = rel_err(got, ref)
     print("3D Anderson LDOS %s (64 sites): %.3e" % (np.dtype(dtype).name, err))
     assert err <= tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32p", 1e-6), ("fp32", 2e-6)])
+def test_exact_product_rows_match_the_oracle_on_a_ragged_batch(oracle, precision, tol):
+    """precision fp32p: FP32 vectors whose row sums of H~ x add exactly split products (FMA),
+    on a ragged batch of three flakes (row offsets not multiples of 16), 1026 moments, against
+    the FP64 oracle; beside it the chained-FMA rows on the same inputs."""
+    hs = [_flake(n, s) for n, s in ((9001, 21), (4003, 22), (12007, 23))]
+    rng = (-9.5, 9.5)
+    M = 1026
+    a, b = oracle.scale(*rng)
+    starters = [oracle.random_starters(x.shape[0], 64, np.float32) for x in hs]
+    flat = np.concatenate([st.ravel() for st in starters])
+    batch = kpm_batch([L.Model(x.astype(np.float32), None) for x in hs], energy_range=rng, precision=precision)
+    got = batch.engine.moments_diag(M, flat)
+    batch.close()
+    for s, x in enumerate(hs):
+        r = oracle.optimize(x, [0], [0], a, b)
+        ref = oracle.moments_diag(r["h2"], oracle.reorder_vector(starters[s].astype(np.float64), r["reorder_map"]), M,
+                                  slices=r["slices"])
+        err = rel_err(got[s], ref)
+        print("%s system %d: %.3e" % (precision, s, err))
+        assert err <= tol
 
 
 @pytest.mark.parametrize("nvec", [64, 16, 1])
