@@ -3,8 +3,8 @@
 Workload (default): 32 Anderson-disordered graphene flakes of uneven size
 (sites drawn uniformly in [50k, 400k], onsite energies uniform in
 [-0.5, 0.5] eV), 64 Rademacher starters per flake, 4096 moments (rounded to
-4098 as the reference does), FP32 recursion vectors (row sums of exactly split
-products) with FP64 moment sums,
+4098 as the reference does), FP32 recursion vectors (row sums compensated by an
+FMA per term) with FP64 moment sums,
 spectral bounds by FP64 Lanczos. All flakes and vectors advance together:
 every Chebyshev step is one kernel launch over the block-diagonal matrix.
 
@@ -80,8 +80,8 @@ def parse():
     p.add_argument("--staging", default="auto", choices=["auto", "registers", "prefetch"],
                    help="diagonal step's matrix entries: per-row loads or staged a chunk ahead (auto = by timing)")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "fp32p", "fp32x"],
-                   help="FP32 recursion row sums: chained FMAs (fp32), exactly split products (fp32p = auto) "
-                        "or compensated (fp32x)")
+                   help="FP32 recursion row sums: chained FMAs (fp32), compensated by an FMA per term "
+                        "(fp32p = auto) or by TwoSum (fp32x)")
     p.add_argument("--fuse", type=int, default=0, choices=[0, 1, 2],
                    help="steps per launch (0 = chosen by timing)")
     p.add_argument("--adj-moments", type=int, default=1024, help="moments of the adjoint workload")
@@ -273,8 +273,8 @@ def workload_config(args, hs):
             "nnz": int(sum(h.nnz for h in hs)), "vectors_per_flake": args.vectors,
             "moments": int(args.moments + ((4 - (args.moments - 2) % 4) % 4)),
             "recursion": "fp32 vectors, %s, fp64 moment sums" % (
-                {"fp32x": "compensated fp32 row sums", "fp32": "fp32 row sums of chained FMAs"}.get(
-                    getattr(args, "precision", "auto"), "fp32 row sums of exactly split products (auto)")),
+                {"fp32x": "fp32 row sums compensated by TwoSum", "fp32": "fp32 row sums of chained FMAs"}.get(
+                    getattr(args, "precision", "auto"), "fp32 row sums compensated by an FMA per term (auto)")),
             "bounds": "fp64 Lanczos per flake",
             "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if args.gpus > 1 else "single"}
 
@@ -740,7 +740,7 @@ def workload_anderson3d(args, stream_of):
     h = L.simple_cubic_periodic(Lc, onsite=rng.uniform(-8.25, 8.25, Lc ** 3).astype(np.float32)).hamiltonian
     n = h.shape[0]
     R = args.cube_vectors
-    eng = _native.Engine(h, _native.make_config(staging=args.staging, fuse_steps=args.fuse))
+    eng = _native.Engine(h, _native.make_config(staging=args.staging, fuse_steps=args.fuse, precision=args.precision))
     eng.scaling_factors()
     st = (rng.integers(0, 2, (R, n), dtype=np.int8) * 2 - 1).astype(np.float32)
     import torch
@@ -793,6 +793,8 @@ def workload_anderson3d(args, stream_of):
           "Gnnz*vec/s", True, t / args.steps,
           {"workload": "3D Anderson: simple cubic %d^3 periodic, W = 16.5, %d vectors, %d moments" % (Lc, R, M),
            "sites": int(n), "nnz": int(h.nnz), "moments": int(M), "vectors": R,
+           "recursion": {"fp32x": "fp32 row sums compensated by TwoSum", "fp32": "fp32 row sums of chained FMAs"}.get(
+               args.precision, "fp32 row sums compensated by an FMA per term (auto)"),
            "l2": "inputs larger than L2 (no flush)"},
           "f32",
           roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",

@@ -49,8 +49,8 @@ extern "C" {
                              H~ x as chained FMAs */
 #define KPM_PREC_FP32X 3  /* as KPM_PREC_FP32, and for real H each row sum of H~ x compensated
                              (error-free products and sums) and rounded once */
-#define KPM_PREC_FP32P 4  /* as KPM_PREC_FP32, and for real H the products of each row sum of H~ x
-                             exact (FMA split), the rounded products summed in FP32 */
+#define KPM_PREC_FP32P 4  /* as KPM_PREC_FP32, and for real H each row sum of H~ x compensated by
+                             one FMA per term (Fast2Sum of the running sum and the rounded product) */
 
 /* matrix formats accepted for API compatibility (kpm/Config.hpp:7) */
 #define KPM_FORMAT_CSR 0

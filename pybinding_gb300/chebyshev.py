@@ -391,8 +391,8 @@ def kpm(model, energy_range=None, kernel="default", num_threads="auto", silent=F
 
     Extra keyword arguments of ``_cpp.kpm`` are accepted: ``matrix_format``,
     ``optimal_size``, ``interleaved``, ``lanczos_precision``; plus the GPU knobs
-    ``precision`` ("auto"; "fp64"; FP32 vectors with row sums of chained FMAs "fp32", of exactly
-    split products "fp32p" -- the automatic choice for a float32 H -- or compensated "fp32x"),
+    ``precision`` ("auto"; "fp64"; FP32 vectors with row sums of chained FMAs "fp32", compensated
+    by one FMA per term "fp32p" -- the automatic choice for a float32 H -- or by TwoSum "fp32x"),
     ``batch_width`` and ``moments_gemm``
     ("fp64": the conductivity's moments matrix on the FP64 CUDA cores; "tensor": on
     the tensor cores from FP32 planes, three-product TF32 split). ``num_threads`` is the

@@ -45,9 +45,9 @@ struct DiagStep {
     int prefetch = 0;         // > 0: ELL entries copied to shared memory a chunk ahead (diag_pf_kernel),
                               // register allocation for 3 or 4 resident blocks per SM (3 or 4);
                               // chosen by the autotuner; unroll is then 1
-    int compensated = 0;      // FP32 real vectors, row sums of H~ x: 0 chained FMAs, 1 exact products
-                              // (FMA split, rounded products summed), 2 compensated (exact products
-                              // and TwoSum, rounded once; one row per thread)
+    int compensated = 0;      // FP32 real vectors, row sums of H~ x: 0 chained FMAs, 1 compensated by
+                              // one FMA per term (Fast2Sum), 2 compensated by exact products and
+                              // TwoSum (rounded once; one row per thread)
     bool real_matrix = false; // complex vectors with real H~ values: val holds [rows][W][vs] of the
                               // real type (vs of that type: hi/lo pairs for FP32)
 };

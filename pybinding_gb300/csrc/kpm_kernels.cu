@@ -183,34 +183,39 @@ __device__ __forceinline__ void two_sum_term(float& sum, float& lo, float h, flo
     lo = fmaf(hl, x, __fadd_rn(lo, __fadd_rn(err, pe)));
 }
 
-// Row sum of H~ x with exact products (CR = 1): each product h x is split exactly into
-// fl(h x) + e by an FMA; the rounded products are summed in FP32 and the parts e, with the
-// low halves of the matrix values, in a second FP32 word. The rounding of the products --
-// large against a row sum that cancels, as the rows of high Chebyshev vectors do -- is then
-// gone; what remains is the rounding of the running sum. Measured (NumPy emulation of these
-// operations, 395k-site flake, 4098 moments): 3.8e-7 of max |mu| per vector against 1.4e-6
-// with chained FMAs and 4.5e-8 with the row sum rounded once.
-__device__ __forceinline__ void exact_product_term(float& sum, float& lo, float h, float hl, float x) {
+// Row sum of H~ x compensated by one FMA per term (CR = 1): s1 = fl(s + fl(h x)); when |s| >=
+// |fl(h x)| the difference s - s1 is exact (Fast2Sum), and one FMA gives h x + (s - s1) -- the
+// product's rounding plus the sum's -- rounded once; it gathers, with the low halves of the
+// matrix values, in a second FP32 word. The rounding inside a row sum that cancels, as the rows
+// of high Chebyshev vectors do, is large against the result; this removes it. Measured (NumPy
+// emulation of these operations, 395k-site flake, 4098 moments): 3.8e-8 of max |mu| per vector,
+// the same as with TwoSum (two_sum_term), against 1.4e-6 with chained FMAs and 3.8e-7 with
+// exact products but plain sums; 6 FP32 operations per term against 11 for TwoSum.
+__device__ __forceinline__ void fma_compensated_term(float& sum, float& lo, float h, float hl, float x) {
     float const p = __fmul_rn(h, x);
-    float const pe = fmaf(h, x, -p);  // h x - fl(h x), exact
-    sum = __fadd_rn(sum, p);
-    lo = fmaf(hl, x, __fadd_rn(lo, pe));
+    float const s1 = __fadd_rn(sum, p);
+    float const c = fmaf(h, x, __fsub_rn(sum, s1));  // (h x - p) + (sum + p - s1), rounded once
+    sum = s1;
+    lo = fmaf(hl, x, __fadd_rn(lo, c));
 }
 
-// The FP32 row arithmetic two vectors at a time: sm_100 and later issue FP32 add, multiply and
-// FMA on pairs (__fadd2_rn, __fmul2_rn, __ffma2_rn), one instruction for two of a lane's E
-// vectors. Each element rounds as its scalar operation does, so the results are the same bits.
-// CR: 0 chained FMAs, 1 exact products (exact_product_term), 2 compensated (two_sum_term).
+// The FP32 row arithmetic of the compensated row sums two vectors at a time: sm_100 and later
+// issue FP32 add, multiply and FMA on pairs (__fadd2_rn, __fmul2_rn, __ffma2_rn), one
+// instruction for two of a lane's E vectors. Each element rounds as its scalar operation does,
+// so the results are the same bits. Chained FMAs (CR = 0) stay scalar: paired, they measured
+// slower (506 against 430 us per step on a 128^3 cube, 64 vectors), and the 3-4 instructions
+// they issue per entry and vector do not limit the step.
+// CR: 0 chained FMAs, 1 FMA-compensated (fma_compensated_term), 2 TwoSum (two_sum_term).
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
 template<int E, int CR>
 __device__ __forceinline__ void row_terms_f32(float (&sum)[E], float (&lo)[E], float h, float hl,
                                               Pack<float, E> const& x) {
-    if constexpr (E % 2 != 0) {
+    if constexpr (E % 2 != 0 || CR == 0) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             if constexpr (CR == 2) two_sum_term(sum[e], lo[e], h, hl, x.v[e]);
-            else if constexpr (CR == 1) exact_product_term(sum[e], lo[e], h, hl, x.v[e]);
+            else if constexpr (CR == 1) fma_compensated_term(sum[e], lo[e], h, hl, x.v[e]);
             else { sum[e] = fmaf(h, x.v[e], sum[e]); lo[e] = fmaf(hl, x.v[e], lo[e]); }
         }
     } else {
@@ -221,22 +226,20 @@ __device__ __forceinline__ void row_terms_f32(float (&sum)[E], float (&lo)[E], f
             float2 const xv = make_float2(x.v[k], x.v[k + 1]);
             float2 s = make_float2(sum[k], sum[k + 1]);
             float2 l = make_float2(lo[k], lo[k + 1]);
-            if constexpr (CR == 0) {
-                s = __ffma2_rn(h2, xv, s);
-                l = __ffma2_rn(hl2, xv, l);
-            } else {
+            if constexpr (CR == 1) {
+                float2 const p = __fmul2_rn(h2, xv);
+                float2 const s1 = __fadd2_rn(s, p);
+                float2 const c = __ffma2_rn(h2, xv, __fadd2_rn(s, neg2(s1)));
+                s = s1;
+                l = __ffma2_rn(hl2, xv, __fadd2_rn(l, c));
+            } else {  // exact product (FMA split) and Knuth's TwoSum of s + p
                 float2 const p = __fmul2_rn(h2, xv);
                 float2 const pe = __ffma2_rn(h2, xv, neg2(p));  // h x - fl(h x), exact
-                if constexpr (CR == 1) {
-                    s = __fadd2_rn(s, p);
-                    l = __ffma2_rn(hl2, xv, __fadd2_rn(l, pe));
-                } else {  // Knuth's TwoSum of s + p
-                    float2 const s1 = __fadd2_rn(s, p);
-                    float2 const bb = __fadd2_rn(s1, neg2(s));
-                    float2 const err = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(s1, neg2(bb)))), __fadd2_rn(p, neg2(bb)));
-                    s = s1;
-                    l = __ffma2_rn(hl2, xv, __fadd2_rn(l, __fadd2_rn(err, pe)));
-                }
+                float2 const s1 = __fadd2_rn(s, p);
+                float2 const bb = __fadd2_rn(s1, neg2(s));
+                float2 const err = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(s1, neg2(bb)))), __fadd2_rn(p, neg2(bb)));
+                s = s1;
+                l = __ffma2_rn(hl2, xv, __fadd2_rn(l, __fadd2_rn(err, pe)));
             }
             sum[k] = s.x;
             sum[k + 1] = s.y;
@@ -247,12 +250,12 @@ __device__ __forceinline__ void row_terms_f32(float (&sum)[E], float (&lo)[E], f
 }
 
 // y_new = (sum + lo) - y_old (or (sum + lo) / 2 for the first step), and the moment sums
-// m2 += x_r^2, m3 += y_new x_r, two vectors at a time
-template<int E, bool INIT>
+// m2 += x_r^2, m3 += y_new x_r, two vectors at a time (PAIR) or one
+template<int E, bool INIT, bool PAIR>
 __device__ __forceinline__ void row_finish_f32(float const (&sum)[E], float const (&lo)[E], Pack<float, E> const& yo,
                                                Pack<float, E> const& xr, Pack<float, E>& yn, float (&m2)[E],
                                                float (&m3)[E]) {
-    if constexpr (E % 2 != 0) {
+    if constexpr (E % 2 != 0 || !PAIR) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             float const sv = sum[e] + lo[e];
@@ -325,10 +328,10 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
                 if (!(live[u] && j0 + q < W)) continue;
                 MV const* vp = val + (static_cast<int64_t>(rr[u]) * W + j0 + q) * VS;
                 MV const a = vp[0];
-                if constexpr (std::is_same_v<V, float> && std::is_same_v<MV, float>) {  // (hi, lo) values
+                if constexpr (CR != 0) {
+                    static_assert(std::is_same_v<V, float> && std::is_same_v<MV, float>, "compensated rows are FP32");
                     row_terms_f32<E, CR>(sum[u], lo[u], a, vp[1], xv[u][q]);
                 } else {
-                    static_assert(CR == 0, "compensated rows are FP32");
 #pragma unroll
                     for (int e = 0; e < E; ++e) vfma(sum[u][e], a, xv[u][q].v[e]);
                     if (VS == 2) {
@@ -343,14 +346,16 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
     for (int u = 0; u < U; ++u) {
         if (!live[u]) continue;
         P yn;
-        if constexpr (std::is_same_v<V, float>) {
-            row_finish_f32<E, INIT>(sum[u], lo[u], yo[u], xr[u], yn, m2, m3r);
+        if constexpr (CR != 0) {
+            row_finish_f32<E, INIT, true>(sum[u], lo[u], yo[u], xr[u], yn, m2, m3r);
+            st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(rr[u]) * K) + lane, yn);
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 V const s = (VS == 2) ? vadd(sum[u][e], lo[u][e]) : sum[u][e];
                 yn.v[e] = INIT ? vhalf(s) : vsub(s, yo[u].v[e]);
             }
+            st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(rr[u]) * K) + lane, yn);
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 m2[e] += vsq(xr[u].v[e]);
@@ -358,7 +363,6 @@ __device__ __forceinline__ void diag_rows(int32_t const* __restrict__ col, MV co
                 if (CPLX) m3i[e] += vdim(yn.v[e], xr[u].v[e]);
             }
         }
-        st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(rr[u]) * K) + lane, yn);
     }
 }
 
@@ -409,13 +413,11 @@ __device__ __forceinline__ void diag_flush(typename Tr<V>::R (&m2)[E], typename 
     for (int e = 0; e < E; ++e) { m2[e] = R(0); m3r[e] = R(0); m3i[e] = R(0); }
 }
 
-// kernels with exact-product or compensated rows are held to 4 resident blocks per SM (64 registers)
-template<class V, int E, int LPR, bool INIT, int U, class MV = V, int CR = 0>
-__global__ void __launch_bounds__(BLOCK, CR != 0 ? 4 : 1)
-diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
-                 V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
-                 Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
-                 double* __restrict__ acc) {
+template<class V, int E, int LPR, bool INIT, int U, class MV, int CR>
+__device__ __forceinline__ void diag_step_body(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
+                                               V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+                                               Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit,
+                                               int nbatch, double* __restrict__ acc) {
     using R = typename Tr<V>::R;
     constexpr bool CPLX = Tr<V>::C;
     constexpr int K = E * LPR;
@@ -457,6 +459,29 @@ diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, in
     }
     if (cur_sys >= 0)
         diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
+}
+
+// Chained FMAs: no register bound (the compiler's own allocation, 64 registers for one row per
+// thread). Compensated row sums are held to 4 resident blocks per SM (64 registers; left free,
+// the compiler takes 88 and 2 blocks fit).
+template<class V, int E, int LPR, bool INIT, int U, class MV = V>
+__global__ void __launch_bounds__(BLOCK)
+diag_step_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
+                 V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+                 Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
+                 double* __restrict__ acc) {
+    diag_step_body<V, E, LPR, INIT, U, MV, 0>(col, val, W, x_all, y_all, batch_stride, tiles, num_tiles, row_limit,
+                                              nbatch, acc);
+}
+
+template<class V, int E, int LPR, bool INIT, int U, class MV, int CR>
+__global__ void __launch_bounds__(BLOCK, 4)
+diag_step_cr_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int W,
+                    V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
+                    Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
+                    double* __restrict__ acc) {
+    diag_step_body<V, E, LPR, INIT, U, MV, CR>(col, val, W, x_all, y_all, batch_stride, tiles, num_tiles, row_limit,
+                                               nbatch, acc);
 }
 
 // ------------------------------------------------------------------ diagonal step, prefetched entries
@@ -602,7 +627,7 @@ diag_pf_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int 
                     for (int q = 0; q < 4; ++q) {
                         if (j0 + q >= W) continue;
                         MV const a = vrow[(j0 + q) * VS];
-                        if constexpr (std::is_same_v<V, float> && std::is_same_v<MV, float>) {
+                        if constexpr (RS != 0) {
                             row_terms_f32<E, RS>(sum, lo, a, vrow[(j0 + q) * VS + 1], xv[q]);
                         } else {
 #pragma unroll
@@ -616,14 +641,16 @@ diag_pf_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int 
                     }
                 }
                 P yn;
-                if constexpr (std::is_same_v<V, float>) {
-                    row_finish_f32<E, INIT>(sum, lo, yo, xr, yn, m2, m3r);
+                if constexpr (RS != 0) {
+                    row_finish_f32<E, INIT, true>(sum, lo, yo, xr, yn, m2, m3r);
+                    st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
                 } else {
 #pragma unroll
                     for (int e = 0; e < E; ++e) {
                         V const sv = (VS == 2) ? vadd(sum[e], lo[e]) : sum[e];
                         yn.v[e] = INIT ? vhalf(sv) : vsub(sv, yo.v[e]);
                     }
+                    st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
 #pragma unroll
                     for (int e = 0; e < E; ++e) {
                         m2[e] += vsq(xr.v[e]);
@@ -631,7 +658,6 @@ diag_pf_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val, int 
                         if (CPLX) m3i[e] += vdim(yn.v[e], xr.v[e]);
                     }
                 }
-                st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(r) * K) + lane, yn);
             }
             __syncwarp();  // the buffer is refilled two chunks later
             pti = nti;
@@ -1227,18 +1253,19 @@ cudaError_t diag_launch_u(DiagStep const& a, cudaStream_t s) {
     auto const* val = static_cast<MV const*>(a.val);
     auto const* x = static_cast<V const*>(a.x);
     auto* y = static_cast<V*>(a.y);
-    if (a.init) {
-        auto fn = diag_step_kernel<V, E, LPR, true, U, MV, CR>;
+    auto run = [&](auto fn) {
         int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
         fn<<<g, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit, a.nbatch,
                                a.acc);
+        return cudaGetLastError();
+    };
+    if constexpr (CR == 0) {
+        if (a.init) return run(diag_step_kernel<V, E, LPR, true, U, MV>);
+        return run(diag_step_kernel<V, E, LPR, false, U, MV>);
     } else {
-        auto fn = diag_step_kernel<V, E, LPR, false, U, MV, CR>;
-        int const g = persistent_grid(reinterpret_cast<void const*>(fn), a.num_tiles);
-        fn<<<g, BLOCK, 0, s>>>(a.col, val, a.W, x, y, a.batch_stride, a.tiles, a.num_tiles, a.row_limit, a.nbatch,
-                               a.acc);
+        if (a.init) return run(diag_step_cr_kernel<V, E, LPR, true, U, MV, CR>);
+        return run(diag_step_cr_kernel<V, E, LPR, false, U, MV, CR>);
     }
-    return cudaGetLastError();
 }
 
 
