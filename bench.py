@@ -43,7 +43,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "KPM Gnnz*vec/s (batched FP32 recursion, FP64 moment sums; moment err vs FP64 stated)"
+METRIC = "KPM Gnnz\u00b7vec/s & HBM GB/s: batched FP32 vs plain FP64 at moment err \u22641e-6"
 UNIT = "Gnnz*vec/s"
 
 
@@ -265,6 +265,20 @@ def oracle_check(h, a, b, starters, M, got64, got32):
             "fp32_vs_oracle": float(np.max(np.abs(got32 - ref)) / scale)}
 
 
+def step_kernel(stats, precision, elem="float"):
+    """Name of the recursion kernel the engine ran last (its stats) for an FP32 precision mode."""
+    comp = precision in ("auto", "fp32p", "fp32x") and elem == "float"
+    if int(stats.steps_per_launch) == 2:
+        name = "diag_pair_kernel"
+    elif int(stats.prefetch):
+        name = "diag_pf_kernel"
+    else:
+        name = "diag_step_cr_kernel" if comp else "diag_step_kernel"
+    rows = {"fp32x": "TwoSum-compensated rows", "fp32": "chained-FMA rows"}.get(
+        precision, "FMA-compensated rows") if elem == "float" else "FP64"
+    return "%s<%s,%d,%d> (%s)" % (name, elem, int(stats.elems_per_lane), int(stats.lanes_per_row), rows)
+
+
 def workload_config(args, hs):
     return {"workload": "batched stochastic DOS moments: %d disordered graphene flakes U[%d,%d] sites, "
                         "%d Rademacher vectors each, %d moments" % (args.flakes, args.min_sites, args.max_sites,
@@ -344,6 +358,7 @@ def run_gpu(args, rank, world, local_rank):
     rec = float(np.median(rec_times))
     fuse = int(eng.stats().steps_per_launch)
     lane_map = (int(eng.stats().elems_per_lane), int(eng.stats().lanes_per_row))
+    kernel_name = step_kernel(eng.stats(), args.precision)
     tiling = {"tile_rows": int(eng.stats().tile_rows), "unroll": int(eng.stats().unroll),
               "prefetch": int(eng.stats().prefetch)}
     launches = 1 + (M // 2 - 1) // fuse  # init + recursion launches
@@ -417,9 +432,7 @@ def run_gpu(args, rank, world, local_rank):
         alg_v = nnz * (8 + 4) + 4 * (nrows + 1) + (3 if fz == 1 else 4) * nrows * R * elem_bytes
         avg_v = float(np.median(recs)) / nl
         out = {"value": work / tv / 1e9, "unit": UNIT, "ms_per_step": tv * 1e3, "timed_steps": nv,
-               "kernel": "%s<%s,%d,%d>" % ("diag_step_kernel" if fz == 1 else "diag_pair_kernel",
-                                           "double" if elem_bytes == 8 else "float", int(sv_st.elems_per_lane),
-                                           int(sv_st.lanes_per_row)),
+               "kernel": step_kernel(sv_st, prec, "double" if elem_bytes == 8 else "float"),
                "roofline": {"bound": "hbm", "achieved": alg_v / avg_v / 1e9, "peak": peak, "unit": "GB/s",
                             "frac": alg_v / avg_v / 1e9 / peak, "alg_bytes_per_launch": alg_v,
                             "avg_launch_ms": avg_v * 1e3}}
@@ -475,9 +488,7 @@ def run_gpu(args, rank, world, local_rank):
                "moment_error_vs_fp64": err,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
-                            "kernel": "%s<float,%d,%d>" % (("diag_pf_kernel" if tiling["prefetch"] else
-                                                            "diag_step_kernel") if fuse == 1 else "diag_pair_kernel",
-                                                           lane_map[0], lane_map[1]),
+                            "kernel": kernel_name,
                             "steps_per_launch": fuse, "tiling": tiling, "alg_bytes_per_launch": alg_bytes,
                             "avg_launch_ms": avg_launch * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
                "cpu_baseline": cpu,
@@ -799,8 +810,7 @@ def workload_anderson3d(args, stream_of):
           "f32",
           roofline={"bound": "hbm", "achieved": alg / avg / 1e9, "peak": peak, "unit": "GB/s",
                     "frac": alg / avg / 1e9 / peak, "traffic": None, "steps_per_launch": fuse,
-                    "kernel": ("diag_pf_kernel" if s.prefetch else "diag_step_kernel") if fuse == 1
-                              else "diag_pair_kernel",
+                    "kernel": step_kernel(s, args.precision),
                     "lane_map": [int(s.elems_per_lane), int(s.lanes_per_row)], "tile_rows": int(s.tile_rows),
                     "unroll": int(s.unroll),
                     "alg_bytes_per_launch": alg, "avg_launch_ms": avg * 1e3,

@@ -461,6 +461,134 @@ __device__ __forceinline__ void diag_step_body(int32_t const* __restrict__ col, 
         diag_flush<V, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(cur_sys * nbatch + cur_batch) * K * NV);
 }
 
+// The FMA-compensated FP32 rows (CR = 1) with every per-vector value held as pairs of vectors
+// (float2) from load to store: the paired instructions then need no moves to form their operands,
+// and a subtraction is a paired FMA by -1 (same rounding as the scalar subtraction). The same
+// bits as fma_compensated_term and the scalar finish.
+template<int E, int LPR, bool INIT, int U>
+__device__ __forceinline__ void diag_rows_f2(int32_t const* __restrict__ col, float const* __restrict__ val, int W,
+                                             float const* __restrict__ x, float* __restrict__ y, int const (&rr)[U],
+                                             bool const (&live)[U], int lane, float2 (&m2)[E / 2],
+                                             float2 (&m3)[E / 2]) {
+    constexpr int K = E * LPR;
+    constexpr int H = E / 2;
+    using P = Pack<float2, H>;
+    float2 const m1 = make_float2(-1.f, -1.f);
+    P xr[U], yo[U];
+    float2 sum[U][H], lo[U][H];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (!live[u]) continue;
+        xr[u] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(rr[u]) * K) + lane);
+        if (!INIT) yo[u] = ld_stream(reinterpret_cast<P const*>(y + static_cast<int64_t>(rr[u]) * K) + lane);
+#pragma unroll
+        for (int k = 0; k < H; ++k) { sum[u][k] = make_float2(0.f, 0.f); lo[u][k] = make_float2(0.f, 0.f); }
+    }
+    for (int j0 = 0; j0 < W; j0 += 4) {
+        int32_t c[U][4];
+        P xv[U][4];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                c[u][q] = (live[u] && j0 + q < W) ? __ldg(col + static_cast<int64_t>(rr[u]) * W + j0 + q) : 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (live[u] && j0 + q < W)
+                    xv[u][q] = ld_ro(reinterpret_cast<P const*>(x + static_cast<int64_t>(c[u][q]) * K) + lane);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (!(live[u] && j0 + q < W)) continue;
+                float const* vp = val + (static_cast<int64_t>(rr[u]) * W + j0 + q) * 2;
+                float2 const h2 = make_float2(vp[0], vp[0]);
+                float2 const hl2 = make_float2(vp[1], vp[1]);
+#pragma unroll
+                for (int k = 0; k < H; ++k) {
+                    float2 const xk = xv[u][q].v[k];
+                    float2 const p = __fmul2_rn(h2, xk);
+                    float2 const s1 = __fadd2_rn(sum[u][k], p);
+                    float2 const cc = __ffma2_rn(h2, xk, __ffma2_rn(s1, m1, sum[u][k]));
+                    sum[u][k] = s1;
+                    lo[u][k] = __ffma2_rn(hl2, xk, __fadd2_rn(lo[u][k], cc));
+                }
+            }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (!live[u]) continue;
+        P yn;
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+            float2 const sv = __fadd2_rn(sum[u][k], lo[u][k]);
+            yn.v[k] = INIT ? __fmul2_rn(sv, make_float2(0.5f, 0.5f)) : __ffma2_rn(yo[u].v[k], m1, sv);
+        }
+        st_stream(reinterpret_cast<P*>(y + static_cast<int64_t>(rr[u]) * K) + lane, yn);
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+            m2[k] = __ffma2_rn(xr[u].v[k], xr[u].v[k], m2[k]);
+            m3[k] = __ffma2_rn(yn.v[k], xr[u].v[k], m3[k]);
+        }
+    }
+}
+
+template<int E, int LPR, bool INIT, int U>
+__device__ __forceinline__ void diag_step_body_f2(int32_t const* __restrict__ col, float const* __restrict__ val,
+                                                  int W, float const* __restrict__ x_all, float* __restrict__ y_all,
+                                                  int64_t batch_stride, Tile const* __restrict__ tiles, int num_tiles,
+                                                  int32_t row_limit, int nbatch, double* __restrict__ acc) {
+    constexpr int K = E * LPR;
+    constexpr int H = E / 2;
+    constexpr int RPP = BLOCK / LPR;
+    __shared__ double red[WARPS * K * 2];
+    int const lane = threadIdx.x % LPR;
+    int const slot = threadIdx.x / LPR;
+    int const G = gridDim.x;
+    float2 m2p[H], m3p[H];
+#pragma unroll
+    for (int k = 0; k < H; ++k) { m2p[k] = make_float2(0.f, 0.f); m3p[k] = make_float2(0.f, 0.f); }
+    auto flush = [&](int sys, int b) {
+        float m2[E], m3r[E], m3i[E];
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+            m2[2 * k] = m2p[k].x;
+            m2[2 * k + 1] = m2p[k].y;
+            m3r[2 * k] = m3p[k].x;
+            m3r[2 * k + 1] = m3p[k].y;
+            m3i[2 * k] = m3i[2 * k + 1] = 0.f;
+            m2p[k] = make_float2(0.f, 0.f);
+            m3p[k] = make_float2(0.f, 0.f);
+        }
+        diag_flush<float, E, LPR>(m2, m3r, m3i, red, acc + static_cast<int64_t>(sys * nbatch + b) * K * 2);
+    };
+    int cur_sys = -1, cur_batch = -1;
+    for (int ti = blockIdx.x; ti < num_tiles; ti += G) {
+        Tile const t = tiles[ti];
+        if (t.system != cur_sys || t.batch != cur_batch) {
+            if (cur_sys >= 0) flush(cur_sys, cur_batch);
+            cur_sys = t.system;
+            cur_batch = t.batch;
+        }
+        float const* __restrict__ x = x_all + t.batch * batch_stride;
+        float* __restrict__ y = y_all + t.batch * batch_stride;
+        int const row_end = min(t.row_end, row_limit);
+        for (int r = t.row_begin + slot; r < row_end; r += RPP * U) {
+            int rr[U];
+            bool live[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                rr[u] = r + u * RPP;
+                live[u] = rr[u] < row_end;
+            }
+            diag_rows_f2<E, LPR, INIT, U>(col, val, W, x, y, rr, live, lane, m2p, m3p);
+        }
+    }
+    if (cur_sys >= 0) flush(cur_sys, cur_batch);
+}
+
 // Chained FMAs: no register bound (the compiler's own allocation, 64 registers for one row per
 // thread). Compensated row sums are held to 4 resident blocks per SM (64 registers; left free,
 // the compiler takes 88 and 2 blocks fit).
@@ -480,8 +608,12 @@ diag_step_cr_kernel(int32_t const* __restrict__ col, MV const* __restrict__ val,
                     V const* __restrict__ x_all, V* __restrict__ y_all, int64_t batch_stride,
                     Tile const* __restrict__ tiles, int num_tiles, int32_t row_limit, int nbatch,
                     double* __restrict__ acc) {
-    diag_step_body<V, E, LPR, INIT, U, MV, CR>(col, val, W, x_all, y_all, batch_stride, tiles, num_tiles, row_limit,
-                                               nbatch, acc);
+    if constexpr (CR == 1 && std::is_same_v<V, float> && std::is_same_v<MV, float> && E % 2 == 0)
+        diag_step_body_f2<E, LPR, INIT, U>(col, val, W, x_all, y_all, batch_stride, tiles, num_tiles, row_limit, nbatch,
+                                           acc);
+    else
+        diag_step_body<V, E, LPR, INIT, U, MV, CR>(col, val, W, x_all, y_all, batch_stride, tiles, num_tiles,
+                                                   row_limit, nbatch, acc);
 }
 
 // ------------------------------------------------------------------ diagonal step, prefetched entries
