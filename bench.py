@@ -244,6 +244,8 @@ def run_reference(args, rank, world):
     v = float(np.median(vals))
     cfg = workload_config(args, hs)
     cfg["sample_moments"] = int(last[1])
+    cfg["recursion"] = ("the reference's CPU algorithm in its own arithmetic (the oracle's restatement of "
+                        "kpm::DefaultCompute: float vectors and values, ELL, interleaved steps)")
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": last[0] * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
