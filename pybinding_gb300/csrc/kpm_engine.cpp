@@ -2524,7 +2524,7 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         d_seg.ensure(vec * seg_len);
         d_lam.ensure(vec * 2);
         d_roll.ensure(vec * 2);
-        d_gt.ensure(sizeof(double) * n * W);  // FP64 gradient sums
+        d_gt.ensure(sizeof(double) * n * W);  // gradient sums: FP64, or (hi, lo) FP32 pairs for FP32 vectors
         d_gd.ensure(sizeof(double) * n);
         KPM_CUDA(cudaMemsetAsync(d_gt.p, 0, d_gt.bytes, e->stream));
         KPM_CUDA(cudaMemsetAsync(d_gd.p, 0, d_gd.bytes, e->stream));
@@ -2642,8 +2642,16 @@ int kpm_adjoint_diag(kpm_engine* e, int64_t num_moments, int64_t num_vectors, co
         float ms = 0;
         KPM_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         std::vector<double> gt(static_cast<size_t>(n) * W), gd(static_cast<size_t>(n));
-        std::memcpy(gt.data(), gt_raw.data(), sizeof(double) * gt.size());
-        std::memcpy(gd.data(), gd_raw.data(), sizeof(double) * gd.size());
+        if (vt == kpm::V_F32) {  // (hi, lo) FP32 pairs
+            std::vector<float> pt(2 * gt.size()), pd(2 * gd.size());
+            std::memcpy(pt.data(), gt_raw.data(), sizeof(float) * pt.size());
+            std::memcpy(pd.data(), gd_raw.data(), sizeof(float) * pd.size());
+            for (size_t i = 0; i < gt.size(); ++i) gt[i] = static_cast<double>(pt[2 * i]) + pt[2 * i + 1];
+            for (size_t i = 0; i < gd.size(); ++i) gd[i] = static_cast<double>(pd[2 * i]) + pd[2 * i + 1];
+        } else {
+            std::memcpy(gt.data(), gt_raw.data(), sizeof(double) * gt.size());
+            std::memcpy(gd.data(), gd_raw.data(), sizeof(double) * gd.size());
+        }
         // gt[p][t] holds G[col(p, t)][p]: entry (i, j) of the input is found in row map[j]
         double const f = 2.0 / sc.a;
         for (int64_t i = 0; i < n; ++i)

@@ -113,8 +113,9 @@ struct AdjStep {
     const void* vp;           // nullable
     double a0, am, ap;
     const void* g;            // row vectors of the gradient term (with gt)
-    void* gt;                 // nullable; FP64 gradient sums [rows][W]
-    void* gd;                 // set with gt; FP64 [rows]
+    void* gt;                 // nullable; gradient sums [rows][W]: FP64 for FP64 vectors, (hi, lo) FP32 pairs
+                              // (float2) for FP32 ones
+    void* gd;                 // set with gt; [rows], the same type
     const Tile* tiles;
     int num_tiles;
 };

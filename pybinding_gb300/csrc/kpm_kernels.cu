@@ -1004,17 +1004,30 @@ cudaError_t dense_launch(DenseStep const& a, cudaStream_t s) {
 // (the gradient of the recursion with respect to the transposed entry S[col_j][r]; the
 // pattern of S is symmetric) and gd[r] += sum_k x[r][k] * g[r][k] (the diagonal, also where
 // S stores none). The per-step sum over the K vectors of a row is taken in the vectors'
-// precision; gt and gd accumulate those over the steps in FP64 (one add per entry and step:
-// an FP32 running sum over M/2 steps of terms of both signs lost ~1e-4 of the largest
-// gradient). The row loop is uniform over the block so that the lanes of a row can reduce
-// with warp shuffles.
+// precision; gt and gd accumulate those over the steps in FP64 for FP64 vectors and, for FP32
+// ones, as an unevaluated pair (hi, lo) of FP32 values added to with Knuth's TwoSum (about 48
+// bits, no FP64 instruction; a plain FP32 running sum over M/2 steps of terms of both signs lost
+// ~1e-4 of the largest gradient). The row loop is uniform over the block so that the lanes of a
+// row can reduce with warp shuffles.
+template<class V> struct GradSum { using T = double; };
+template<> struct GradSum<float> { using T = float2; };
+__device__ __forceinline__ double grad_add(double a, double p) { return a + p; }
+__device__ __forceinline__ float2 grad_add(float2 a, float p) {
+    float const s = __fadd_rn(a.x, p);
+    float const bb = __fsub_rn(s, a.x);
+    float const e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    return make_float2(s, __fadd_rn(a.y, e));
+}
+
 template<class V, int E, int LPR>
 __global__ void __launch_bounds__(BLOCK)
 adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int W, V const* __restrict__ x,
                 V const* yprev, V* out, int half, V const* __restrict__ v0, V const* __restrict__ vm,
-                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g, double* __restrict__ gt,
-                double* __restrict__ gd, Tile const* __restrict__ tiles, int num_tiles) {
+                V const* __restrict__ vp, V a0, V am, V ap, V const* __restrict__ g,
+                typename GradSum<V>::T* __restrict__ gt, typename GradSum<V>::T* __restrict__ gd,
+                Tile const* __restrict__ tiles, int num_tiles) {
     static_assert(!Tr<V>::C, "the adjoint step is real");
+    using G = typename GradSum<V>::T;
     constexpr int K = E * LPR;
     constexpr int RPP = BLOCK / LPR;
     constexpr int VS = Tr<V>::VS;
@@ -1034,7 +1047,8 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
             int const rs = live ? r : t.row_begin;  // dead lanes follow a valid row without storing
             int64_t const off = static_cast<int64_t>(rs) * K;
             P gv, yo, q0;
-            double gpre = 0.0, gsum = 0.0;
+            G gpre{};
+            V gsum = V(0);  // one term per lane and step
             if (spread && live) {
                 if (lane < W) gpre = gt[static_cast<int64_t>(r) * W + lane];
                 else if (lane == W) gpre = gd[r];
@@ -1050,9 +1064,9 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 #pragma unroll
                 for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
                 if (spread) {
-                    if (lane == W) gsum += static_cast<double>(p);
+                    if (lane == W) gsum += p;
                 } else if (live && lane == 0) {
-                    gd[r] += static_cast<double>(p);
+                    gd[r] = grad_add(gd[r], p);
                 }
             }
             V sum[E], lo[E];
@@ -1085,16 +1099,16 @@ adj_step_kernel(int32_t const* __restrict__ col, V const* __restrict__ val, int 
 #pragma unroll
                         for (int o = 1; o < LPR; o <<= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
                         if (spread) {
-                            if (lane == j0 + q) gsum += static_cast<double>(p);
+                            if (lane == j0 + q) gsum += p;
                         } else if (live && lane == 0) {
-                            gt[static_cast<int64_t>(r) * W + j0 + q] += static_cast<double>(p);
+                            gt[static_cast<int64_t>(r) * W + j0 + q] = grad_add(gt[static_cast<int64_t>(r) * W + j0 + q], p);
                         }
                     }
                 }
             }
             if (spread && live) {
-                if (lane < W) gt[static_cast<int64_t>(r) * W + lane] = gpre + gsum;
-                else if (lane == W) gd[r] = gpre + gsum;
+                if (lane < W) gt[static_cast<int64_t>(r) * W + lane] = grad_add(gpre, gsum);
+                else if (lane == W) gd[r] = grad_add(gpre, gsum);
             }
             if (live && out != nullptr) {
                 P o;
@@ -1130,8 +1144,8 @@ cudaError_t adj_launch(AdjStep const& a, cudaStream_t s) {
                               static_cast<V const*>(a.yprev), static_cast<V*>(a.out), a.half ? 1 : 0,
                               static_cast<V const*>(a.v0), static_cast<V const*>(a.vm), static_cast<V const*>(a.vp),
                               static_cast<V>(a.a0), static_cast<V>(a.am), static_cast<V>(a.ap),
-                              static_cast<V const*>(a.g), static_cast<double*>(a.gt), static_cast<double*>(a.gd), a.tiles,
-                              a.num_tiles);
+                              static_cast<V const*>(a.g), static_cast<typename GradSum<V>::T*>(a.gt),
+                              static_cast<typename GradSum<V>::T*>(a.gd), a.tiles, a.num_tiles);
     return cudaGetLastError();
 }
 
