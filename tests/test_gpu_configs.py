@@ -230,7 +230,7 @@ def test_spatial_ldos_of_a_3d_anderson_cube_matches_oracle(oracle, dtype, tol):
     assert err <= tol
 
 
-@pytest.mark.parametrize("precision,tol", [("fp32p", 2e-7), ("fp32", 2e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp32p", 4e-7), ("fp32", 2e-6)])
 def test_fma_compensated_rows_match_the_oracle_on_a_ragged_batch(oracle, precision, tol):
     """precision fp32p: FP32 vectors whose row sums of H~ x are compensated by one FMA per term,
     on a ragged batch of three flakes (row offsets not multiples of 16), 1026 moments, against
