@@ -1009,7 +1009,6 @@ struct kpm_engine {
     };
     static SharedCache<Tuned>& tuned() { static SharedCache<Tuned> c; return c; }
     static SharedCache<FuseChoice>& fuse_tuned() { static SharedCache<FuseChoice> c; return c; }
-    std::vector<std::array<double, 3>> last_tuning;  // (rows per tile, unroll, ms) of the last tuning run
 
     static Shape timing_batches(Shape t) {
         t.nbatch = std::min(t.nbatch, 4);
@@ -1034,7 +1033,6 @@ struct kpm_engine {
         {   // small problems (L2-resident, latency bound) want short tiles for parallelism,
             // large ones taller tiles for fewer flushes: timed either way
             double best_ms = 1e30;
-            last_tuning.clear();
             for (auto const& mp : maps)
                 for (int unroll : {1, 2})
                     for (int rpt : {1, 2, 4, 8, 16, 32, 64}) {
@@ -1056,7 +1054,6 @@ struct kpm_engine {
                         KPM_CUDA(cudaEventSynchronize(ev1));
                         float ms = 0;
                         KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                        last_tuning.push_back({static_cast<double>(t.rows_per_tile), static_cast<double>(unroll), ms / 3});
                         if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, unroll, t.E, t.LPR}; }
                     }
             // the step with prefetched ELL entries (diag_pf_kernel): tiles of whole warp chunks
@@ -1085,7 +1082,6 @@ struct kpm_engine {
                     KPM_CUDA(cudaEventSynchronize(ev1));
                     float ms = 0;
                     KPM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                    last_tuning.push_back({static_cast<double>(t.rows_per_tile), static_cast<double>(-pf), ms / 3});
                     if (ms < best_ms) { best_ms = ms; best = Tuned{t.rows_per_tile, 1, sh.E, sh.LPR, pf}; }
                 }
             base.prefetch = 0;
