@@ -47,9 +47,10 @@ METRIC = "KPM Gnnz\u00b7vec/s & HBM GB/s: batched FP32 vs plain FP64 at moment e
 UNIT = "Gnnz*vec/s"
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one diag_step_kernel<float,4,16> launch
-# (64 FP32 vectors per row) on the 4-flake case of the same workload: 1,070,628,096 bytes over
-# 1,362,158 rows (ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum, one launch)
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the FP32 step with 64 vectors per
+# row on the 4-flake case of the same workload: 1,070,628,096 bytes over 1,362,158 rows for
+# diag_step_kernel<float,4,16> (chained FMAs); diag_step_cr_kernel<float,4,16> (compensated rows,
+# the same loads and stores) measured 1,070,174,464 (ncu, one launch each)
 DIAG_STEP_DRAM_BYTES_PER_ROW = 1070628096.0 / 1362158
 
 
