@@ -22,7 +22,9 @@ def test_reference_arm_prints_one_contract_line():
                 "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
         assert key in d, key
     assert d["impl"] == "reference"
-    assert d["metric"] == json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"]
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
     assert d["value"] > 0 and d["higher_is_better"] is True
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1
